@@ -1,0 +1,342 @@
+"""Benchmark of the MMSB tensor-method pipeline on GB300.
+
+Workload (the GPU-at-scale configuration of the reference path): synthetic MMSB
+graph with n = 200,000 nodes in four equal random partitions, k = 100,
+alpha0 = 0.1, B = 0.05 on the diagonal and 5e-4 off it, int32 CSR; FP32
+whitening (Gaussian sketch panels), online STPM for 20 sweeps with minibatch
+4,096 and beta_t = 1/(1+t), then unwhitening + normalisation + community sets.
+
+One step = one full pass of the pipeline (whitening, whitened data, 20 STPM
+sweeps, unwhitening) over the resident graph.  value = STPM node-updates per
+second of the whole job (n_X * sweeps per step / step time).  e2e = the same
+through the public C ABI with host buffers: graph upload (H2D), run, Pi and
+lambda download (D2H) inside the timed region.
+
+--impl reference times the FP64 CPU restatement of the reference path
+(oracle/mmsb_oracle.py) on the host cores on a bounded sample of the same
+workload; its node-updates/s are extrapolated from measured whitening and
+per-sweep times.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+
+WORKLOAD = dict(name="mmsb-n200k-k100-fp32-online", n=200_000, k=100, alpha0=0.1, p_in=0.05,
+                p_out=5e-4, sweeps=20, minibatch=4096, seed=0)
+
+
+def load_pkg():
+    sys.path.insert(0, str(ROOT))
+    import __graft_entry__ as ge
+    return ge._package()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Host-side barrier and max-reduction over replicas (gloo, CPU tensors)."""
+
+    def __init__(self, ws):
+        self.ws = ws
+        self.dist = None
+        if ws > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v):
+        if not self.dist:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index, out_path=None):
+        self.gpu = gpu_index
+        self.out_path = out_path
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        if self.out_path:
+            Path(self.out_path).write_text("\n".join(self.lines) + "\n")
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_graph(mm, wl):
+    return mm.generate(wl["n"], wl["k"], wl["alpha0"], wl["p_in"], wl["p_out"], wl["seed"])
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+
+def cpu_port_sample(mm, wl, graph=None, max_seconds=30.0):
+    """Times the FP64 oracle port on host cores: whitening once, STPM sweeps
+    until the time budget, unwhitening once; returns node-updates/s of the
+    full workload extrapolated from those measured parts."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import mmsb_oracle as O
+    if graph is None:
+        graph = make_graph(mm, wl)
+    Gxa, Gxb, Gxc, Gba, Gca = graph.scipy_blocks()
+    k, a0 = wl["k"], wl["alpha0"]
+    rng = np.random.default_rng(0)
+    nX, nA, nB, nC = graph.parts
+    sk = (rng.standard_normal((nB, 2 * k)), rng.standard_normal((nC, 2 * k)),
+          rng.standard_normal((nA, 2 * k)))
+    t0 = time.perf_counter()
+    wh = O.second_whiten(Gxa, Gxb, Gxc, k, a0, sk)
+    y = O.whitened_data(Gxa, Gxb, Gxc, wh)
+    t_whiten = time.perf_counter() - t0
+    phi = O.polar(rng.standard_normal((k, k)))
+    batches = O.stpm_minibatches(nX, wl["minibatch"])
+    p0, p1, p2 = O.alpha_coeffs(a0)
+    t1 = time.perf_counter()
+    steps = 0
+    budget = max(1.0, max_seconds - t_whiten)
+    for t, nodes in enumerate(batches):
+        beta = 1.0 / (1.0 + t)
+        S = phi.T @ phi
+        step = 3.0 * (phi @ (S * S)) - 3.0 * O.online_grad_terms(phi, y, nodes, a0)
+        phi = O.polar(phi - beta * step)
+        steps += 1
+        if time.perf_counter() - t1 > budget:
+            break
+    t_steps = time.perf_counter() - t1
+    t_sweep = t_steps / steps * len(batches)
+    t2 = time.perf_counter()
+    lam = O.tensor_values(phi, y, a0)
+    O.postprocess(Gxa, Gba, Gca, wh, lam, phi)
+    t_post = time.perf_counter() - t2
+    total = t_whiten + wl["sweeps"] * t_sweep + t_post
+    nu = nX * wl["sweeps"] / total
+    sample = (f"FP64 numpy/scipy port: whitening {t_whiten:.2f}s, {steps} of {len(batches)} "
+              f"minibatch steps of one sweep {t_steps:.2f}s, post {t_post:.2f}s; "
+              f"extrapolated to {wl['sweeps']} sweeps = {total:.1f}s per step")
+    return nu, sample, total
+
+
+def run_reference(args, wl, ws, rank):
+    if rank != 0:
+        return
+    mm = load_pkg()
+    graph = make_graph(mm, wl)
+    vals = []
+    sample = ""
+    for i in range(args.warmup + args.steps):
+        nu, sample, total = cpu_port_sample(mm, wl, graph, max_seconds=args.cpu_seconds)
+        if i >= args.warmup:
+            vals.append(nu)
+        if args.warmup + args.steps > 2 and i == 0 and total > 0:
+            pass
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": "stpm_node_updates_per_s", "value": v,
+            "unit": "node-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": wl["n"] // 4 * wl["sweeps"] / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl["name"], **{k: wl[k] for k in wl if k != "name"}},
+            "cpu_baseline": {"value": v, "unit": "node-updates/s", "cores": os.cpu_count(),
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "node-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, wl, ws, rank, local):
+    mm = load_pkg()
+    dist = Dist(ws)
+    graph = make_graph(mm, wl)
+    nX = graph.parts[0]
+    cfg = mm.default_config(k=wl["k"], alpha0=wl["alpha0"], stpm_method=mm.STPM_ONLINE,
+                            sweeps=wl["sweeps"], minibatch=wl["minibatch"], seed=wl["seed"],
+                            device=local, tau=0.1)
+    p = mm.Pipeline(cfg)
+    p.upload(graph)
+    for _ in range(args.warmup):
+        p.run()
+    p.synchronize()
+    dist.barrier()
+    clocks = ClockSampler(local, ROOT / "gpurun_out" / "clocks.csv"
+                          if (ROOT / "gpurun_out").is_dir() else None)
+    clocks.start()
+    dev_ms, spmm_ms, spmm_bytes, spmm_launch, launches = [], 0.0, 0.0, 0, 0
+    stage = {"whiten_ms": 0.0, "stpm_ms": 0.0, "post_ms": 0.0}
+    t_host0 = time.perf_counter()
+    for _ in range(args.steps):
+        p.flush_l2()
+        p.synchronize()
+        p.run()
+        st = p.stats()
+        dev_ms.append(st["total_ms"])
+        for key in stage:
+            stage[key] += st[key]
+        spmm_ms += st["spmm_ms"]
+        spmm_bytes += st["spmm_bytes"]
+        spmm_launch += st["spmm_launches"]
+        launches += st["kernel_launches"]
+    p.synchronize()
+    t_host = time.perf_counter() - t_host0
+    dist.barrier()
+    clk = clocks.stop()
+    step_ms = dist.max(sum(dev_ms) / len(dev_ms))
+    nu_per_rank = nX * wl["sweeps"] / (step_ms / 1e3)
+    value = nu_per_rank * ws
+
+    # e2e: upload from host buffers + run + Pi/lambda download, host wall clock
+    h2d = sum(b.row_ptr.nbytes + b.col_idx.nbytes for b in graph.blocks)
+    d2h = graph.n_nodes * wl["k"] * 4 + wl["k"] * 8
+    e2e_ms = []
+    for _ in range(max(1, min(args.steps, 3))):
+        p.flush_l2()
+        p.synchronize()
+        dist.barrier()
+        t0 = time.perf_counter()
+        p.upload(graph)
+        p.run()
+        pi = p.pi()
+        lam = p.lam()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_step = dist.max(statistics.median(e2e_ms))
+    e2e_value = nX * wl["sweeps"] / (e2e_step / 1e3) * ws
+
+    peak, peak_kind = peaks()
+    achieved = (spmm_bytes / max(spmm_ms, 1e-9) / 1e6) if spmm_ms > 0 else None
+    line = {
+        "metric": "stpm_node_updates_per_s", "value": value, "unit": "node-updates/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": wl["name"], "n": wl["n"], "k": wl["k"], "alpha0": wl["alpha0"],
+                   "p_in": wl["p_in"], "p_out": wl["p_out"], "sweeps": wl["sweeps"],
+                   "minibatch": wl["minibatch"], "seed": wl["seed"], "nnz_directed": sum(
+                       b.nnz for b in graph.blocks[:3]) * 2,
+                   "l2": "256 MiB buffer written between timed steps",
+                   "parallelism": f"replicas{ws}"},
+        "stages_ms_per_step": {k_: v / args.steps for k_, v in stage.items()},
+        "host_wall_ms_per_step": t_host * 1e3 / args.steps,
+        "e2e": {"value": e2e_value, "unit": "node-updates/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_step},
+        "gpu_launches": launches,
+        "roofline": {"kernel": "spmm_rows_kernel (whitening SpMM)", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "peak_source": peak_kind, "launches_per_step": spmm_launch / args.steps,
+                     "algorithmic_bytes_per_step": spmm_bytes / args.steps},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        nu, sample, _ = cpu_port_sample(mm, wl, graph, max_seconds=args.cpu_seconds)
+        line["cpu_baseline"] = {"value": nu, "unit": "node-updates/s", "cores": os.cpu_count(),
+                                "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    p.close()
+    dist.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n", type=int, default=None, help="override node count (testing)")
+    args = ap.parse_args()
+    wl = dict(WORKLOAD)
+    if args.n:
+        wl["n"] = args.n
+        wl["name"] += f"-n{args.n}"
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, wl, ws, rank)
+    else:
+        run_ours(args, wl, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,487 @@
+"""Python host mirror of the GB300 MMSB tensor-method library (include/mmsb.h).
+
+The product is the C ABI in ``lib/libmmsb.so`` (host C++ + sm_103a CUDA
+kernels).  This module binds it with ctypes and mirrors the reference's
+interface for the path:
+
+  reference                                          here
+  -------------------------------------------------  ---------------------------
+  second_whiten(Gx_a, Gx_b, Gx_c, W, Z_B_part1, ...)  Pipeline.whiten / second_whiten
+    (CommunityDetectionSoftware_CPU/.../Util.cpp:38)
+  tensorDecom_alpha0(D_a, D_a_mu, ..., lambda, phi)   Pipeline.stpm / tensor_decom_alpha0
+    (Util.cpp:131)
+  main() post-processing + normProbMatrix             Pipeline.postproc
+    (CommunityDetection.cpp:89-139)
+  read_G_sparse / write_pi (IOfn.cpp:21, 57)          read_coo / write_triplets
+
+There is no CPU fallback: if the shared library is missing, importing works but
+every call raises ``LibraryNotBuilt``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "lib" / "libmmsb.so"
+CSRC = PKG_DIR / "csrc"
+
+OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory",
+          4: "call out of order", 5: "numerical failure", 6: "stopped on request",
+          7: "I/O error", 8: "device wait timed out", 9: "unsupported configuration"}
+
+BLOCK_XA, BLOCK_XB, BLOCK_XC, BLOCK_BA, BLOCK_CA = range(5)
+STPM_BATCH_POWER, STPM_ONLINE, STPM_ADJOINT = range(3)
+PREC_FP32, PREC_BF16 = range(2)
+
+
+class LibraryNotBuilt(RuntimeError):
+    pass
+
+
+class MmsbError(RuntimeError):
+    def __init__(self, status, msg=""):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("k", ctypes.c_int32), ("alpha0", ctypes.c_double),
+                ("datatype", ctypes.c_int32), ("stpm_method", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("sweeps", ctypes.c_int32),
+                ("minibatch", ctypes.c_int32), ("lr0", ctypes.c_double),
+                ("theta", ctypes.c_double), ("min_iter", ctypes.c_int32),
+                ("max_iter", ctypes.c_int32), ("tol", ctypes.c_double),
+                ("pinv_tol", ctypes.c_double), ("nystrom_rows_factor", ctypes.c_int32),
+                ("normalize", ctypes.c_int32), ("seed", ctypes.c_uint64),
+                ("tau", ctypes.c_float), ("device", ctypes.c_int32)]
+
+
+class Csr(ctypes.Structure):
+    _fields_ = [("n_rows", ctypes.c_int64), ("n_cols", ctypes.c_int64), ("nnz", ctypes.c_int64),
+                ("row_ptr", ctypes.POINTER(ctypes.c_int64)),
+                ("col_idx", ctypes.POINTER(ctypes.c_int32)),
+                ("val", ctypes.POINTER(ctypes.c_float))]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("whiten_ms", ctypes.c_double), ("ydata_ms", ctypes.c_double),
+                ("stpm_ms", ctypes.c_double), ("post_ms", ctypes.c_double),
+                ("total_ms", ctypes.c_double), ("spmm_ms", ctypes.c_double),
+                ("spmm_bytes", ctypes.c_double), ("spmm_launches", ctypes.c_int64),
+                ("stpm_steps", ctypes.c_int64), ("node_updates", ctypes.c_int64),
+                ("stpm_last_error", ctypes.c_double), ("kernel_launches", ctypes.c_int64),
+                ("polar_iterations", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class GenParams(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("k", ctypes.c_int32), ("alpha0", ctypes.c_double),
+                ("p_in", ctypes.c_double), ("p_out", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("keep_pi", ctypes.c_int32)]
+
+
+_lib = None
+
+_P = ctypes.c_void_p
+_D = ctypes.POINTER(ctypes.c_double)
+_F = ctypes.POINTER(ctypes.c_float)
+_SIGS = {
+    "mmsb_config_default": (None, [ctypes.POINTER(Config)]),
+    "mmsb_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(_P)]),
+    "mmsb_destroy": (None, [_P]),
+    "mmsb_upload_graph": (ctypes.c_int, [_P, ctypes.POINTER(Csr)]),
+    "mmsb_whiten": (ctypes.c_int, [_P, ctypes.POINTER(_D)]),
+    "mmsb_stpm": (ctypes.c_int, [_P, _D]),
+    "mmsb_postproc": (ctypes.c_int, [_P]),
+    "mmsb_run": (ctypes.c_int, [_P]),
+    "mmsb_num_nodes": (ctypes.c_int64, [_P]),
+    "mmsb_get_pi": (ctypes.c_int, [_P, _F]),
+    "mmsb_get_sets": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
+    "mmsb_get_lambda": (ctypes.c_int, [_P, _D]),
+    "mmsb_get_phi": (ctypes.c_int, [_P, _D]),
+    "mmsb_get_whitening": (ctypes.c_int, [_P, _D, _D, _D, _D, _D]),
+    "mmsb_get_means": (ctypes.c_int, [_P, _D, _D, _D]),
+    "mmsb_get_whitened": (ctypes.c_int, [_P, _F, _F, _F, _D, _D, _D]),
+    "mmsb_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
+    "mmsb_set_whitening": (ctypes.c_int, [_P, _D, _D, _D, _D, _D, _D, _D, _D]),
+    "mmsb_set_whitened": (ctypes.c_int, [_P, _D, _D, _D, _D, _D, _D]),
+    "mmsb_set_phi_lambda": (ctypes.c_int, [_P, _D, _D]),
+    "mmsb_stpm_loss_fwd": (ctypes.c_int, [_P, _D, ctypes.c_int64, ctypes.c_int64, _D]),
+    "mmsb_stpm_loss_bwd": (ctypes.c_int, [_P, _D, ctypes.c_int64, ctypes.c_int64, _D]),
+    "mmsb_request_stop": (None, [_P]),
+    "mmsb_last_error": (ctypes.c_char_p, [_P]),
+    "mmsb_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "mmsb_flush_l2": (ctypes.c_int, [_P]),
+    "mmsb_synchronize": (ctypes.c_int, [_P]),
+    "mmsb_op_spmm": (ctypes.c_int, [ctypes.POINTER(Csr), ctypes.c_int, _F, ctypes.c_int64,
+                                    ctypes.c_float, _F]),
+    "mmsb_op_symeig": (ctypes.c_int, [_D, ctypes.c_int32, _D, _D]),
+    "mmsb_generate": (ctypes.c_int, [ctypes.POINTER(GenParams), ctypes.POINTER(_P)]),
+    "mmsb_host_graph_free": (None, [_P]),
+    "mmsb_host_graph_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64),
+                                            ctypes.POINTER(ctypes.c_int64)]),
+    "mmsb_host_graph_block": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(Csr)]),
+    "mmsb_host_graph_pi": (ctypes.c_int, [_P, _F]),
+    "mmsb_read_coo": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int64, ctypes.c_int64,
+                                     ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_P)]),
+    "mmsb_write_triplets_f32": (ctypes.c_int, [ctypes.c_char_p, _F, ctypes.c_int64,
+                                               ctypes.c_int64]),
+    "mmsb_write_triplets_f64": (ctypes.c_int, [ctypes.c_char_p, _D, ctypes.c_int64,
+                                               ctypes.c_int64]),
+}
+
+
+def build(jobs: int = 8, quiet: bool = True) -> Path:
+    """Compile lib/libmmsb.so for sm_103a (nvcc + g++, in-tree)."""
+    out = subprocess.run(["make", "-C", str(CSRC), f"-j{jobs}"], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("libmmsb build failed:\n" + out.stdout[-4000:] + out.stderr[-4000:])
+    if not quiet:
+        print(out.stdout)
+    return LIB_PATH
+
+
+def lib():
+    """The loaded C library; raises LibraryNotBuilt if lib/libmmsb.so is absent."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise LibraryNotBuilt(f"{LIB_PATH} is missing: run build() first (no CPU fallback)")
+        L = ctypes.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def _check(st, ctx=None):
+    if st != OK:
+        msg = lib().mmsb_last_error(ctx).decode() if ctx is not None else ""
+        raise MmsbError(st, msg)
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_D) if a is not None else None
+
+
+def _fptr(a):
+    return a.ctypes.data_as(_F) if a is not None else None
+
+
+def default_config(**kw) -> Config:
+    c = Config()
+    lib().mmsb_config_default(ctypes.byref(c))
+    for k_, v in kw.items():
+        if not hasattr(c, k_):
+            raise KeyError(k_)
+        setattr(c, k_, v)
+    return c
+
+
+# ---- host graphs -------------------------------------------------------------
+
+class CsrBlock:
+    """Host CSR block (numpy arrays; int64 row offsets, int32 columns)."""
+
+    def __init__(self, n_rows, n_cols, row_ptr, col_idx, val=None):
+        self.n_rows, self.n_cols = int(n_rows), int(n_cols)
+        self.row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+        self.col_idx = np.ascontiguousarray(col_idx, dtype=np.int32)
+        self.val = None if val is None else np.ascontiguousarray(val, dtype=np.float32)
+
+    @property
+    def nnz(self):
+        return int(self.col_idx.size)
+
+    def ctype(self) -> Csr:
+        c = Csr()
+        c.n_rows, c.n_cols, c.nnz = self.n_rows, self.n_cols, self.nnz
+        c.row_ptr = self.row_ptr.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        c.col_idx = self.col_idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        c.val = self.val.ctypes.data_as(_F) if self.val is not None else None
+        return c
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        v = self.val if self.val is not None else np.ones(self.nnz)
+        return sp.csr_matrix((v.astype(np.float64), self.col_idx, self.row_ptr),
+                             shape=(self.n_rows, self.n_cols))
+
+    @staticmethod
+    def from_scipy(m):
+        m = m.tocsr()
+        m.sort_indices()
+        vals = None if np.all(m.data == 1) else m.data
+        return CsrBlock(m.shape[0], m.shape[1], m.indptr, m.indices, vals)
+
+
+class Graph:
+    """The five adjacency blocks X->A, X->B, X->C, B->A, C->A plus metadata."""
+
+    def __init__(self, blocks, parts, n_edges=None, pi=None):
+        self.blocks = list(blocks)
+        self.parts = tuple(int(p) for p in parts)
+        self.n_edges = n_edges
+        self.pi = pi
+
+    @property
+    def n_nodes(self):
+        return sum(self.parts)
+
+    def scipy_blocks(self):
+        return [b.to_scipy() for b in self.blocks]
+
+
+def generate(n, k, alpha0, p_in, p_out, seed=0, keep_pi=False) -> Graph:
+    """Seeded synthetic MMSB graph (C++ generator in the library)."""
+    L = lib()
+    h = _P()
+    _check(L.mmsb_generate(ctypes.byref(GenParams(n, k, alpha0, p_in, p_out, seed,
+                                                  int(keep_pi))), ctypes.byref(h)))
+    try:
+        parts = (ctypes.c_int64 * 4)()
+        ne = ctypes.c_int64()
+        _check(L.mmsb_host_graph_info(h, parts, ctypes.byref(ne)))
+        blocks = []
+        for b in range(5):
+            c = Csr()
+            _check(L.mmsb_host_graph_block(h, b, ctypes.byref(c)))
+            rp = np.ctypeslib.as_array(c.row_ptr, (c.n_rows + 1,)).copy()
+            ci = (np.ctypeslib.as_array(c.col_idx, (c.nnz,)).copy() if c.nnz
+                  else np.zeros(0, np.int32))
+            blocks.append(CsrBlock(c.n_rows, c.n_cols, rp, ci))
+        pi = None
+        if keep_pi:
+            pi = np.zeros((n, k), dtype=np.float32)
+            _check(L.mmsb_host_graph_pi(h, _fptr(pi)))
+        return Graph(blocks, list(parts), ne.value, pi)
+    finally:
+        L.mmsb_host_graph_free(h)
+
+
+def read_coo(path, n_rows, n_cols, datatype=0, compat=False) -> CsrBlock:
+    """read_G_sparse (IOfn.cpp:21-54); compat=True reproduces its quirks."""
+    L = lib()
+    h = _P()
+    _check(L.mmsb_read_coo(str(path).encode(), n_rows, n_cols, datatype, int(compat),
+                           ctypes.byref(h)))
+    try:
+        c = Csr()
+        _check(L.mmsb_host_graph_block(h, 0, ctypes.byref(c)))
+        rp = np.ctypeslib.as_array(c.row_ptr, (c.n_rows + 1,)).copy()
+        ci = np.ctypeslib.as_array(c.col_idx, (c.nnz,)).copy() if c.nnz else np.zeros(0, np.int32)
+        val = np.ctypeslib.as_array(c.val, (c.nnz,)).copy() if (c.val and c.nnz) else None
+        return CsrBlock(c.n_rows, c.n_cols, rp, ci, val)
+    finally:
+        L.mmsb_host_graph_free(h)
+
+
+def write_triplets(path, m):
+    """write_pi (IOfn.cpp:57-67): 1-based row/col/value of the nonzeros."""
+    m = np.asfortranarray(m)
+    if m.dtype == np.float32:
+        _check(lib().mmsb_write_triplets_f32(str(path).encode(), m.ctypes.data_as(_F),
+                                              m.shape[0], m.shape[1]))
+    else:
+        m = np.asfortranarray(m, dtype=np.float64)
+        _check(lib().mmsb_write_triplets_f64(str(path).encode(), m.ctypes.data_as(_D),
+                                              m.shape[0], m.shape[1]))
+
+
+# ---- the pipeline ---------------------------------------------------------------
+
+class Pipeline:
+    """One GPU context: upload -> whiten -> stpm -> postproc (host numpy in/out)."""
+
+    def __init__(self, config: Config | None = None, **kw):
+        self.cfg = config if config is not None else default_config(**kw)
+        h = _P()
+        _check(lib().mmsb_create(ctypes.byref(self.cfg), ctypes.byref(h)))
+        self._h = h
+        self.k = self.cfg.k
+        self.parts = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mmsb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, st):
+        _check(st, self._h)
+
+    def upload(self, graph: Graph):
+        arr = (Csr * 5)(*[b.ctype() for b in graph.blocks])
+        self._keep = graph
+        self._ck(lib().mmsb_upload_graph(self._h, arr))
+        self.parts = graph.parts
+        return self
+
+    def whiten(self, sketches=None):
+        if sketches is None:
+            self._ck(lib().mmsb_whiten(self._h, None))
+        else:
+            sk = [np.asfortranarray(s, dtype=np.float64) for s in sketches]
+            arr = (_D * 3)(*[_dptr(s) for s in sk])
+            self._ck(lib().mmsb_whiten(self._h, arr))
+        return self
+
+    def stpm(self, phi0=None):
+        p = None if phi0 is None else np.asfortranarray(phi0, dtype=np.float64)
+        self._ck(lib().mmsb_stpm(self._h, _dptr(p)))
+        return self
+
+    def postproc(self):
+        self._ck(lib().mmsb_postproc(self._h))
+        return self
+
+    def run(self):
+        self._ck(lib().mmsb_run(self._h))
+        return self
+
+    def synchronize(self):
+        self._ck(lib().mmsb_synchronize(self._h))
+
+    def flush_l2(self):
+        self._ck(lib().mmsb_flush_l2(self._h))
+
+    def request_stop(self):
+        lib().mmsb_request_stop(self._h)
+
+    # results
+    def n_nodes(self):
+        return int(lib().mmsb_num_nodes(self._h))
+
+    def pi(self):
+        out = np.zeros((self.k, self.n_nodes()), dtype=np.float32, order="F")
+        self._ck(lib().mmsb_get_pi(self._h, _fptr(out)))
+        return out
+
+    def sets(self):
+        words = (self.k + 31) // 32
+        out = np.zeros((self.n_nodes(), words), dtype=np.uint32)
+        self._ck(lib().mmsb_get_sets(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
+        bits = np.unpackbits(out.view(np.uint8), axis=1, bitorder="little")[:, :self.k]
+        return bits.T.astype(bool)
+
+    def lam(self):
+        out = np.zeros(self.k)
+        self._ck(lib().mmsb_get_lambda(self._h, _dptr(out)))
+        return out
+
+    def phi(self):
+        out = np.zeros((self.k, self.k), order="F")
+        self._ck(lib().mmsb_get_phi(self._h, _dptr(out)))
+        return out
+
+    def whitening(self):
+        nX, nA, nB, nC = self.parts
+        k = self.k
+        W, zb1, zc1 = (np.zeros((nA, k), order="F") for _ in range(3))
+        zb2 = np.zeros((k, nB), order="F")
+        zc2 = np.zeros((k, nC), order="F")
+        self._ck(lib().mmsb_get_whitening(self._h, _dptr(W), _dptr(zb1), _dptr(zb2), _dptr(zc1),
+                                          _dptr(zc2)))
+        mu = [np.zeros(n) for n in (nA, nB, nC)]
+        self._ck(lib().mmsb_get_means(self._h, *[_dptr(m) for m in mu]))
+        return dict(W=W, Zb1=zb1, Zb2=zb2, Zc1=zc1, Zc2=zc2, mu_a=mu[0], mu_b=mu[1], mu_c=mu[2])
+
+    def whitened(self):
+        nX = self.parts[0]
+        k = self.k
+        ys = [np.zeros((k, nX), dtype=np.float32, order="F") for _ in range(3)]
+        ms = [np.zeros(k) for _ in range(3)]
+        self._ck(lib().mmsb_get_whitened(self._h, *[_fptr(y) for y in ys], *[_dptr(m) for m in ms]))
+        return dict(Da=ys[0], Db=ys[1], Dc=ys[2], Da_mu=ms[0], Db_mu=ms[1], Dc_mu=ms[2])
+
+    def stats(self):
+        s = Stats()
+        self._ck(lib().mmsb_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+    # stage inputs
+    def set_whitening(self, wh):
+        arrs = [np.asfortranarray(wh[n], dtype=np.float64)
+                for n in ("W", "Zb1", "Zb2", "Zc1", "Zc2", "mu_a", "mu_b", "mu_c")]
+        self._ck(lib().mmsb_set_whitening(self._h, *[_dptr(a) for a in arrs]))
+        return self
+
+    def set_whitened(self, y):
+        arrs = [np.asfortranarray(y[n], dtype=np.float64)
+                for n in ("Da", "Db", "Dc", "Da_mu", "Db_mu", "Dc_mu")]
+        self._ck(lib().mmsb_set_whitened(self._h, *[_dptr(a) for a in arrs]))
+        return self
+
+    def set_phi_lambda(self, phi, lam):
+        p = np.asfortranarray(phi, dtype=np.float64)
+        l_ = np.ascontiguousarray(lam, dtype=np.float64)
+        self._ck(lib().mmsb_set_phi_lambda(self._h, _dptr(p), _dptr(l_)))
+        return self
+
+    # adjoint form
+    def loss(self, phi, begin=0, count=0):
+        p = np.asfortranarray(phi, dtype=np.float64)
+        out = ctypes.c_double()
+        self._ck(lib().mmsb_stpm_loss_fwd(self._h, _dptr(p), begin, count, ctypes.byref(out)))
+        return out.value
+
+    def loss_grad(self, phi, begin=0, count=0):
+        p = np.asfortranarray(phi, dtype=np.float64)
+        out = np.zeros((self.k, self.k), order="F")
+        self._ck(lib().mmsb_stpm_loss_bwd(self._h, _dptr(p), begin, count, _dptr(out)))
+        return out
+
+
+# ---- reference-named convenience wrappers ----------------------------------------
+
+def second_whiten(graph: Graph, k, alpha0, sketches=None, **cfg):
+    """second_whiten (Util.cpp:38-127) on the GPU; returns W, Z parts and means."""
+    with Pipeline(k=k, alpha0=alpha0, **cfg) as p:
+        p.upload(graph).whiten(sketches)
+        return p.whitening()
+
+
+def spmm(block: CsrBlock, P, transpose=False, alpha=1.0):
+    """Y = alpha * G P (or G^T P) through the library's CSR SpMM kernel."""
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    n_out = block.n_cols if transpose else block.n_rows
+    Y = np.zeros((n_out, P.shape[1]), dtype=np.float32)
+    c = block.ctype()
+    _check(lib().mmsb_op_spmm(ctypes.byref(c), int(transpose), _fptr(P), P.shape[1], alpha,
+                              _fptr(Y)))
+    return Y
+
+
+def symeig(A):
+    """Eigen-pairs (descending) of a symmetric positive semi-definite matrix."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    n = A.shape[0]
+    ev = np.zeros(n)
+    V = np.zeros((n, n), order="F")
+    _check(lib().mmsb_op_symeig(_dptr(A), n, _dptr(ev), _dptr(V)))
+    return ev, V

@@ -1,0 +1,126 @@
+// Shared declarations of the device kernels (launchers) and small helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#define MMSB_CUDA_TRY(expr)                       \
+  do {                                            \
+    cudaError_t e_ = (expr);                      \
+    if (e_ != cudaSuccess) return e_;             \
+  } while (0)
+
+namespace mmsb {
+
+constexpr int kNumSMs = 152;
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
+
+// Device-side status word shared by kernels that can fail (non-finite
+// values, bounded waits).  Bit flags, OR-ed with atomicOr.
+enum DeviceFlag : unsigned {
+  kFlagNonFinite = 1u,
+  kFlagCholeskyBreakdown = 2u,
+  kFlagNoConvergence = 4u,
+  kFlagTimeout = 8u,
+};
+
+// Counts launches of this library's kernels (reported in mmsb_stats).
+extern thread_local int64_t g_launch_count;
+
+// ---- sparse (k_sparse.cu) ---------------------------------------------------
+
+// Y[n_rows x ld] (row-major) = alpha * G * P[n_cols x ld]; ld % 4 == 0.
+cudaError_t spmm_f32(const int64_t* rp, const int32_t* ci, const float* val, int64_t n_rows,
+                     const float* P, int ld, float alpha, float* Y, cudaStream_t s);
+// Transposed CSR (deterministic: columns sorted within each row).
+cudaError_t csr_transpose(const int64_t* rp, const int32_t* ci, const float* val, int64_t n_rows,
+                          int64_t n_cols, int64_t nnz, int64_t* rpT, int32_t* ciT, float* valT,
+                          int32_t* scratch_cnt, cudaStream_t s);
+// out[r] = scale * sum of row r of G (row count for binary)
+cudaError_t row_sums_f64(const int64_t* rp, const float* val, int64_t n_rows, double scale,
+                         double* out, cudaStream_t s);
+
+// Fused unwhitening + normProbMatrix + threshold over one CSR block:
+// raw[r,:] = G[r,:] * P (ld = ldp, first k columns), normalised per row,
+// written to pi[(row_offset + r) * k + i] and set bits.
+cudaError_t unwhiten_normprob(const int64_t* rp, const int32_t* ci, const float* val,
+                              int64_t n_rows, const float* P, int ldp, int k, float tau,
+                              int64_t row_offset, float* pi, uint32_t* bits, cudaStream_t s);
+
+// ---- dense (k_dense.cu) -----------------------------------------------------
+
+// S[pa x pb] (column-major FP64) = alpha * A^T B, A: n x pa (lda), B: n x pb (ldb),
+// row-major FP32; FP32 partial sums over row chunks, FP64 across chunks.
+cudaError_t gram_tsk(const float* A, int lda, int pa, const float* B, int ldb, int pb, int64_t n,
+                     double alpha, double* S, double* partials, int64_t partials_cap,
+                     cudaStream_t s);
+size_t gram_tsk_partials(int64_t n, int pa, int pb);
+// Y[n x ldy] (row-major FP32) = M[n x ldm] (first p cols) * F (p x q, column-major FP64, ldf);
+// columns q..ldy-1 of Y are zeroed.
+cudaError_t panel_times_small(const float* M, int ldm, int p, int64_t n, const double* F, int ldf,
+                              int q, float* Y, int ldy, cudaStream_t s);
+// C (m x n) = alpha * op(A) op(B) + beta * C, FP64 column-major, small sizes.
+cudaError_t dgemm_small(bool ta, bool tb, int m, int n, int k, double alpha, const double* A,
+                        int lda, const double* B, int ldb, double beta, double* C, int ldc,
+                        cudaStream_t s);
+// Upper Cholesky S = R^T R with drop tolerance: a pivot <= drop2 zeroes row j of R.
+cudaError_t chol_upper_drop(int p, const double* S, int lds, double* R, double drop2,
+                            unsigned* flags, cudaStream_t s);
+// T = R^{-1} for upper triangular R (rows with R_jj == 0 -> zero rows/cols of T).
+cudaError_t trinv_upper(int p, const double* R, double* T, cudaStream_t s);
+// Eigen-decomposition of Z = Y Y^T from Y (p x p, column-major FP64): one-sided
+// Jacobi on Y; eigenvalues descending, eigenvectors column-major p x p.
+cudaError_t eig_from_factor(int p, const double* Y, double* evals, double* evecs,
+                            float* work, unsigned* flags, cudaStream_t s);
+// Modified Gram-Schmidt of the columns of an m x p FP64 matrix (reference drop rule).
+cudaError_t mgs_cols(int m, int p, const double* P, int ldp, double* Q, int ldq, double tol,
+                     cudaStream_t s);
+// Ogita-Aishima eigen refinement pieces (see k_dense.cu).
+cudaError_t oa_correction(int n, const double* A, const double* XtX, const double* S, double* E,
+                          double* lam, cudaStream_t s);
+cudaError_t sort_eigen(int n, const double* lam, const double* X, double* evals, double* evecs,
+                       cudaStream_t s);
+cudaError_t panel_set_col(float* P, int ld, int64_t rows, int col, const double* v,
+                          cudaStream_t s);
+cudaError_t panel_copy(const float* src, int lds, int64_t rows, int q, float* dst, int ldd,
+                       cudaStream_t s);
+// Philox-4x32-10 standard normal panel, row-major n x ld (first q columns).
+cudaError_t gaussian_panel(float* P, int64_t n, int q, int ld, uint64_t seed, uint64_t stream,
+                           cudaStream_t s);
+// Column-major FP64 (rows x cols, ld) <-> row-major FP32 panel conversions.
+cudaError_t colmajor64_to_panel(const double* A, int64_t rows, int cols, int64_t lda, float* P,
+                                int ldp, cudaStream_t s);
+cudaError_t panel_to_colmajor64(const float* P, int ldp, int64_t rows, int cols, double* A,
+                                int64_t lda, cudaStream_t s);
+// Scale columns: P[:, j] *= d[j] (row-major panel, FP64 factors).
+cudaError_t panel_scale_cols(float* P, int ldp, int64_t n, int q, const double* d,
+                             cudaStream_t s);
+cudaError_t fill_f32(float* p, int64_t n, float v, cudaStream_t s);
+cudaError_t fill_f64(double* p, int64_t n, double v, cudaStream_t s);
+// dst[j] = src[j] (FP64 vector ops on device, tiny)
+cudaError_t axpy_f64(int64_t n, double a, const double* x, double* y, cudaStream_t s);
+
+// ---- small element-wise helpers (k_misc.cu) -----------------------------------
+
+cudaError_t sig_from_evals(int k, const double* ev, double* sig, cudaStream_t s);
+cudaError_t scale_cols_pinv(int rows, int k, double* F, int ldf, const double* sig, double tol,
+                            cudaStream_t s);
+cudaError_t sqrt_pinv(int k, const double* sig, double tol, double* a, double* b, cudaStream_t s);
+cudaError_t diag_guard(int k, double* core, cudaStream_t s);
+cudaError_t panel_rank1(float* P, int ld, int64_t n, int q, double alpha, const double* u,
+                        const double* v, cudaStream_t s);
+cudaError_t f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
+cudaError_t f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t s);
+cudaError_t phi_scaled(int k, const float* phi, const double* lambda, double tol, double* F,
+                       cudaStream_t s);
+cudaError_t transpose_f64(int p, const double* A, double* At, cudaStream_t s);
+cudaError_t cube_sum(int n, const double* S, double a, double* out, cudaStream_t s);
+cudaError_t hadamard_square(int64_t n, const double* a, double* b, cudaStream_t s);
+cudaError_t mask_cols(int rows, int k, double* F, int ldf, const double* sig, double tol,
+                      cudaStream_t s);
+cudaError_t set_row_scaled(int rows, int cols, double* B, int ldb, int row, double alpha,
+                           const double* v, cudaStream_t s);
+cudaError_t eye_mask(int m, int p, const double* R, int ldr, double* Q, int ldq, cudaStream_t s);
+
+}  // namespace mmsb

@@ -1,0 +1,768 @@
+// Dense kernels of the whitening chain: tall-skinny Gram products (FP32
+// partial sums, FP64 across row chunks), tall-skinny x small products, small
+// FP64 GEMMs, upper Cholesky with the modified-Gram-Schmidt drop rule, upper
+// triangular inverse, one-sided Jacobi eigen-solver, and the Philox Gaussian
+// sketch panel.
+//
+// Why FP64 only on p x p data: GB300's FP64 rate is ~1/64 of its FP32 rate,
+// so every n-sized product stays FP32 and only the p x p factors (p = 2k <= 512)
+// are FP64.
+#include "common.cuh"
+
+#include <algorithm>
+
+namespace mmsb {
+
+namespace {
+
+// ---- tall-skinny Gram: S = alpha * A^T B --------------------------------------
+
+constexpr int GT = 64;      // output tile edge
+constexpr int GR = 32;      // rows per smem stage
+constexpr int GCHUNK = 256; // rows accumulated in FP32 before the FP64 add
+
+__global__ void __launch_bounds__(256) gram_partial_kernel(
+    const float* __restrict__ A, int lda, int pa, const float* __restrict__ B, int ldb, int pb,
+    int64_t n, int64_t rows_per_split, double* __restrict__ partials) {
+  __shared__ float As[GR][GT + 1];
+  __shared__ float Bs[GR][GT + 1];
+  const int ta = blockIdx.x, tb = blockIdx.y, split = blockIdx.z;
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;  // 4x4 patch at (ty*4, tx*4)
+  const int64_t r0 = split * rows_per_split;
+  const int64_t r1 = min(n, r0 + rows_per_split);
+  double accd[4][4];
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      accd[i][j] = 0.0;
+      acc[i][j] = 0.f;
+    }
+  int since = 0;
+  for (int64_t rb = r0; rb < r1; rb += GR) {
+    for (int e = tid; e < GR * GT; e += 256) {
+      const int rr = e / GT, cc = e % GT;
+      const int64_t row = rb + rr;
+      const int ca = ta * GT + cc, cb = tb * GT + cc;
+      As[rr][cc] = (row < r1 && ca < pa) ? A[row * lda + ca] : 0.f;
+      Bs[rr][cc] = (row < r1 && cb < pb) ? B[row * ldb + cb] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int rr = 0; rr < GR; ++rr) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[rr][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[rr][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+    since += GR;
+    if (since >= GCHUNK) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          accd[i][j] += (double)acc[i][j];
+          acc[i][j] = 0.f;
+        }
+      since = 0;
+    }
+  }
+  // partials layout: [split][pb][pa] (column-major per split)
+  double* out = partials + (int64_t)split * pa * pb;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int ia = ta * GT + ty * 4 + i, jb = tb * GT + tx * 4 + j;
+      if (ia < pa && jb < pb) out[(int64_t)jb * pa + ia] = accd[i][j] + (double)acc[i][j];
+    }
+}
+
+__global__ void gram_reduce_kernel(const double* __restrict__ partials, int nsplit, int64_t m,
+                                   double alpha, double* __restrict__ S) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int t = 0; t < nsplit; ++t) s += partials[(int64_t)t * m + e];
+    S[e] = alpha * s;
+  }
+}
+
+int gram_nsplit(int64_t n, int pa, int pb) {
+  const int tiles = (int)(ceil_div(pa, GT) * ceil_div(pb, GT));
+  int64_t want = ceil_div(2 * kNumSMs, tiles);
+  want = std::min<int64_t>(want, ceil_div(n, GCHUNK));
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, 256));
+}
+
+// ---- M (n x p, FP32 row-major) * F (p x q, FP64 column-major) ----------------
+
+constexpr int PT_R = 64, PT_C = 64, PT_K = 32;
+
+__global__ void __launch_bounds__(256) panel_small_kernel(
+    const float* __restrict__ M, int ldm, int p, int64_t n, const double* __restrict__ F,
+    int ldf, int q, float* __restrict__ Y, int ldy) {
+  __shared__ float Ms[PT_R][PT_K + 1];
+  __shared__ float Fs[PT_K][PT_C + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  const int64_t row0 = (int64_t)blockIdx.x * PT_R;
+  const int col0 = blockIdx.y * PT_C;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < p; k0 += PT_K) {
+    for (int e = tid; e < PT_R * PT_K; e += 256) {
+      const int rr = e / PT_K, kk = e % PT_K;
+      const int64_t row = row0 + rr;
+      Ms[rr][kk] = (row < n && k0 + kk < p) ? M[row * ldm + k0 + kk] : 0.f;
+    }
+    for (int e = tid; e < PT_K * PT_C; e += 256) {
+      const int kk = e / PT_C, cc = e % PT_C;
+      Fs[kk][cc] = (k0 + kk < p && col0 + cc < q) ? (float)F[(int64_t)(col0 + cc) * ldf + k0 + kk]
+                                                  : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < PT_K; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = Ms[ty * 4 + i][kk];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Fs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int64_t row = row0 + ty * 4 + i;
+    if (row >= n) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int col = col0 + tx * 4 + j;
+      if (col < ldy) Y[row * ldy + col] = col < q ? acc[i][j] : 0.f;
+    }
+  }
+}
+
+// ---- small FP64 GEMM ------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) dgemm_small_kernel(bool ta, bool tb, int m, int n, int k,
+                                                          double alpha, const double* __restrict__ A,
+                                                          int lda, const double* __restrict__ B,
+                                                          int ldb, double beta,
+                                                          double* __restrict__ C, int ldc) {
+  __shared__ double As[32][33];
+  __shared__ double Bs[32][33];
+  const int tid = threadIdx.x;
+  const int tx = tid % 32, ty = tid / 32;  // each thread: rows ty + 8*i, col tx
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  double acc[4] = {0, 0, 0, 0};
+  for (int k0 = 0; k0 < k; k0 += 32) {
+    for (int e = tid; e < 1024; e += 256) {
+      const int a = e % 32, b = e / 32;
+      // As[ii][kk] = op(A)[i0+ii, k0+kk]
+      {
+        const int ii = a, kk = b;
+        const int gi = i0 + ii, gk = k0 + kk;
+        double v = 0.0;
+        if (gi < m && gk < k) v = ta ? A[(int64_t)gi * lda + gk] : A[(int64_t)gk * lda + gi];
+        As[ii][kk] = v;
+      }
+      // Bs[kk][jj] = op(B)[k0+kk, j0+jj]
+      {
+        const int kk = a, jj = b;
+        const int gk = k0 + kk, gj = j0 + jj;
+        double v = 0.0;
+        if (gk < k && gj < n) v = tb ? B[(int64_t)gk * ldb + gj] : B[(int64_t)gj * ldb + gk];
+        Bs[kk][jj] = v;
+      }
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < 32; ++kk) {
+      const double b = Bs[kk][tx];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i] = fma(As[ty + 8 * i][kk], b, acc[i]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gi = i0 + ty + 8 * i, gj = j0 + tx;
+    if (gi < m && gj < n) {
+      double* c = C + (int64_t)gj * ldc + gi;
+      *c = alpha * acc[i] + (beta == 0.0 ? 0.0 : beta * *c);
+    }
+  }
+}
+
+// ---- upper Cholesky with drop rule (one CTA) ---------------------------------
+
+__global__ void __launch_bounds__(1024) chol_upper_kernel(int p, const double* __restrict__ S,
+                                                          int lds, double* __restrict__ R,
+                                                          double drop2, unsigned* flags) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int64_t e = tid; e < (int64_t)p * p; e += nt) {
+    const int i = (int)(e % p), l = (int)(e / p);
+    R[e] = i <= l ? S[(int64_t)l * lds + i] : 0.0;
+  }
+  __syncthreads();
+  __shared__ double rjj;
+  for (int j = 0; j < p; ++j) {
+    if (tid == 0) {
+      const double d = R[(int64_t)j * p + j];
+      if (!(d > drop2)) {
+        rjj = 0.0;
+        if (!(d == d)) atomicOr(flags, kFlagNonFinite);
+      } else {
+        rjj = sqrt(d);
+      }
+      R[(int64_t)j * p + j] = rjj;
+    }
+    __syncthreads();
+    const double r = rjj;
+    for (int l = j + 1 + tid; l < p; l += nt) {
+      double* x = &R[(int64_t)l * p + j];
+      *x = r > 0.0 ? *x / r : 0.0;
+    }
+    __syncthreads();
+    const int m = p - j - 1;
+    const int64_t cnt = (int64_t)m * m;
+    for (int64_t e = tid; e < cnt; e += nt) {
+      const int ii = j + 1 + (int)(e % m), ll = j + 1 + (int)(e / m);
+      if (ii <= ll) R[(int64_t)ll * p + ii] -= R[(int64_t)ii * p + j] * R[(int64_t)ll * p + j];
+    }
+    __syncthreads();
+  }
+}
+
+// ---- T = R^{-1} (upper), one warp per column ------------------------------------
+
+__global__ void __launch_bounds__(256) trinv_upper_kernel(int p, const double* __restrict__ R,
+                                                          double* __restrict__ T) {
+  extern __shared__ double tcol[];  // [warps][p]
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = blockIdx.x * (blockDim.x >> 5) + w;
+  if (j >= p) return;
+  double* t = tcol + (int64_t)w * p;
+  for (int i = lane; i < p; i += 32) t[i] = 0.0;
+  __syncwarp();
+  const double rjj = R[(int64_t)j * p + j];
+  if (lane == 0) t[j] = rjj != 0.0 ? 1.0 / rjj : 0.0;
+  __syncwarp();
+  for (int i = j - 1; i >= 0; --i) {
+    double s = 0.0;
+    for (int l = i + 1 + lane; l <= j; l += 32) s += R[(int64_t)l * p + i] * t[l];
+#pragma unroll
+    for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    const double rii = R[(int64_t)i * p + i];
+    if (lane == 0) t[i] = rii != 0.0 ? -s / rii : 0.0;
+    __syncwarp();
+  }
+  for (int i = lane; i < p; i += 32) T[(int64_t)j * p + i] = t[i];
+}
+
+// ---- one-sided Jacobi: eigenpairs of Y Y^T -------------------------------------
+
+template <bool kSmem>
+__global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __restrict__ Y,
+                                                      double* __restrict__ evals,
+                                                      double* __restrict__ evecs,
+                                                      float* __restrict__ gwork,
+                                                      unsigned* flags, int max_sweeps, float tol) {
+  extern __shared__ float smem[];
+  float* X = kSmem ? smem : gwork;  // column-major p x p
+  __shared__ int rot_count;
+  __shared__ int order[512];
+  __shared__ float nrm2[512];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int64_t e = tid; e < (int64_t)p * p; e += nt) X[e] = (float)Y[e];
+  const int m = p + (p & 1);  // players in the round-robin tournament
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (tid == 0) rot_count = 0;
+    __syncthreads();
+    for (int r = 0; r < m - 1; ++r) {
+      for (int s = warp; s < m / 2; s += nw) {
+        // circle method: player 0 fixed, the rest rotate by r
+        const int a = s == 0 ? 0 : 1 + ((s - 1 + r) % (m - 1));
+        const int b = 1 + ((m - 2 - s + r) % (m - 1));
+        const int i = min(a, b), j = max(a, b);
+        if (j >= p) continue;
+        float* xi = X + (int64_t)i * p;
+        float* xj = X + (int64_t)j * p;
+        float al = 0.f, be = 0.f, ga = 0.f;
+        for (int t = lane; t < p; t += 32) {
+          const float u = xi[t], v = xj[t];
+          al = fmaf(u, u, al);
+          be = fmaf(v, v, be);
+          ga = fmaf(u, v, ga);
+        }
+#pragma unroll
+        for (int off = 16; off; off >>= 1) {
+          al += __shfl_xor_sync(0xffffffffu, al, off);
+          be += __shfl_xor_sync(0xffffffffu, be, off);
+          ga += __shfl_xor_sync(0xffffffffu, ga, off);
+        }
+        if (fabsf(ga) > tol * sqrtf(al * be) && ga != 0.f) {
+          const float zeta = (be - al) / (2.f * ga);
+          const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+          const float c = rsqrtf(1.f + t * t), sn = c * t;
+          for (int u = lane; u < p; u += 32) {
+            const float x = xi[u], y = xj[u];
+            xi[u] = c * x - sn * y;
+            xj[u] = sn * x + c * y;
+          }
+          if (lane == 0) atomicAdd(&rot_count, 1);
+        }
+      }
+      __syncthreads();
+    }
+    if (rot_count == 0) break;
+    __syncthreads();
+  }
+  // eigenvalue i = squared norm of column i
+  for (int i = warp; i < p; i += nw) {
+    float s = 0.f;
+    for (int t = lane; t < p; t += 32) s = fmaf(X[(int64_t)i * p + t], X[(int64_t)i * p + t], s);
+#pragma unroll
+    for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) nrm2[i] = s;
+  }
+  __syncthreads();
+  // descending order by rank (ties broken by index)
+  for (int i = tid; i < p; i += nt) {
+    int rank = 0;
+    for (int j = 0; j < p; ++j) rank += (nrm2[j] > nrm2[i]) || (nrm2[j] == nrm2[i] && j < i);
+    order[rank] = i;
+  }
+  __syncthreads();
+  for (int r = warp; r < p; r += nw) {
+    const int i = order[r];
+    const float s = nrm2[i];
+    const float inv = s > 0.f ? rsqrtf(s) : 0.f;
+    if (lane == 0) evals[r] = (double)s;
+    for (int t = lane; t < p; t += 32) evecs[(int64_t)r * p + t] = (double)(X[(int64_t)i * p + t] * inv);
+  }
+}
+
+// ---- Gram-Schmidt of the columns of a small m x p FP64 matrix (one CTA) -------------
+// orthogonalize_cols (CPU/Spectral.cpp:146-166) processes the columns left to
+// right, removes the projections on the previous (orthonormal or zero)
+// columns and normalises; a residual norm <= tol zeroes the column.  Here each
+// column is projected twice with classical Gram-Schmidt (CGS2), which matches
+// modified Gram-Schmidt to round-off and turns the inner loop into parallel
+// dot products (m, p <= 512).
+
+__global__ void __launch_bounds__(512) cgs2_cols_kernel(int m, int p, const double* __restrict__ P,
+                                                        int ldp, double* __restrict__ Q, int ldq,
+                                                        double tol) {
+  extern __shared__ double sh[];
+  double* v = sh;        // m
+  double* d = sh + m;    // p
+  __shared__ double red[16];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  for (int j = 0; j < p; ++j) {
+    for (int r = tid; r < m; r += nt) v[r] = P[(int64_t)j * ldp + r];
+    __syncthreads();
+    for (int pass = 0; pass < 2; ++pass) {
+      // d_i = Q_i . v for i < j (one thread per previous column)
+      for (int i = tid; i < j; i += nt) {
+        const double* qi = Q + (int64_t)i * ldq;
+        double s = 0.0;
+        for (int r = 0; r < m; ++r) s = fma(qi[r], v[r], s);
+        d[i] = s;
+      }
+      __syncthreads();
+      // v -= sum_i d_i Q_i (one thread per row)
+      for (int r = tid; r < m; r += nt) {
+        double s = 0.0;
+        for (int i = 0; i < j; ++i) s = fma(d[i], Q[(int64_t)i * ldq + r], s);
+        v[r] -= s;
+      }
+      __syncthreads();
+    }
+    double nrm = 0.0;
+    for (int r = tid; r < m; r += nt) nrm = fma(v[r], v[r], nrm);
+#pragma unroll
+    for (int off = 16; off; off >>= 1) nrm += __shfl_xor_sync(0xffffffffu, nrm, off);
+    if (lane == 0) red[warp] = nrm;
+    __syncthreads();
+    double tot = 0.0;
+    for (int w = 0; w < (nt >> 5); ++w) tot += red[w];
+    const double nn = sqrt(tot);
+    const double sc = nn > tol ? 1.0 / nn : 0.0;
+    for (int r = tid; r < m; r += nt) Q[(int64_t)j * ldq + r] = v[r] * sc;
+    __syncthreads();
+  }
+}
+
+// ---- Ogita-Aishima refinement of all eigenpairs (FP64) ------------------------------
+// Given A (n x n), X (approximate eigenvectors), R = I - X^T X and S = X^T A X,
+// computes E with X' = X + X E (Ogita & Aishima 2018, Algorithm 1); eigenvalue
+// estimates are written to lam.  One CTA (n <= 512).
+
+__global__ void __launch_bounds__(1024) oa_correction_kernel(int n, const double* __restrict__ A,
+                                                             const double* __restrict__ XtX,
+                                                             const double* __restrict__ S,
+                                                             double* __restrict__ E,
+                                                             double* __restrict__ lam) {
+  __shared__ double red[3][32];
+  __shared__ double delta;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < n; i += nt) {
+    const double rii = 1.0 - XtX[(int64_t)i * n + i];
+    lam[i] = S[(int64_t)i * n + i] / (1.0 - rii);
+  }
+  __syncthreads();
+  double fs = 0.0, fa = 0.0, fr = 0.0;
+  for (int64_t e = tid; e < (int64_t)n * n; e += nt) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    const double r = (i == j ? 1.0 : 0.0) - XtX[e];
+    const double sd = S[e] - (i == j ? lam[i] : 0.0);
+    fs += sd * sd;
+    fa += A[e] * A[e];
+    fr += r * r;
+  }
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    fs += __shfl_xor_sync(0xffffffffu, fs, off);
+    fa += __shfl_xor_sync(0xffffffffu, fa, off);
+    fr += __shfl_xor_sync(0xffffffffu, fr, off);
+  }
+  if ((tid & 31) == 0) {
+    red[0][tid >> 5] = fs;
+    red[1][tid >> 5] = fa;
+    red[2][tid >> 5] = fr;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double a = 0, b = 0, c = 0;
+    for (int w = 0; w < (nt >> 5); ++w) {
+      a += red[0][w];
+      b += red[1][w];
+      c += red[2][w];
+    }
+    delta = 2.0 * (sqrt(a) + sqrt(b) * sqrt(c));
+  }
+  __syncthreads();
+  const double dl = delta;
+  for (int64_t e = tid; e < (int64_t)n * n; e += nt) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    const double r = (i == j ? 1.0 : 0.0) - XtX[e];
+    double v;
+    if (i == j) {
+      v = 0.5 * r;
+    } else {
+      const double gap = lam[j] - lam[i];
+      v = fabs(gap) > dl ? (S[e] + lam[j] * r) / gap : 0.5 * r;
+    }
+    E[e] = v;
+  }
+}
+
+// columns of X reordered by descending lam (stable on ties by index)
+__global__ void sort_eigen_kernel(int n, const double* __restrict__ lam, const double* __restrict__ X,
+                                  double* __restrict__ evals, double* __restrict__ evecs) {
+  extern __shared__ int order[];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    int rank = 0;
+    for (int j = 0; j < n; ++j) rank += (lam[j] > lam[i]) || (lam[j] == lam[i] && j < i);
+    order[rank] = i;
+  }
+  __syncthreads();
+  for (int64_t e = threadIdx.x; e < (int64_t)n * n; e += blockDim.x) {
+    const int r = (int)(e % n), c = (int)(e / n);
+    evecs[e] = X[(int64_t)order[c] * n + r];
+  }
+  for (int c = threadIdx.x; c < n; c += blockDim.x) evals[c] = lam[order[c]];
+}
+
+// P (rows x q, row-major panel ld) gets column `col` = v (FP64 vector, length rows)
+__global__ void panel_set_col_kernel(float* __restrict__ P, int ld, int64_t rows, int col,
+                                     const double* __restrict__ v) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (int64_t)gridDim.x * blockDim.x)
+    P[r * ld + col] = (float)v[r];
+}
+
+// dst (rows x ld_d) first q columns = src (rows x ld_s) first q columns, rest zero
+__global__ void panel_copy_kernel(const float* __restrict__ src, int lds, int64_t rows, int q,
+                                  float* __restrict__ dst, int ldd) {
+  const int64_t total = rows * ldd;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / ldd;
+    const int c = (int)(e % ldd);
+    dst[e] = c < q ? src[r * lds + c] : 0.f;
+  }
+}
+
+// ---- Philox-4x32-10 Gaussian panel (Salmon et al., SC'11) -----------------------
+
+__device__ __forceinline__ void philox_round(uint32_t c[4], uint32_t k[2]) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t hi0 = __umulhi(M0, c[0]), lo0 = M0 * c[0];
+  const uint32_t hi1 = __umulhi(M1, c[2]), lo1 = M1 * c[2];
+  const uint32_t n0 = hi1 ^ c[1] ^ k[0], n1 = lo1, n2 = hi0 ^ c[3] ^ k[1], n3 = lo0;
+  c[0] = n0;
+  c[1] = n1;
+  c[2] = n2;
+  c[3] = n3;
+  k[0] += 0x9E3779B9u;
+  k[1] += 0xBB67AE85u;
+}
+
+__global__ void gaussian_panel_kernel(float* __restrict__ P, int64_t n, int q, int ld,
+                                      uint64_t seed, uint64_t stream) {
+  const int64_t total = n * q;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g * 4 < total;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t c[4] = {(uint32_t)g, (uint32_t)(g >> 32), (uint32_t)stream, (uint32_t)(stream >> 32)};
+    uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+#pragma unroll
+    for (int r = 0; r < 10; ++r) philox_round(c, k);
+    float z[4];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      // Box-Muller on two uniforms in (0, 1]
+      const float u1 = ((float)(c[2 * h] >> 8) + 1.f) * (1.f / 16777216.f);
+      const float u2 = ((float)(c[2 * h + 1] >> 8) + 0.5f) * (1.f / 16777216.f);
+      const float rad = sqrtf(-2.f * logf(u1));
+      float sn, cs;
+      sincospif(2.f * u2, &sn, &cs);
+      z[2 * h] = rad * cs;
+      z[2 * h + 1] = rad * sn;
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int64_t idx = g * 4 + e;
+      if (idx < total) P[(idx / q) * ld + (idx % q)] = z[e];
+    }
+  }
+}
+
+__global__ void colmajor_to_panel_kernel(const double* __restrict__ A, int64_t rows, int cols,
+                                         int64_t lda, float* __restrict__ P, int ldp) {
+  const int64_t total = rows * ldp;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / ldp;
+    const int c = (int)(e % ldp);
+    P[e] = c < cols ? (float)A[(int64_t)c * lda + r] : 0.f;
+  }
+}
+
+__global__ void panel_to_colmajor_kernel(const float* __restrict__ P, int ldp, int64_t rows,
+                                         int cols, double* __restrict__ A, int64_t lda) {
+  const int64_t total = rows * cols;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e % rows;
+    const int c = (int)(e / rows);
+    A[(int64_t)c * lda + r] = (double)P[r * ldp + c];
+  }
+}
+
+__global__ void scale_cols_kernel(float* __restrict__ P, int ldp, int64_t n, int q,
+                                  const double* __restrict__ d) {
+  const int64_t total = n * q;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / q;
+    const int c = (int)(e % q);
+    P[r * ldp + c] = (float)(P[r * ldp + c] * d[c]);
+  }
+}
+
+template <typename T>
+__global__ void fill_kernel(T* __restrict__ p, int64_t n, T v) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    p[e] = v;
+}
+
+__global__ void axpy_kernel(int64_t n, double a, const double* __restrict__ x,
+                            double* __restrict__ y) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    y[e] += a * x[e];
+}
+
+unsigned grid_for(int64_t n, int T = 256) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(8 * kNumSMs, ceil_div(n, T)));
+}
+
+}  // namespace
+
+size_t gram_tsk_partials(int64_t n, int pa, int pb) {
+  return (size_t)gram_nsplit(n, pa, pb) * pa * pb;
+}
+
+cudaError_t gram_tsk(const float* A, int lda, int pa, const float* B, int ldb, int pb, int64_t n,
+                     double alpha, double* S, double* partials, int64_t partials_cap,
+                     cudaStream_t s) {
+  const int nsplit = gram_nsplit(n, pa, pb);
+  if ((int64_t)nsplit * pa * pb > partials_cap) return cudaErrorInvalidValue;
+  const int64_t rows_per_split = round_up(ceil_div(n, nsplit), GR);
+  dim3 grid((unsigned)ceil_div(pa, GT), (unsigned)ceil_div(pb, GT), (unsigned)nsplit);
+  gram_partial_kernel<<<grid, 256, 0, s>>>(A, lda, pa, B, ldb, pb, n, rows_per_split, partials);
+  ++g_launch_count;
+  gram_reduce_kernel<<<grid_for((int64_t)pa * pb), 256, 0, s>>>(partials, nsplit,
+                                                                 (int64_t)pa * pb, alpha, S);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t panel_times_small(const float* M, int ldm, int p, int64_t n, const double* F, int ldf,
+                              int q, float* Y, int ldy, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  dim3 grid((unsigned)ceil_div(n, PT_R), (unsigned)ceil_div(ldy, PT_C));
+  panel_small_kernel<<<grid, 256, 0, s>>>(M, ldm, p, n, F, ldf, q, Y, ldy);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t dgemm_small(bool ta, bool tb, int m, int n, int k, double alpha, const double* A,
+                        int lda, const double* B, int ldb, double beta, double* C, int ldc,
+                        cudaStream_t s) {
+  if (m == 0 || n == 0) return cudaSuccess;
+  dim3 grid((unsigned)ceil_div(m, 32), (unsigned)ceil_div(n, 32));
+  dgemm_small_kernel<<<grid, 256, 0, s>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t chol_upper_drop(int p, const double* S, int lds, double* R, double drop2,
+                            unsigned* flags, cudaStream_t s) {
+  chol_upper_kernel<<<1, 1024, 0, s>>>(p, S, lds, R, drop2, flags);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t trinv_upper(int p, const double* R, double* T, cudaStream_t s) {
+  const int warps = 8;
+  trinv_upper_kernel<<<(unsigned)ceil_div(p, warps), warps * 32, (size_t)warps * p * sizeof(double),
+                       s>>>(p, R, T);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t eig_from_factor(int p, const double* Y, double* evals, double* evecs, float* work,
+                            unsigned* flags, cudaStream_t s) {
+  if (p > 512) return cudaErrorInvalidValue;
+  const size_t sm = (size_t)p * p * sizeof(float);
+  const int max_sweeps = 6;  // three FP64 refinement steps follow
+  const float tol = 8.f * sqrtf((float)p) * 6e-8f;
+  if (sm <= 200 * 1024) {
+    static bool attr_set = false;
+    if (!attr_set) {
+      MMSB_CUDA_TRY(cudaFuncSetAttribute(jacobi_kernel<true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      attr_set = true;
+    }
+    jacobi_kernel<true><<<1, 1024, sm, s>>>(p, Y, evals, evecs, work, flags, max_sweeps, tol);
+  } else {
+    jacobi_kernel<false><<<1, 1024, 0, s>>>(p, Y, evals, evecs, work, flags, max_sweeps, tol);
+  }
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t gaussian_panel(float* P, int64_t n, int q, int ld, uint64_t seed, uint64_t stream,
+                           cudaStream_t s) {
+  if (q < ld) MMSB_CUDA_TRY(cudaMemsetAsync(P, 0, sizeof(float) * n * ld, s));
+  gaussian_panel_kernel<<<grid_for(ceil_div(n * q, 4)), 256, 0, s>>>(P, n, q, ld, seed, stream);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t colmajor64_to_panel(const double* A, int64_t rows, int cols, int64_t lda, float* P,
+                                int ldp, cudaStream_t s) {
+  colmajor_to_panel_kernel<<<grid_for(rows * ldp), 256, 0, s>>>(A, rows, cols, lda, P, ldp);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t panel_to_colmajor64(const float* P, int ldp, int64_t rows, int cols, double* A,
+                                int64_t lda, cudaStream_t s) {
+  panel_to_colmajor_kernel<<<grid_for(rows * cols), 256, 0, s>>>(P, ldp, rows, cols, A, lda);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t panel_scale_cols(float* P, int ldp, int64_t n, int q, const double* d,
+                             cudaStream_t s) {
+  scale_cols_kernel<<<grid_for(n * q), 256, 0, s>>>(P, ldp, n, q, d);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t fill_f32(float* p, int64_t n, float v, cudaStream_t s) {
+  fill_kernel<float><<<grid_for(n), 256, 0, s>>>(p, n, v);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t fill_f64(double* p, int64_t n, double v, cudaStream_t s) {
+  fill_kernel<double><<<grid_for(n), 256, 0, s>>>(p, n, v);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t axpy_f64(int64_t n, double a, const double* x, double* y, cudaStream_t s) {
+  axpy_kernel<<<grid_for(n), 256, 0, s>>>(n, a, x, y);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t mgs_cols(int m, int p, const double* P, int ldp, double* Q, int ldq, double tol,
+                     cudaStream_t s) {
+  if (m > 4096 || p > 4096) return cudaErrorInvalidValue;
+  cgs2_cols_kernel<<<1, 512, sizeof(double) * (m + p), s>>>(m, p, P, ldp, Q, ldq, tol);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t oa_correction(int n, const double* A, const double* XtX, const double* S, double* E,
+                          double* lam, cudaStream_t s) {
+  oa_correction_kernel<<<1, 1024, 0, s>>>(n, A, XtX, S, E, lam);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t sort_eigen(int n, const double* lam, const double* X, double* evals, double* evecs,
+                       cudaStream_t s) {
+  sort_eigen_kernel<<<1, 1024, sizeof(int) * n, s>>>(n, lam, X, evals, evecs);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t panel_set_col(float* P, int ld, int64_t rows, int col, const double* v,
+                          cudaStream_t s) {
+  panel_set_col_kernel<<<grid_for(rows), 256, 0, s>>>(P, ld, rows, col, v);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t panel_copy(const float* src, int lds, int64_t rows, int q, float* dst, int ldd,
+                       cudaStream_t s) {
+  panel_copy_kernel<<<grid_for(rows * ldd), 256, 0, s>>>(src, lds, rows, q, dst, ldd);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+}  // namespace mmsb

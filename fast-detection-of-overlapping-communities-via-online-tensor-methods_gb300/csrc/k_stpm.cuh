@@ -1,0 +1,90 @@
+// Argument blocks and launchers of the tensor-power-method kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace mmsb {
+
+enum StpmMode : int {
+  kModePlain = 0,    // one contraction with (Y1, Y2 -> Yout)
+  kModeAdjoint = 1,  // exact gradient of the cubic form: three contractions
+  kModeLoss = 2,     // forward value of the cubic form only
+};
+
+enum StpmStep : int {
+  kStepOnline = 0,  // Phi - beta (3 theta O - gscale G), then polar
+  kStepPolar = 1,   // polar factor of Phi only
+};
+
+struct StpmPartialArgs {
+  const float* y1;
+  const float* y2;
+  const float* y3;  // plain: Yout
+  int64_t ldy;      // row stride of the node-major y arrays
+  const float* phi; // k x k column-major
+  const float* mu1;
+  const float* mu2;
+  const float* mu3;
+  int64_t begin, count;  // node range
+  int k;
+  float c0, c2;          // plain: C = c0 Z1Z2 + c2(Z1 m2 + m1 Z2); adjoint/loss: p0, p2
+  float* gpart;          // [grid][part_stride]: k*k partial G, then 3k d-sums (+1 loss)
+  int64_t part_stride;
+};
+
+struct StpmReduceArgs {
+  int mode;
+  int k;
+  const float* gpart;
+  int64_t part_stride;
+  int nparts;
+  const float* phi;
+  const float* mu1;
+  const float* mu2;
+  const float* mu3;
+  const float* mu_out;  // plain mode
+  double c1, c2;        // plain: d = c1 m1 m2 + c2 sum Z1Z2; adjoint/loss: p1, p2
+  double scale;         // multiplies the contraction (adjoint: 1/count)
+  double count;         // nodes in the pass
+  float* G;             // k x k column-major output
+  double* loss_out;     // loss mode: sum_i That(phi_i,phi_i,phi_i)
+};
+
+struct StpmUpdateArgs {
+  int k;
+  int step_mode;
+  float* phi;           // in/out, k x k column-major
+  const float* G;       // unused by the fused step (kept for the batch path)
+  // fused reduction of the partial kernel's output (online/adjoint steps)
+  int mode;             // kModePlain or kModeAdjoint
+  const float* gpart;
+  int64_t part_stride;
+  int nparts;
+  const float* mu1;
+  const float* mu2;
+  const float* mu3;     // plain: mu_out
+  double c1, c2, scale, count;
+  float beta;
+  float theta3;         // 3 * theta
+  float gscale;         // 3 (plain) or 1 (adjoint: G already holds dT)
+  int max_ns;
+  float ns_tol;
+  unsigned* flags;
+  int* ns_iters;         // accumulates Newton-Schulz iterations
+};
+
+int stpm_kp(int k);
+int stpm_step_kp(int k);
+size_t stpm_partial_smem(int KP, int mode);
+// grid of the partial kernel (a multiple of its cluster size); partial
+// blocks written = grid / stpm_partial_cluster()
+int stpm_partial_grid(int64_t count);
+int stpm_partial_cluster();
+cudaError_t stpm_partial(int mode, const StpmPartialArgs& a, int grid, cudaStream_t s);
+cudaError_t stpm_reduce(const StpmReduceArgs& a, cudaStream_t s);
+cudaError_t stpm_update(const StpmUpdateArgs& a, cudaStream_t s);
+cudaError_t stpm_batch_update(int k, float* phi, const float* G, double* lambda, double* err,
+                              cudaStream_t s);
+cudaError_t stpm_tensor_values(int k, float* phi, const float* G, double* lambda, cudaStream_t s);
+
+}  // namespace mmsb

@@ -1,0 +1,731 @@
+// Host orchestration of the pipeline on one stream: whitening chain,
+// whitened data, tensor power method and unwhitening.  All arithmetic runs in
+// this library's CUDA kernels; the host only sequences launches.
+#include "pipeline.h"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "k_stpm.cuh"
+
+using namespace mmsb;
+
+mmsb_ctx::~mmsb_ctx() {
+  if (s) cudaStreamSynchronize(s);
+  for (auto& kv : ws) cudaFree(kv.second.first);
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& pr : spmm_pool) {
+    if (pr.first) cudaEventDestroy(pr.first);
+    if (pr.second) cudaEventDestroy(pr.second);
+  }
+  if (s) cudaStreamDestroy(s);
+}
+
+void* mmsb_ctx::buf(const std::string& name, size_t bytes) {
+  bytes = std::max<size_t>(bytes, 16);
+  auto it = ws.find(name);
+  if (it != ws.end() && it->second.second >= bytes) return it->second.first;
+  if (it != ws.end()) {
+    cudaStreamSynchronize(s);
+    cudaFree(it->second.first);
+    ws.erase(it);
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw MmsbError(e == cudaErrorMemoryAllocation ? MMSB_ERR_OUT_OF_MEMORY : MMSB_ERR_CUDA,
+                    "cudaMalloc(" + name + ", " + std::to_string(bytes) + "): " +
+                        cudaGetErrorString(e));
+  }
+  ws[name] = {p, bytes};
+  return p;
+}
+
+void mmsb_ctx::free_graph() {
+  for (int b = 0; b < MMSB_NUM_BLOCKS; ++b) {
+    g[b] = DevCsr{};
+    gt[b] = DevCsr{};
+  }
+  have_graph = have_white = have_y = have_phi = have_post = false;
+}
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw MmsbError(MMSB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+namespace {
+
+struct Timer {
+  mmsb_ctx* c;
+  int a, b;
+  double* out;
+  Timer(mmsb_ctx* ctx, int ia, int ib, double* o) : c(ctx), a(ia), b(ib), out(o) {
+    ck(cudaEventRecord(c->ev[a], c->s), "event");
+  }
+  void stop() {
+    ck(cudaEventRecord(c->ev[b], c->s), "event");
+    ck(cudaEventSynchronize(c->ev[b]), "event sync");
+    float ms = 0.f;
+    ck(cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]), "elapsed");
+    *out = ms;
+  }
+};
+
+void check_flags(mmsb_ctx* c, const char* stage) {
+  unsigned f = 0;
+  ck(cudaMemcpyAsync(&f, c->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, c->s), "flags");
+  ck(cudaStreamSynchronize(c->s), "sync");
+  if (f & (kFlagNonFinite | kFlagCholeskyBreakdown)) {
+    ck(cudaMemsetAsync(c->flags, 0, sizeof(unsigned), c->s), "flags");
+    throw MmsbError(MMSB_ERR_NUMERICAL, std::string(stage) + ": non-finite values");
+  }
+  if (f & kFlagTimeout) throw MmsbError(MMSB_ERR_TIMEOUT, std::string(stage) + ": device wait timed out");
+}
+
+// SpMM with timing bookkeeping (algorithmic bytes: CSR + one panel-row
+// gather per nonzero + output)
+void spmm(mmsb_ctx* c, const DevCsr& g, const float* P, int ld, float alpha, float* Y) {
+  const size_t slot = c->spmm_events.size();
+  if (slot < c->spmm_pool.size()) {
+    ck(cudaEventRecord(c->spmm_pool[slot].first, c->s), "event");
+    ck(spmm_f32(g.rp, g.ci, g.val, g.n_rows, P, ld, alpha, Y, c->s), "spmm");
+    ck(cudaEventRecord(c->spmm_pool[slot].second, c->s), "event");
+    c->spmm_events.push_back(slot);
+  } else {
+    ck(spmm_f32(g.rp, g.ci, g.val, g.n_rows, P, ld, alpha, Y, c->s), "spmm");
+  }
+  c->stats.spmm_launches += 1;
+  c->stats.spmm_bytes += 8.0 * (g.n_rows + 1) + 4.0 * g.nnz * (g.val ? 2 : 1) +
+                         4.0 * g.nnz * ld + 4.0 * g.n_rows * ld;
+}
+
+struct Nys {
+  float* U;     // n x ldk panel
+  double* sig;  // k
+};
+
+}  // namespace
+
+// Symmetric positive semi-definite eigen-decomposition (n <= 512), eigenvalues
+// descending: FP32 one-sided Jacobi on the Cholesky factor, then two FP64
+// Ogita-Aishima refinement steps (quadratic convergence to FP64 accuracy).
+void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A, double* evals,
+                     double* V, const double* factor) {
+  cudaStream_t s = c->s;
+  double* R = c->tbuf<double>(tag + ".eR", (size_t)n * n);
+  double* Y = c->tbuf<double>(tag + ".eY", (size_t)n * n);
+  double* X = c->tbuf<double>(tag + ".eX", (size_t)n * n);
+  double* X2 = c->tbuf<double>(tag + ".eX2", (size_t)n * n);
+  double* G = c->tbuf<double>(tag + ".eG", (size_t)n * n);
+  double* AX = c->tbuf<double>(tag + ".eAX", (size_t)n * n);
+  double* S = c->tbuf<double>(tag + ".eS", (size_t)n * n);
+  double* E = c->tbuf<double>(tag + ".eE", (size_t)n * n);
+  double* lam = c->tbuf<double>(tag + ".elam", (size_t)n);
+  float* work = c->tbuf<float>("jacobi_work", (size_t)n * n);
+  if (factor) {
+    Y = const_cast<double*>(factor);  // A = Y Y^T given
+  } else {
+    ck(chol_upper_drop(n, A, n, R, 1e-300, c->flags, s), "eig chol");
+    ck(transpose_f64(n, R, Y, s), "eig R^T");
+  }
+  ck(eig_from_factor(n, Y, lam, X, work, c->flags, s), "jacobi");
+  for (int step = 0; step < 3; ++step) {
+    ck(dgemm_small(true, false, n, n, n, 1.0, X, n, X, n, 0.0, G, n, s), "X^T X");
+    ck(dgemm_small(false, false, n, n, n, 1.0, A, n, X, n, 0.0, AX, n, s), "A X");
+    ck(dgemm_small(true, false, n, n, n, 1.0, X, n, AX, n, 0.0, S, n, s), "X^T A X");
+    ck(oa_correction(n, A, G, S, E, lam, s), "oa");
+    ck(cudaMemcpyAsync(X2, X, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, s), "copy");
+    ck(dgemm_small(false, false, n, n, n, 1.0, X, n, E, n, 1.0, X2, n, s), "X + X E");
+    std::swap(X, X2);
+  }
+  ck(sort_eigen(n, lam, X, evals, V, s), "sort");
+}
+
+namespace {
+
+// SVD_symNystrom_sparse (CPU/Spectral.cpp:169-223) of M = A B, where A is an
+// n x m FP32 panel of full column rank and B an m x p FP64 matrix (B == nullptr:
+// identity, m == p).  With A = Q_A R_A (CholQR2), orthogonalize_cols(M) equals
+// Q_A * MGS(R_A B) because Q_A is an isometry, so the modified Gram-Schmidt and
+// its drop rule run in FP64 on the small coordinate matrix P = R_A B:
+//   Nystrom branch (n > 20k):  QQ = Q[0:p,:],  H = P QQ  (C = M QQ = Q_A H)
+//   thin-SVD branch:           H = P
+// The eigen-pairs (sigma^2, W) of H H^T give U = C V diag(1/sigma) = Q_A W
+// = A R_A^{-1} W and sigma.
+Nys svd_sym_nystrom(mmsb_ctx* c, const std::string& tag, const float* A, int lda, int m,
+                    const double* B, int64_t n) {
+  const int p = c->p, k = c->k, ldk = c->ldk;
+  cudaStream_t s = c->s;
+  const double tol = c->cfg.pinv_tol;
+  const int64_t cap = (int64_t)gram_tsk_partials(std::max<int64_t>(n, 1), m, m);
+  double* part = c->tbuf<double>("gram_part", (size_t)cap);
+  double* S1 = c->tbuf<double>(tag + ".S1", (size_t)m * m);
+  double* S2 = c->tbuf<double>(tag + ".S2", (size_t)m * m);
+  double* R1 = c->tbuf<double>(tag + ".R1", (size_t)m * m);
+  double* R2 = c->tbuf<double>(tag + ".R2", (size_t)m * m);
+  double* RA = c->tbuf<double>(tag + ".RA", (size_t)m * m);
+  double* T1 = c->tbuf<double>(tag + ".T1", (size_t)m * m);
+  double* P = c->tbuf<double>(tag + ".P", (size_t)m * p);
+  double* Hm = c->tbuf<double>(tag + ".H", (size_t)m * p);
+  double* Zs = c->tbuf<double>(tag + ".Zs", (size_t)m * m);
+  double* ev = c->tbuf<double>(tag + ".ev", (size_t)m);
+  double* Wv = c->tbuf<double>(tag + ".W", (size_t)m * m);
+  double* F = c->tbuf<double>(tag + ".F", (size_t)m * k);
+  double* sig = c->tbuf<double>(tag + ".sig", (size_t)k);
+  float* U = c->tbuf<float>(tag + ".U", (size_t)n * ldk);
+  float* Q1 = c->tbuf<float>("nys.Q1", (size_t)n * round_up(m, 4));
+  const int ldq = (int)round_up(m, 4);
+  // CholQR2: A = Q_A R_A
+  ck(gram_tsk(A, lda, m, A, lda, m, n, 1.0, S1, part, cap, s), "gram1");
+  ck(chol_upper_drop(m, S1, m, R1, 1e-300, c->flags, s), "chol1");
+  ck(trinv_upper(m, R1, T1, s), "trinv1");
+  ck(panel_times_small(A, lda, m, n, T1, m, m, Q1, ldq, s), "Q1");
+  ck(gram_tsk(Q1, ldq, m, Q1, ldq, m, n, 1.0, S2, part, cap, s), "gram2");
+  ck(chol_upper_drop(m, S2, m, R2, 1e-300, c->flags, s), "chol2");
+  ck(dgemm_small(false, false, m, m, m, 1.0, R2, m, R1, m, 0.0, RA, m, s), "R_A");
+  // Q_A = Q1 R2^{-1} with R2 ~ I: products with Q_A use Q1 and T2 = R2^{-1}
+  double* T2 = c->tbuf<double>(tag + ".T2", (size_t)m * m);
+  ck(trinv_upper(m, R2, T2, s), "R2^-1");
+  // P = R_A B
+  if (B)
+    ck(dgemm_small(false, false, m, p, m, 1.0, RA, m, B, m, 0.0, P, m, s), "P");
+  else
+    ck(cudaMemcpyAsync(P, RA, sizeof(double) * m * p, cudaMemcpyDeviceToDevice, s), "P");
+  const bool nystrom = n > (int64_t)c->cfg.nystrom_rows_factor * k;
+  if (nystrom) {
+    double* Qs = c->tbuf<double>(tag + ".Qs", (size_t)m * p);
+    double* Ap = c->tbuf<double>(tag + ".Ap", (size_t)p * m);
+    double* QAp = c->tbuf<double>(tag + ".QAp", (size_t)p * m);
+    double* QQ = c->tbuf<double>(tag + ".QQ", (size_t)p * p);
+    if (B)
+      ck(mgs_cols(m, p, P, m, Qs, m, tol, s), "mgs");
+    else  // MGS of the upper-triangular R_A is the identity (zero where R_jj == 0)
+      ck(eye_mask(m, p, P, m, Qs, m, s), "mgs(R)");
+    // QQ = Q[0:p, :] = Q_A[0:p, :] Q_small = Q1[0:p, :] R2^{-1} Q_small  (Spectral.cpp:185-188)
+    ck(panel_to_colmajor64(Q1, ldq, p, m, Ap, p, s), "Q1[0:p]");
+    ck(dgemm_small(false, false, p, m, m, 1.0, Ap, p, T2, m, 0.0, QAp, p, s), "Q_A[0:p]");
+    ck(dgemm_small(false, false, p, p, m, 1.0, QAp, p, Qs, m, 0.0, QQ, p, s), "QQ");
+    ck(dgemm_small(false, false, m, p, p, 1.0, P, m, QQ, p, 0.0, Hm, m, s), "H");
+  } else {
+    ck(cudaMemcpyAsync(Hm, P, sizeof(double) * m * p, cudaMemcpyDeviceToDevice, s), "H");
+  }
+  ck(dgemm_small(false, true, m, m, p, 1.0, Hm, m, Hm, m, 0.0, Zs, m, s), "H H^T");
+  // Zs = H H^T: with a square H the one-sided Jacobi runs on H directly
+  sym_eig_refined(c, tag, m, Zs, ev, Wv, m == p ? Hm : nullptr);
+  // sigma = sqrt(ev_k); U = Q_A W_k diag(sigma > tol) = Q1 (R2^{-1} W_k) (masked)
+  ck(sig_from_evals(k, ev, sig, s), "sig");
+  ck(dgemm_small(false, false, m, k, m, 1.0, T2, m, Wv, m, 0.0, F, m, s), "F");
+  ck(mask_cols(m, k, F, m, sig, tol, s), "mask");
+  ck(panel_times_small(Q1, ldq, m, n, F, m, k, U, ldk, s), "U");
+  return Nys{U, sig};
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+void pipeline_upload(mmsb_ctx* c, const mmsb_csr* blocks) {
+  const int rows_part[5] = {0, 0, 0, 2, 3};
+  const int cols_part[5] = {1, 2, 3, 1, 1};
+  int64_t part[4] = {-1, -1, -1, -1};
+  for (int b = 0; b < MMSB_NUM_BLOCKS; ++b) {
+    const mmsb_csr& m = blocks[b];
+    if (m.n_rows < 0 || m.n_cols < 0 || m.nnz < 0 || (m.nnz > 0 && (!m.row_ptr || !m.col_idx)) ||
+        (!m.row_ptr && m.n_rows > 0))
+      throw MmsbError(MMSB_ERR_INVALID_ARG, "block " + std::to_string(b) + ": bad CSR");
+    for (int side = 0; side < 2; ++side) {
+      const int pp = side ? cols_part[b] : rows_part[b];
+      const int64_t n = side ? m.n_cols : m.n_rows;
+      if (part[pp] >= 0 && part[pp] != n)
+        throw MmsbError(MMSB_ERR_INVALID_ARG, "inconsistent partition sizes across blocks");
+      part[pp] = n;
+    }
+    if (m.n_rows > 0 && (m.row_ptr[0] != 0 || m.row_ptr[m.n_rows] != m.nnz))
+      throw MmsbError(MMSB_ERR_INVALID_ARG, "block " + std::to_string(b) + ": row_ptr/nnz mismatch");
+    if (m.n_cols > INT32_MAX) throw MmsbError(MMSB_ERR_INVALID_ARG, "too many columns");
+  }
+  c->free_graph();
+  c->nX = part[0];
+  c->nA = part[1];
+  c->nB = part[2];
+  c->nC = part[3];
+  if (c->nX < 1 || c->nA < 1 || c->nB < 1 || c->nC < 1)
+    throw MmsbError(MMSB_ERR_INVALID_ARG, "every partition needs at least one node");
+  for (int b = 0; b < MMSB_NUM_BLOCKS; ++b) {
+    const mmsb_csr& m = blocks[b];
+    DevCsr& d = c->g[b];
+    const std::string t = "g" + std::to_string(b);
+    d.n_rows = m.n_rows;
+    d.n_cols = m.n_cols;
+    d.nnz = m.nnz;
+    d.rp = c->tbuf<int64_t>(t + ".rp", m.n_rows + 1);
+    d.ci = c->tbuf<int32_t>(t + ".ci", m.nnz);
+    d.val = m.val ? c->tbuf<float>(t + ".val", m.nnz) : nullptr;
+    ck(cudaMemcpyAsync(d.rp, m.row_ptr, sizeof(int64_t) * (m.n_rows + 1), cudaMemcpyHostToDevice, c->s), "H2D rp");
+    if (m.nnz) ck(cudaMemcpyAsync(d.ci, m.col_idx, sizeof(int32_t) * m.nnz, cudaMemcpyHostToDevice, c->s), "H2D ci");
+    if (m.val) ck(cudaMemcpyAsync(d.val, m.val, sizeof(float) * m.nnz, cudaMemcpyHostToDevice, c->s), "H2D val");
+    DevCsr& e = c->gt[b];
+    e.n_rows = m.n_cols;
+    e.n_cols = m.n_rows;
+    e.nnz = m.nnz;
+    e.rp = c->tbuf<int64_t>(t + "t.rp", m.n_cols + 1);
+    e.ci = c->tbuf<int32_t>(t + "t.ci", m.nnz);
+    e.val = m.val ? c->tbuf<float>(t + "t.val", m.nnz) : nullptr;
+    int32_t* scratch = c->tbuf<int32_t>("transpose_scratch", 2 * (m.n_cols + 1) + 2 * m.nnz + 2);
+    ck(csr_transpose(d.rp, d.ci, d.val, d.n_rows, d.n_cols, d.nnz, e.rp, e.ci, e.val, scratch, c->s),
+       "transpose");
+  }
+  ck(cudaStreamSynchronize(c->s), "upload sync");
+  c->have_graph = true;
+}
+
+static void alloc_results(mmsb_ctx* c) {
+  const int k = c->k, ldk = c->ldk;
+  c->W = c->tbuf<float>("W", (size_t)c->nA * ldk);
+  c->Zb1 = c->tbuf<float>("Zb1", (size_t)c->nA * ldk);
+  c->Zc1 = c->tbuf<float>("Zc1", (size_t)c->nA * ldk);
+  c->mu = c->tbuf<double>("mu", (size_t)(c->nA + c->nB + c->nC));
+  for (int q = 0; q < 3; ++q) c->y[q] = c->tbuf<float>("y" + std::to_string(q), (size_t)c->nX * ldk);
+  c->ymu = c->tbuf<float>("ymu", 3 * (size_t)k);
+  c->ymu64 = c->tbuf<double>("ymu64", 3 * (size_t)k);
+  c->phi = c->tbuf<float>("phi", (size_t)k * k);
+  c->lambda = c->tbuf<double>("lambda", (size_t)k);
+}
+
+// whitened data and means from W, Zb1, Ub, Zc1, Uc (CommunityDetection.cpp:66-68)
+void pipeline_ydata(mmsb_ctx* c) {
+  const int k = c->k, ldk = c->ldk;
+  cudaStream_t s = c->s;
+  double* part = c->tbuf<double>("gram_part_y", gram_tsk_partials(std::max(c->nA, std::max(c->nB, c->nC)), k, k));
+  const int64_t cap = (int64_t)gram_tsk_partials(std::max(c->nA, std::max(c->nB, c->nC)), k, k);
+  double* ZW = c->tbuf<double>("ZW", (size_t)k * k);
+  float* Wb = c->tbuf<float>("Wb_eff", (size_t)c->nB * ldk);
+  float* Wc = c->tbuf<float>("Wc_eff", (size_t)c->nC * ldk);
+  float* mu32 = c->tbuf<float>("mu32", (size_t)(c->nA + c->nB + c->nC) * 4);
+  const double* mu_a = c->mu;
+  const double* mu_b = c->mu + c->nA;
+  const double* mu_c = c->mu + c->nA + c->nB;
+  // Wb_eff = Ub (Zb1^T W), Wc_eff = Uc (Zc1^T W)
+  ck(gram_tsk(c->Zb1, ldk, k, c->W, ldk, k, c->nA, 1.0, ZW, part, cap, s), "Zb1^T W");
+  ck(panel_times_small(c->Ub, ldk, k, c->nB, ZW, k, k, Wb, ldk, s), "Wb");
+  ck(gram_tsk(c->Zc1, ldk, k, c->W, ldk, k, c->nA, 1.0, ZW, part, cap, s), "Zc1^T W");
+  ck(panel_times_small(c->Uc, ldk, k, c->nC, ZW, k, k, Wc, ldk, s), "Wc");
+  spmm(c, c->g[MMSB_BLOCK_XA], c->W, ldk, 1.f, c->y[0]);
+  spmm(c, c->g[MMSB_BLOCK_XB], Wb, ldk, 1.f, c->y[1]);
+  spmm(c, c->g[MMSB_BLOCK_XC], Wc, ldk, 1.f, c->y[2]);
+  // whitened means: W_P^T mu_P (mu as an n x 1 panel, ld 4)
+  ck(colmajor64_to_panel(mu_a, c->nA, 1, c->nA, mu32, 4, s), "mu32a");
+  ck(gram_tsk(c->W, ldk, k, mu32, 4, 1, c->nA, 1.0, c->ymu64, part, cap, s), "ymu_a");
+  ck(colmajor64_to_panel(mu_b, c->nB, 1, c->nB, mu32, 4, s), "mu32b");
+  ck(gram_tsk(Wb, ldk, k, mu32, 4, 1, c->nB, 1.0, c->ymu64 + k, part, cap, s), "ymu_b");
+  ck(colmajor64_to_panel(mu_c, c->nC, 1, c->nC, mu32, 4, s), "mu32c");
+  ck(gram_tsk(Wc, ldk, k, mu32, 4, 1, c->nC, 1.0, c->ymu64 + 2 * k, part, cap, s), "ymu_c");
+  ck(f64_to_f32(c->ymu64, c->ymu, 3 * k, s), "ymu32");
+  c->have_y = true;
+}
+
+// sums the device time of the SpMM launches recorded since the last call
+void collect_spmm_time(mmsb_ctx* c) {
+  double ms = 0.0;
+  for (size_t slot : c->spmm_events) {
+    ck(cudaEventSynchronize(c->spmm_pool[slot].second), "event sync");
+    float t = 0.f;
+    ck(cudaEventElapsedTime(&t, c->spmm_pool[slot].first, c->spmm_pool[slot].second), "elapsed");
+    ms += t;
+  }
+  c->stats.spmm_ms += ms;
+  c->spmm_events.clear();
+}
+
+void pipeline_whiten(mmsb_ctx* c, const double* const* sketches) {
+  if (!c->have_graph) throw MmsbError(MMSB_ERR_STATE, "whiten before upload_graph");
+  c->spmm_events.clear();
+  const int k = c->k, p = c->p, ldp = c->ldp, ldk = c->ldk;
+  cudaStream_t s = c->s;
+  alloc_results(c);
+  const double inv = c->cfg.normalize ? 1.0 / (double)c->nX : 1.0;
+  const double tol = c->cfg.pinv_tol;
+  const DevCsr &XA = c->g[0], &XB = c->g[1], &XC = c->g[2];
+  const DevCsr &XAt = c->gt[0], &XBt = c->gt[1], &XCt = c->gt[2];
+  const int64_t nmax = std::max(std::max(c->nX, c->nA), std::max(c->nB, c->nC));
+  float* R[3];
+  const int64_t rn[3] = {c->nB, c->nC, c->nA};
+  for (int q = 0; q < 3; ++q) {
+    R[q] = c->tbuf<float>("R" + std::to_string(q), (size_t)rn[q] * ldp);
+    if (sketches && sketches[q]) {
+      double* tmp = c->tbuf<double>("sketch_upload", (size_t)rn[q] * p);
+      ck(cudaMemcpyAsync(tmp, sketches[q], sizeof(double) * rn[q] * p, cudaMemcpyHostToDevice, s), "H2D sketch");
+      ck(colmajor64_to_panel(tmp, rn[q], p, rn[q], R[q], ldp, s), "sketch panel");
+    } else {
+      ck(gaussian_panel(R[q], rn[q], p, ldp, c->cfg.seed, 11 + q, s), "gaussian");
+    }
+  }
+  // partition means (Util.cpp:48-51): column sums of G_XP = row sums of G_XP^T
+  ck(row_sums_f64(XAt.rp, XAt.val, c->nA, inv, c->mu, s), "mu_a");
+  ck(row_sums_f64(XBt.rp, XBt.val, c->nB, inv, c->mu + c->nA, s), "mu_b");
+  ck(row_sums_f64(XCt.rp, XCt.val, c->nC, inv, c->mu + c->nA + c->nB, s), "mu_c");
+
+  float* T1 = c->tbuf<float>("T1", (size_t)c->nX * ldp);
+  float* XR = c->tbuf<float>("XR", (size_t)nmax * ldp);
+  float* Gram = c->tbuf<float>("Gram", (size_t)nmax * ldp);
+  float* T3 = c->tbuf<float>("T3", (size_t)c->nX * ldk);
+  float* VL = c->tbuf<float>("VL", (size_t)nmax * ldk);
+  double* Linv_sqrt = c->tbuf<double>("Linv_sqrt", (size_t)k);
+  double* Linv_c = c->tbuf<double>("Linv_c", (size_t)k);
+  double* Linv_b = c->tbuf<double>("Linv_b", (size_t)k);
+  c->Ub = c->tbuf<float>("Ub", (size_t)c->nB * ldk);
+  c->Uc = c->tbuf<float>("Uc", (size_t)c->nC * ldk);
+  float* Vc = c->tbuf<float>("Vc", (size_t)c->nB * ldk);
+  float* Vb = c->tbuf<float>("Vb", (size_t)c->nC * ldk);
+
+  // pinv_Nystrom_sparse_component (Spectral.cpp:296-315) of
+  //   Zc_den = inv Gx_c^T Gx_b (n_C x n_B), sketch R_c (n_B x 2k)
+  //   Zb_den = inv Gx_b^T Gx_c (n_B x n_C), sketch R_b (n_C x 2k)
+  struct Side {
+    const DevCsr *Gin, *Gout_t, *Gout, *Gin_t;
+    int64_t n_in, n_out;
+    float* Rk;
+    float* V;
+    float* U;
+    double* Linv;
+    const char* tag;
+  } sides[2] = {
+      {&XB, &XCt, &XC, &XBt, c->nB, c->nC, R[0], Vc, c->Uc, Linv_c, "zc"},
+      {&XC, &XBt, &XB, &XCt, c->nC, c->nB, R[1], Vb, c->Ub, Linv_b, "zb"},
+  };
+  for (auto& sd : sides) {
+    // X = inv Gout^T Gin  (n_out x n_in):  XR = X R ; Gram = X^T XR
+    spmm(c, *sd.Gin, sd.Rk, ldp, 1.f, T1);                  // Gin R       (n_X x p)
+    spmm(c, *sd.Gout_t, T1, ldp, (float)inv, XR);           // X R         (n_out x p)
+    spmm(c, *sd.Gout, XR, ldp, 1.f, T1);                    // Gout XR     (n_X x p)
+    spmm(c, *sd.Gin_t, T1, ldp, (float)inv, Gram);          // X^T X R     (n_in x p)
+    Nys ny = svd_sym_nystrom(c, sd.tag, Gram, ldp, p, nullptr, sd.n_in);  // V, sigma
+    ck(cudaMemcpyAsync(sd.V, ny.U, sizeof(float) * sd.n_in * ldk, cudaMemcpyDeviceToDevice, s), "V");
+    // U = X V diag(sqrt(pinv(sigma)));  Linv = pinv(sqrt(sigma))  (Spectral.cpp:235-244, 307)
+    ck(sqrt_pinv(k, ny.sig, tol, Linv_sqrt, sd.Linv, s), "Linv");
+    ck(cudaMemcpyAsync(VL, sd.V, sizeof(float) * sd.n_in * ldk, cudaMemcpyDeviceToDevice, s), "VL");
+    ck(panel_scale_cols(VL, ldk, sd.n_in, k, Linv_sqrt, s), "VL scale");
+    spmm(c, *sd.Gin, VL, ldk, 1.f, T3);
+    spmm(c, *sd.Gout_t, T3, ldk, (float)inv, sd.U);
+  }
+  // Z_C_part1 = Zc_num V_c diag(Linv_c), Zc_num = inv Gx_a^T Gx_b (Util.cpp:83-84)
+  ck(cudaMemcpyAsync(VL, Vc, sizeof(float) * c->nB * ldk, cudaMemcpyDeviceToDevice, s), "VL");
+  ck(panel_scale_cols(VL, ldk, c->nB, k, Linv_c, s), "Vc scale");
+  spmm(c, XB, VL, ldk, 1.f, T3);
+  spmm(c, XAt, T3, ldk, (float)inv, c->Zc1);
+  // Z_B_part1 = Zb_num V_b diag(Linv_b), Zb_num = inv Gx_a^T Gx_c (Util.cpp:96-97)
+  ck(cudaMemcpyAsync(VL, Vb, sizeof(float) * c->nC * ldk, cudaMemcpyDeviceToDevice, s), "VL");
+  ck(panel_scale_cols(VL, ldk, c->nC, k, Linv_b, s), "Vb scale");
+  spmm(c, XC, VL, ldk, 1.f, T3);
+  spmm(c, XAt, T3, ldk, (float)inv, c->Zb1);
+  // core = U_c^T Zc_den U_b = inv (Gx_c U_c)^T (Gx_b U_b)  (Util.cpp:90-94)
+  float* T4 = c->tbuf<float>("T4", (size_t)c->nX * ldk);
+  double* core = c->tbuf<double>("core", (size_t)k * k);
+  const int64_t cap = (int64_t)gram_tsk_partials(nmax, std::max(k, p), p);
+  double* part = c->tbuf<double>("gram_part_w", (size_t)cap);
+  spmm(c, XC, c->Uc, ldk, 1.f, T3);
+  spmm(c, XB, c->Ub, ldk, 1.f, T4);
+  ck(gram_tsk(T3, ldk, k, T4, ldk, k, c->nX, inv, core, part, cap, s), "core");
+  ck(diag_guard(k, core, s), "core guard");
+  // M2 sketch = (a0+1) Zc1 core (Zb1^T R_a) - a0 mu_a (mu_a^T R_a)  (Util.cpp:103-113),
+  // kept factored as M2 = [Zc1 | mu_a] B with B = [(a0+1) core Zb1^T R_a ; -a0 mu_a^T R_a]
+  // (rank <= k+1, so its Gram-Schmidt must see FP64 round-off, not FP32)
+  const int m2 = k + 1, ldm2 = (int)round_up(m2, 4);
+  double* Q1 = c->tbuf<double>("ZbR", (size_t)k * p);
+  double* ma = c->tbuf<double>("muR", (size_t)p);
+  double* Bm = c->tbuf<double>("M2B", (size_t)m2 * p);
+  float* mu32 = c->tbuf<float>("mu32", (size_t)(c->nA + c->nB + c->nC) * 4);
+  float* Am = c->tbuf<float>("M2A", (size_t)c->nA * ldm2);
+  ck(gram_tsk(c->Zb1, ldk, k, R[2], ldp, p, c->nA, 1.0, Q1, part, cap, s), "Zb1^T R");
+  ck(colmajor64_to_panel(c->mu, c->nA, 1, c->nA, mu32, 4, s), "mu32");
+  ck(gram_tsk(mu32, 4, 1, R[2], ldp, p, c->nA, 1.0, ma, part, cap, s), "mu^T R");
+  ck(dgemm_small(false, false, k, p, k, c->cfg.alpha0 + 1.0, core, k, Q1, k, 0.0, Bm, m2, s), "B");
+  ck(set_row_scaled(m2, p, Bm, m2, k, -c->cfg.alpha0, ma, s), "B shift row");
+  ck(panel_copy(c->Zc1, ldk, c->nA, k, Am, ldm2, s), "A_M");
+  ck(panel_set_col(Am, ldm2, c->nA, k, c->mu, s), "A_M mu");
+  // W = U_w diag(pinv(sqrt(sigma_w)))  (Util.cpp:116-123)
+  Nys nw = svd_sym_nystrom(c, "w", Am, ldm2, m2, Bm, c->nA);
+  ck(sqrt_pinv(k, nw.sig, tol, nullptr, Linv_sqrt, s), "Lw");
+  ck(cudaMemcpyAsync(c->W, nw.U, sizeof(float) * c->nA * ldk, cudaMemcpyDeviceToDevice, s), "W");
+  ck(panel_scale_cols(c->W, ldk, c->nA, k, Linv_sqrt, s), "W scale");
+  c->have_white = true;
+  pipeline_ydata(c);
+  check_flags(c, "whitening");
+  collect_spmm_time(c);
+}
+
+// ---------------------------------------------------------------------------
+
+struct PartialOut {
+  float* gpart;
+  int grid;
+  int64_t stride;
+};
+
+// per-CTA partial contractions over nodes [begin, begin+count)
+static PartialOut stpm_partials(mmsb_ctx* c, int mode, int q1, int q2, int q3, int64_t begin,
+                                int64_t count, double c0, double c2) {
+  const int k = c->k;
+  const int grid = stpm_partial_grid(count);
+  const int64_t stride = (int64_t)k * k + 3 * k + 4;
+  float* gpart = c->tbuf<float>("gpart", (size_t)grid * stride);
+  StpmPartialArgs a{};
+  a.y1 = c->y[q1];
+  a.y2 = c->y[q2];
+  a.y3 = c->y[q3];
+  a.ldy = c->ldk;
+  a.phi = c->phi;
+  a.mu1 = c->ymu + q1 * k;
+  a.mu2 = c->ymu + q2 * k;
+  a.mu3 = c->ymu + q3 * k;
+  a.begin = begin;
+  a.count = count;
+  a.k = k;
+  a.c0 = (float)c0;
+  a.c2 = (float)c2;
+  a.gpart = gpart;
+  a.part_stride = stride;
+  ck(stpm_partial(mode, a, grid, c->s), "stpm_partial");
+  return PartialOut{gpart, grid / stpm_partial_cluster(), stride};
+}
+
+static void stpm_pass(mmsb_ctx* c, int mode, int q1, int q2, int q3, int64_t begin, int64_t count,
+                      double c0, double c1, double c2, double scale, float* G, double* loss) {
+  const int k = c->k;
+  PartialOut po = stpm_partials(c, mode, q1, q2, q3, begin, count, c0, c2);
+  StpmReduceArgs r{};
+  r.mode = mode;
+  r.k = k;
+  r.gpart = po.gpart;
+  r.part_stride = po.stride;
+  r.nparts = po.grid;
+  r.phi = c->phi;
+  r.mu1 = c->ymu + q1 * k;
+  r.mu2 = c->ymu + q2 * k;
+  r.mu3 = c->ymu + q3 * k;
+  r.mu_out = r.mu3;
+  r.c1 = c1;
+  r.c2 = c2;
+  r.scale = scale;
+  r.count = (double)count;
+  r.G = G;
+  r.loss_out = loss;
+  ck(stpm_reduce(r, c->s), "stpm_reduce");
+}
+
+static StpmUpdateArgs step_args(mmsb_ctx* c, int step_mode, int* ns_iters) {
+  StpmUpdateArgs u{};
+  u.k = c->k;
+  u.step_mode = step_mode;
+  u.phi = c->phi;
+  u.theta3 = (float)(3.0 * c->cfg.theta);
+  u.max_ns = 80;
+  u.ns_tol = 2e-6f;  // early exit; the 1e-3 + one-iteration rule ends typical steps
+  u.flags = c->flags;
+  u.ns_iters = ns_iters;
+  return u;
+}
+
+static void polar_only(mmsb_ctx* c, int* ns_iters) {
+  StpmUpdateArgs u = step_args(c, kStepPolar, ns_iters);
+  ck(stpm_update(u, c->s), "stpm_polar");
+}
+
+// one minibatch update: partial contractions, then the fused reduction +
+// Phi - beta (3 theta O - gscale G) + polar orthonormalisation on one cluster
+static void stpm_step(mmsb_ctx* c, int mode, int64_t x0, int64_t cnt, double c0, double c1,
+                      double c2, double scale, double beta, double gscale, int* ns_iters) {
+  const int k = c->k;
+  PartialOut po = stpm_partials(c, mode, 0, 1, 2, x0, cnt, c0, c2);
+  StpmUpdateArgs u = step_args(c, kStepOnline, ns_iters);
+  u.mode = mode;
+  u.gpart = po.gpart;
+  u.part_stride = po.stride;
+  u.nparts = po.grid;
+  u.mu1 = c->ymu;
+  u.mu2 = c->ymu + k;
+  u.mu3 = c->ymu + 2 * k;
+  u.c1 = c1;
+  u.c2 = c2;
+  u.scale = scale;
+  u.count = (double)cnt;
+  u.beta = (float)beta;
+  u.gscale = (float)gscale;
+  ck(stpm_update(u, c->s), "stpm_step");
+}
+
+void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
+  if (!c->have_y) throw MmsbError(MMSB_ERR_STATE, "stpm before whitening");
+  const int k = c->k;
+  if (k > 128) throw MmsbError(MMSB_ERR_UNSUPPORTED, "STPM kernels support k <= 128");
+  cudaStream_t s = c->s;
+  const double a0 = c->cfg.alpha0;
+  const double p0 = (a0 + 1.0) * (a0 + 2.0) / 2.0, p1 = a0 * a0, p2 = -a0 * (a0 + 1.0) / 2.0;
+  float* G = c->tbuf<float>("G", (size_t)k * k);
+  int* ns_it = c->tbuf<int>("ns_iters", 4);
+  ck(cudaMemsetAsync(ns_it, 0, sizeof(int), s), "ns counter");
+  if (phi0) {
+    double* tmp = c->tbuf<double>("phi64", (size_t)k * k);
+    ck(cudaMemcpyAsync(tmp, phi0, sizeof(double) * k * k, cudaMemcpyHostToDevice, s), "H2D phi0");
+    ck(f64_to_f32(tmp, c->phi, (int64_t)k * k, s), "phi0");
+  } else {
+    // orthonormal start: polar factor of a seeded Gaussian matrix
+    ck(gaussian_panel(c->phi, k, k, k, c->cfg.seed, 7, s), "phi0");
+    polar_only(c, ns_it);
+  }
+  const int64_t nx = c->nX;
+  c->stats.stpm_steps = 0;
+  if (c->cfg.stpm_method == MMSB_STPM_BATCH_POWER) {
+    // tensorDecom_alpha0 (Util.cpp:131-184)
+    const double inv_x = 1.0 / (double)nx;
+    const double p_main = p0 * inv_x, p_s1 = p2 * inv_x, p_s0 = p1;
+    double err = 0.0;
+    for (int64_t it = 1;; ++it) {
+      if (c->stop.load()) throw MmsbError(MMSB_ERR_STOPPED, "stop requested");
+      stpm_pass(c, kModePlain, 1, 2, 0, 0, nx, p_main, p_s0, p_s1, 1.0, G, nullptr);
+      ck(stpm_batch_update(k, c->phi, G, c->lambda, c->dscalar, s), "batch update");
+      c->stats.stpm_steps = it;
+      if (it >= c->cfg.min_iter) {
+        ck(cudaMemcpyAsync(&err, c->dscalar, sizeof(double), cudaMemcpyDeviceToHost, s), "err");
+        ck(cudaStreamSynchronize(s), "sync");
+        if (err < c->cfg.tol || it > c->cfg.max_iter) break;
+      }
+    }
+    c->stats.stpm_last_error = err;
+    c->stats.node_updates = nx * c->stats.stpm_steps;
+  } else {
+    const bool adj = c->cfg.stpm_method == MMSB_STPM_ADJOINT;
+    const int64_t b = std::max<int64_t>(1, std::min<int64_t>(c->cfg.minibatch, nx));
+    int64_t t = 0;
+    for (int sw = 0; sw < c->cfg.sweeps; ++sw) {
+      for (int64_t x0 = 0; x0 < nx; x0 += b) {
+        if (c->stop.load()) throw MmsbError(MMSB_ERR_STOPPED, "stop requested");
+        const int64_t cnt = std::min<int64_t>(b, nx - x0);
+        const double beta = c->cfg.lr0 / (1.0 + (double)t);
+        if (adj)  // dT (column i = d That_i / d phi_i); step = 3 theta O - dT
+          stpm_step(c, kModeAdjoint, x0, cnt, p0, p1, p2, 1.0 / cnt, beta, 1.0, ns_it);
+        else  // G = mean of The_second_term; step = 3 theta O - 3 G
+          stpm_step(c, kModePlain, x0, cnt, p0 / cnt, p1, p2 / cnt, 1.0, beta, 3.0, ns_it);
+        ++t;
+      }
+    }
+    c->stats.stpm_steps = t;
+    c->stats.node_updates = nx * c->cfg.sweeps;
+    int nsit = 0;
+    ck(cudaMemcpyAsync(&nsit, ns_it, sizeof(int), cudaMemcpyDeviceToHost, s), "ns counter");
+    ck(cudaStreamSynchronize(s), "sync");
+    c->stats.polar_iterations = nsit;
+    // lambda_i = That(phi_i, phi_i, phi_i) over all of X; sign fixed so lambda > 0
+    stpm_pass(c, kModePlain, 0, 1, 2, 0, nx, p0 / nx, p1, p2 / nx, 1.0, G, nullptr);
+    ck(stpm_tensor_values(k, c->phi, G, c->lambda, s), "lambda");
+  }
+  check_flags(c, "stpm");
+  c->have_phi = true;
+}
+
+void pipeline_post(mmsb_ctx* c) {
+  if (!c->have_phi || !c->have_white) throw MmsbError(MMSB_ERR_STATE, "postproc before stpm");
+  const int k = c->k, ldk = c->ldk;
+  cudaStream_t s = c->s;
+  const int64_t N = c->nX + c->nA + c->nB + c->nC;
+  const int words = (k + 31) / 32;
+  c->pi = c->tbuf<float>("pi", (size_t)N * k);
+  c->bits = c->tbuf<uint32_t>("bits", (size_t)N * words);
+  double* F = c->tbuf<double>("postF", (size_t)k * k);
+  double* ZP = c->tbuf<double>("postZP", (size_t)k * k);
+  float* PA = c->tbuf<float>("PA", (size_t)c->nA * ldk);
+  float* PA2 = c->tbuf<float>("PA2", (size_t)c->nB * ldk);
+  const int64_t cap = (int64_t)gram_tsk_partials(c->nA, k, k);
+  double* part = c->tbuf<double>("gram_part_post", (size_t)cap);
+  // P_A = W Phi diag(pinv(lambda)) = (diag(pinv lambda) Phi^T W^T)^T  (CommunityDetection.cpp:98-100)
+  ck(phi_scaled(k, c->phi, c->lambda, c->cfg.pinv_tol, F, s), "F");
+  ck(panel_times_small(c->W, ldk, k, c->nA, F, k, k, PA, ldk, s), "PA");
+  // pi_a needs Z_B_part2^T (Z_B_part1^T P_A) (CommunityDetection.cpp:101)
+  ck(gram_tsk(c->Zb1, ldk, k, PA, ldk, k, c->nA, 1.0, ZP, part, cap, s), "Zb1^T PA");
+  ck(panel_times_small(c->Ub, ldk, k, c->nB, ZP, k, k, PA2, ldk, s), "PA2");
+  const float tau = c->cfg.tau;
+  const DevCsr &XA = c->g[0], &BA = c->g[3], &CA = c->g[4], &BAt = c->gt[3];
+  ck(unwhiten_normprob(XA.rp, XA.ci, XA.val, XA.n_rows, PA, ldk, k, tau, 0, c->pi, c->bits, s), "pi_x");
+  ck(unwhiten_normprob(BAt.rp, BAt.ci, BAt.val, BAt.n_rows, PA2, ldk, k, tau, c->nX, c->pi, c->bits, s), "pi_a");
+  ck(unwhiten_normprob(BA.rp, BA.ci, BA.val, BA.n_rows, PA, ldk, k, tau, c->nX + c->nA, c->pi, c->bits, s), "pi_b");
+  ck(unwhiten_normprob(CA.rp, CA.ci, CA.val, CA.n_rows, PA, ldk, k, tau, c->nX + c->nA + c->nB, c->pi, c->bits, s), "pi_c");
+  c->have_post = true;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint form: L(Phi) = theta sum_ij (phi_i.phi_j)^3 - 2 sum_i That(phi_i,phi_i,phi_i)
+
+namespace {
+
+struct PhiSwap {
+  mmsb_ctx* c;
+  float* saved;
+  double* phi64;
+  PhiSwap(mmsb_ctx* ctx, const double* phi_host) : c(ctx), saved(ctx->phi) {
+    const int k = c->k;
+    phi64 = c->tbuf<double>("loss_phi64", (size_t)k * k);
+    c->phi = c->tbuf<float>("loss_phi32", (size_t)k * k);
+    ck(cudaMemcpyAsync(phi64, phi_host, sizeof(double) * k * k, cudaMemcpyHostToDevice, c->s), "H2D phi");
+    ck(f64_to_f32(phi64, c->phi, (int64_t)k * k, c->s), "phi32");
+  }
+  ~PhiSwap() { c->phi = saved; }
+};
+
+void check_range(mmsb_ctx* c, int64_t& begin, int64_t& count) {
+  if (!c->have_y) throw MmsbError(MMSB_ERR_STATE, "loss needs whitened data");
+  if (c->k > 128) throw MmsbError(MMSB_ERR_UNSUPPORTED, "STPM kernels support k <= 128");
+  if (count <= 0) {
+    begin = 0;
+    count = c->nX;
+  }
+  if (begin < 0 || begin + count > c->nX) throw MmsbError(MMSB_ERR_INVALID_ARG, "node range");
+}
+
+}  // namespace
+
+double pipeline_loss(mmsb_ctx* c, const double* phi, int64_t begin, int64_t count) {
+  check_range(c, begin, count);
+  const int k = c->k;
+  const double a0 = c->cfg.alpha0;
+  const double p0 = (a0 + 1.0) * (a0 + 2.0) / 2.0, p1 = a0 * a0, p2 = -a0 * (a0 + 1.0) / 2.0;
+  PhiSwap sw(c, phi);
+  float* G = c->tbuf<float>("G", (size_t)k * k);
+  double* S = c->tbuf<double>("loss_S", (size_t)k * k);
+  stpm_pass(c, kModeLoss, 0, 1, 2, begin, count, p0, p1, p2, 1.0, G, c->dscalar + 1);
+  ck(dgemm_small(true, false, k, k, k, 1.0, sw.phi64, k, sw.phi64, k, 0.0, S, k, c->s), "S");
+  ck(cube_sum(k * k, S, c->cfg.theta, c->dscalar + 2, c->s), "cube");
+  double h[2] = {0, 0};
+  ck(cudaMemcpyAsync(h, c->dscalar + 1, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->s), "D2H");
+  ck(cudaStreamSynchronize(c->s), "sync");
+  return h[1] - 2.0 * h[0];
+}
+
+void pipeline_loss_grad(mmsb_ctx* c, const double* phi, int64_t begin, int64_t count,
+                        double* dphi) {
+  check_range(c, begin, count);
+  const int k = c->k;
+  const double a0 = c->cfg.alpha0;
+  const double p0 = (a0 + 1.0) * (a0 + 2.0) / 2.0, p1 = a0 * a0, p2 = -a0 * (a0 + 1.0) / 2.0;
+  PhiSwap sw(c, phi);
+  float* G = c->tbuf<float>("G", (size_t)k * k);
+  double* S = c->tbuf<double>("loss_S", (size_t)k * k);
+  double* S2 = c->tbuf<double>("loss_S2", (size_t)k * k);
+  double* out = c->tbuf<double>("loss_grad", (size_t)k * k);
+  double* dT = c->tbuf<double>("loss_dT", (size_t)k * k);
+  // dT: column i = d That_i / d phi_i (three partials of the cubic form)
+  stpm_pass(c, kModeAdjoint, 0, 1, 2, begin, count, p0, p1, p2, 1.0 / (double)count, G, nullptr);
+  ck(f32_to_f64(G, dT, (int64_t)k * k, c->s), "dT");
+  // 6 theta Phi (S o S) - 2 dT
+  ck(dgemm_small(true, false, k, k, k, 1.0, sw.phi64, k, sw.phi64, k, 0.0, S, k, c->s), "S");
+  ck(hadamard_square((int64_t)k * k, S, S2, c->s), "S2");
+  ck(dgemm_small(false, false, k, k, k, 6.0 * c->cfg.theta, sw.phi64, k, S2, k, 0.0, out, k, c->s), "O");
+  ck(axpy_f64((int64_t)k * k, -2.0, dT, out, c->s), "grad");
+  ck(cudaMemcpyAsync(dphi, out, sizeof(double) * k * k, cudaMemcpyDeviceToHost, c->s), "D2H");
+  ck(cudaStreamSynchronize(c->s), "sync");
+}

@@ -1,0 +1,284 @@
+/*
+ * mmsb.h -- C ABI of the GB300-native MMSB tensor-method pipeline.
+ *
+ * The pipeline is the reference's community-detection path
+ *   whitening  ->  whitened data y = W^T G^T  ->  tensor power method  ->
+ *   unwhitening + normalisation,
+ * i.e. CommunityDetectionSoftware_CPU/CommunityDetection/CommunityDetection.cpp:16-149
+ * (CPU tree) and CommunityDetectionSoftware_GPU/stpm.c:132-1015 (GPU tree).
+ *
+ * Conventions
+ *   - every call returns mmsb_status (MMSB_OK == 0); nothing calls exit();
+ *     the reference exits with 1 on file errors (IOfn.cpp:30-34,
+ *     GPU/pre_proc.c:54-58) and 2 on library errors (GPU/pre_proc.c:96-109);
+ *   - dense matrices are column-major, like Eigen's default and CULA;
+ *   - all pointers passed to the API are HOST pointers; the library owns the
+ *     device copies and one CUDA stream per context;
+ *   - a context is not thread-safe, except mmsb_request_stop();
+ *   - graph blocks are CSR with int64 row offsets and int32 column indices,
+ *     0-based (the text readers convert the reference's 1-based COO).
+ */
+#ifndef MMSB_H_
+#define MMSB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MMSB_ABI_VERSION 1
+
+typedef enum mmsb_status {
+  MMSB_OK = 0,
+  MMSB_ERR_INVALID_ARG = 1,
+  MMSB_ERR_CUDA = 2,
+  MMSB_ERR_OUT_OF_MEMORY = 3,
+  MMSB_ERR_STATE = 4,      /* call out of order (e.g. stpm before whiten) */
+  MMSB_ERR_NUMERICAL = 5,  /* NaN/Inf or a factorisation that broke down */
+  MMSB_ERR_STOPPED = 6,    /* mmsb_request_stop() was honoured */
+  MMSB_ERR_IO = 7,
+  MMSB_ERR_TIMEOUT = 8,    /* a bounded device-side wait gave up */
+  MMSB_ERR_UNSUPPORTED = 9
+} mmsb_status;
+
+/* The five adjacency blocks the reference reads (CommunityDetection.cpp:30-34,
+ * 47-49, 94-95): rows x cols. */
+enum {
+  MMSB_BLOCK_XA = 0, /* n_X x n_A  (Gx_a) */
+  MMSB_BLOCK_XB = 1, /* n_X x n_B  (Gx_b) */
+  MMSB_BLOCK_XC = 2, /* n_X x n_C  (Gx_c) */
+  MMSB_BLOCK_BA = 3, /* n_B x n_A  (Gb_a) */
+  MMSB_BLOCK_CA = 4, /* n_C x n_A  (Gc_a) */
+  MMSB_NUM_BLOCKS = 5
+};
+
+typedef enum mmsb_stpm_method {
+  /* tensorDecom_alpha0 (CPU/Util.cpp:131-184): full-batch power iteration,
+   * lambda = ||T(I,phi,phi)||^3, column normalisation, MINITER/MAXITER/TOLERANCE */
+  MMSB_STPM_BATCH_POWER = 0,
+  /* minibatch stochastic update with the Diff_Loss gradient (CPU/Util.cpp:257-304)
+   * and re-orthonormalisation after every step (GPU/stpm.c:774-786) */
+  MMSB_STPM_ONLINE = 1,
+  /* the same schedule driven by the exact adjoint of the implicit tensor loss
+   * L(Phi) = theta*sum_ij (phi_i.phi_j)^3 - 2*sum_i T(phi_i,phi_i,phi_i) */
+  MMSB_STPM_ADJOINT = 2
+} mmsb_stpm_method;
+
+typedef enum mmsb_precision {
+  MMSB_PREC_FP32 = 0, /* y, Phi and every bulk product in FP32 */
+  MMSB_PREC_BF16 = 1  /* y and Phi in BF16 on the tensor cores, FP32 accumulation */
+} mmsb_precision;
+
+typedef struct mmsb_config {
+  int32_t k;              /* KHID: number of communities */
+  double alpha0;          /* Dirichlet concentration */
+  int32_t datatype;       /* DATATYPE: 0 binary, 1 weighted (IOfn.cpp:40-49) */
+  int32_t stpm_method;    /* mmsb_stpm_method */
+  int32_t precision;      /* mmsb_precision */
+  int32_t sweeps;         /* online/adjoint: passes over the X partition */
+  int32_t minibatch;      /* online/adjoint: nodes per update */
+  double lr0;             /* online/adjoint: beta_t = lr0 / (1 + t) */
+  double theta;           /* weight of the orthogonality term of the loss */
+  int32_t min_iter;       /* batch power: MINITER  (CPU/stdafx.h:57) */
+  int32_t max_iter;       /* batch power: MAXITER  (CPU/stdafx.h:58) */
+  double tol;             /* batch power: TOLERANCE (CPU/stdafx.h:59) */
+  double pinv_tol;        /* pinv threshold, TOLERANCE in CPU/Spectral.cpp:44-68 */
+  int32_t nystrom_rows_factor; /* Nystrom branch iff rows > factor*k (Spectral.cpp:173) */
+  int32_t normalize;      /* NORMALIZE (CPU/stdafx.h:60): moments scaled by 1/n_X */
+  uint64_t seed;          /* Gaussian sketch panel and initial Phi */
+  float tau;              /* community-set threshold on normalised Pi */
+  int32_t device;         /* CUDA device ordinal */
+} mmsb_config;
+
+/* One CSR block (host memory).  val == NULL means binary (all ones). */
+typedef struct mmsb_csr {
+  int64_t n_rows;
+  int64_t n_cols;
+  int64_t nnz;
+  const int64_t* row_ptr; /* n_rows + 1 */
+  const int32_t* col_idx; /* nnz */
+  const float* val;       /* nnz or NULL */
+} mmsb_csr;
+
+/* Device time of each stage of the last call, milliseconds (CUDA events on
+ * the context's stream), plus iteration counters. */
+typedef struct mmsb_stats {
+  double whiten_ms;
+  double ydata_ms;
+  double stpm_ms;
+  double post_ms;
+  double total_ms;
+  double spmm_ms;          /* summed time of the whitening SpMM launches */
+  double spmm_bytes;       /* algorithmic bytes of those launches */
+  int64_t spmm_launches;
+  int64_t stpm_steps;      /* minibatch updates (online/adjoint) or iterations (batch) */
+  int64_t node_updates;    /* n_X * sweeps (online/adjoint) or n_X * iterations */
+  double stpm_last_error;  /* batch power: last ||Phi - Phi_old||_F */
+  int64_t kernel_launches; /* launches of this library's kernels by the last call */
+  int64_t polar_iterations; /* Newton-Schulz iterations summed over the STPM steps */
+} mmsb_stats;
+
+typedef struct mmsb_ctx mmsb_ctx;
+
+/* ---- configuration and lifetime ---------------------------------------- */
+
+/* Fills the reference's defaults: alpha0 1, binary, batch power with
+ * MINITER 100 / MAXITER 10000 / TOLERANCE 1e-6 (CPU/stdafx.h:56-60),
+ * pinv tolerance 1e-6, Nystrom factor 20, NORMALIZE on; online schedule
+ * 10 sweeps, minibatch 100, beta_t = 1/(1+t), theta 1. */
+void mmsb_config_default(mmsb_config* cfg);
+
+/* Replaces the reference's globals NX..KHID/alpha0/DATATYPE
+ * (CPU/CommunityDetection.cpp:9-26) and the GPU tree's device choice
+ * (GPU/stpm.c:1111-1118). */
+mmsb_status mmsb_create(const mmsb_config* cfg, mmsb_ctx** out);
+void mmsb_destroy(mmsb_ctx* ctx);
+
+/* Copies the five blocks to the device and builds their transposes there.
+ * Replaces read_G_sparse x5 (CPU/IOfn.cpp:21-54; CommunityDetection.cpp:47-49,94-95)
+ * and read_G (GPU/pre_proc.c:49-80). */
+mmsb_status mmsb_upload_graph(mmsb_ctx* ctx, const mmsb_csr blocks[MMSB_NUM_BLOCKS]);
+
+/* ---- pipeline stages ------------------------------------------------------ */
+
+/* second_whiten (CPU/Util.cpp:38-127) plus the whitened data and means
+ * (CommunityDetection.cpp:66-68); GPU tree: pre_proc (GPU/pre_proc.c:112-372).
+ * sketches == NULL: Gaussian sketch panels N(0,1) drawn on the device from
+ * cfg.seed.  Otherwise sketches[0..2] are R_c (n_B x 2k), R_b (n_C x 2k) and
+ * R_a (n_A x 2k), column-major, used where random_embedding_mat
+ * (CPU/Spectral.cpp:118-134) is called. */
+mmsb_status mmsb_whiten(mmsb_ctx* ctx, const double* const* sketches);
+
+/* Tensor decomposition: tensorDecom_alpha0 (CPU/Util.cpp:131-184) or the
+ * GPU tree's STPM loop (GPU/stpm.c:497-809), per cfg.stpm_method.
+ * phi0 == NULL: orthonormal start drawn from cfg.seed; else k x k column-major. */
+mmsb_status mmsb_stpm(mmsb_ctx* ctx, const double* phi0);
+
+/* Unwhitening, concatenation [X|A|B|C], normProbMatrix and the community-set
+ * threshold: CommunityDetection.cpp:98-139 / GPU/post_proc.c:62-119. */
+mmsb_status mmsb_postproc(mmsb_ctx* ctx);
+
+/* mmsb_whiten(NULL) + mmsb_stpm(NULL) + mmsb_postproc on the uploaded graph. */
+mmsb_status mmsb_run(mmsb_ctx* ctx);
+
+/* ---- results (host buffers) --------------------------------------------- */
+
+int64_t mmsb_num_nodes(const mmsb_ctx* ctx); /* n_X + n_A + n_B + n_C */
+
+/* Normalised memberships, k x N column-major over the node order [X|A|B|C]
+ * (CommunityDetection.cpp:121-139). */
+mmsb_status mmsb_get_pi(mmsb_ctx* ctx, float* pi);
+/* Community sets {i : pi(i,node) > tau}: N words of ceil(k/32) uint32 each. */
+mmsb_status mmsb_get_sets(mmsb_ctx* ctx, uint32_t* bits);
+mmsb_status mmsb_get_lambda(mmsb_ctx* ctx, double* lambda);  /* k */
+mmsb_status mmsb_get_phi(mmsb_ctx* ctx, double* phi);        /* k x k */
+/* W (n_A x k), Z_B_part1 (n_A x k), Z_B_part2 (k x n_B), Z_C_part1 (n_A x k),
+ * Z_C_part2 (k x n_C); any pointer may be NULL (CPU/Util.cpp:38-40 outputs). */
+mmsb_status mmsb_get_whitening(mmsb_ctx* ctx, double* W, double* zb1, double* zb2,
+                               double* zc1, double* zc2);
+mmsb_status mmsb_get_means(mmsb_ctx* ctx, double* mu_a, double* mu_b, double* mu_c);
+/* Whitened data k x n_X column-major (Data_a_G/Data_b_G/Data_c_G) and the
+ * whitened means (k each); any pointer may be NULL. */
+mmsb_status mmsb_get_whitened(mmsb_ctx* ctx, float* ya, float* yb, float* yc,
+                              double* ymu_a, double* ymu_b, double* ymu_c);
+mmsb_status mmsb_get_stats(const mmsb_ctx* ctx, mmsb_stats* out);
+
+/* ---- stage inputs (stage-wise parity with the reference) ---------------- */
+
+/* Installs W, Z_B_part1/2, Z_C_part1/2 and the means (same shapes as the
+ * getters) and computes the whitened data from them on the device. */
+mmsb_status mmsb_set_whitening(mmsb_ctx* ctx, const double* W, const double* zb1,
+                               const double* zb2, const double* zc1, const double* zc2,
+                               const double* mu_a, const double* mu_b, const double* mu_c);
+/* Installs whitened data (k x n_X column-major) and whitened means. */
+mmsb_status mmsb_set_whitened(mmsb_ctx* ctx, const double* ya, const double* yb,
+                              const double* yc, const double* ymu_a, const double* ymu_b,
+                              const double* ymu_c);
+/* Installs Phi (k x k) and lambda (k) for mmsb_postproc. */
+mmsb_status mmsb_set_phi_lambda(mmsb_ctx* ctx, const double* phi, const double* lambda);
+
+/* ---- adjoint form ------------------------------------------------------- */
+
+/* Implicit tensor loss over the whitened nodes [node_begin, node_begin+count)
+ * (count <= 0: all of X):
+ *   L(Phi) = theta * sum_ij (phi_i . phi_j)^3 - 2 * sum_i That(phi_i, phi_i, phi_i),
+ *   That(u,u,u) = mean_x [p0 (u.a)(u.b)(u.c) + p2((u.a)(u.b)(u.mc) + (u.a)(u.mb)(u.c)
+ *                 + (u.ma)(u.b)(u.c))] + p1 (u.ma)(u.mb)(u.mc),
+ * p0 = (a0+1)(a0+2)/2, p1 = a0^2, p2 = -a0(a0+1)/2 (CPU/Util.cpp:289-291).
+ * This is ||T - sum phi^{x3}||^2 - ||T||^2 for theta = 1.  Forward returns L;
+ * backward returns dL/dPhi (k x k column-major), recomputing Z = Phi^T y. */
+mmsb_status mmsb_stpm_loss_fwd(mmsb_ctx* ctx, const double* phi, int64_t node_begin,
+                               int64_t count, double* loss);
+mmsb_status mmsb_stpm_loss_bwd(mmsb_ctx* ctx, const double* phi, int64_t node_begin,
+                               int64_t count, double* dphi);
+
+/* ---- control ------------------------------------------------------------ */
+
+/* Thread-safe; mirrors forceExit_flag (GPU/stpm.c:61,754-758).  The STPM loop
+ * stops at the next step boundary and the call returns MMSB_ERR_STOPPED. */
+void mmsb_request_stop(mmsb_ctx* ctx);
+const char* mmsb_last_error(const mmsb_ctx* ctx);
+const char* mmsb_status_string(mmsb_status st);
+/* Writes a buffer larger than L2 on the context's stream (benchmark hygiene). */
+mmsb_status mmsb_flush_l2(mmsb_ctx* ctx);
+mmsb_status mmsb_synchronize(mmsb_ctx* ctx);
+
+/* ---- single operators (tests and kernel benchmarks) ----------------------- */
+
+/* Y (n_rows x p, row-major) = alpha * G * P (P: n_cols x p, row-major);
+ * with transpose != 0, Y (n_cols x p) = alpha * G^T * P (P: n_rows x p). */
+mmsb_status mmsb_op_spmm(const mmsb_csr* g, int transpose, const float* P, int64_t p,
+                         float alpha, float* Y);
+/* Symmetric eigen-decomposition of an n x n matrix (column-major, n <= 512),
+ * eigenvalues descending; vectors column-major n x n. */
+mmsb_status mmsb_op_symeig(const double* A, int32_t n, double* evals, double* evecs);
+
+/* ---- synthetic MMSB graphs ---------------------------------------------- */
+
+typedef struct mmsb_gen_params {
+  int64_t n;        /* nodes, split uniformly at random into X, A, B, C */
+  int32_t k;        /* communities */
+  double alpha0;    /* Dirichlet(alpha0/k * 1) memberships */
+  double p_in;      /* B diagonal */
+  double p_out;     /* B off-diagonal */
+  uint64_t seed;
+  int32_t keep_pi;  /* keep the ground-truth memberships */
+} mmsb_gen_params;
+
+typedef struct mmsb_host_graph mmsb_host_graph;
+
+mmsb_status mmsb_generate(const mmsb_gen_params* params, mmsb_host_graph** out);
+void mmsb_host_graph_free(mmsb_host_graph* g);
+/* part sizes n_X, n_A, n_B, n_C; undirected edge count */
+mmsb_status mmsb_host_graph_info(const mmsb_host_graph* g, int64_t part_sizes[4],
+                                 int64_t* n_edges);
+/* Borrowed view of one block, valid until mmsb_host_graph_free. */
+mmsb_status mmsb_host_graph_block(const mmsb_host_graph* g, int which, mmsb_csr* out);
+/* Ground-truth memberships k x N column-major in [X|A|B|C] order (keep_pi). */
+mmsb_status mmsb_host_graph_pi(const mmsb_host_graph* g, float* pi);
+
+/* ---- file contract (CPU/IOfn.cpp:21-67) ----------------------------------- */
+
+/* Reads a 1-based COO text block ("row col" or "row col value" per line,
+ * datatype 0/1).  compat != 0 reproduces the reference reader exactly:
+ * the last triplet is pushed twice when the file ends after a newline
+ * (IOfn.cpp:36-49 feof loop) and duplicates are summed, then entries with
+ * |v| <= 1e-6 are pruned.  compat == 0 de-duplicates instead.  The block
+ * is owned by a host graph handle freed with mmsb_host_graph_free. */
+mmsb_status mmsb_read_coo(const char* path, int64_t n_rows, int64_t n_cols,
+                          int32_t datatype, int32_t compat, mmsb_host_graph** out);
+/* Writes "row\tcol\tvalue" 1-based triplets of the nonzeros of a column-major
+ * rows x cols matrix in column order, values with 6 significant digits,
+ * as write_pi (IOfn.cpp:57-67) prints them. */
+mmsb_status mmsb_write_triplets_f32(const char* path, const float* m, int64_t rows,
+                                    int64_t cols);
+mmsb_status mmsb_write_triplets_f64(const char* path, const double* m, int64_t rows,
+                                    int64_t cols);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MMSB_H_ */

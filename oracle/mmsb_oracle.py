@@ -1,0 +1,301 @@
+"""FP64 CPU restatement of the reference's MMSB tensor-method path -- the ORACLE.
+
+This module is test infrastructure: only tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg use it, always as the checker, never as the thing
+measured or shipped.  The GPU library never calls it.
+
+Parity is pinned by tests/golden/: fixtures produced by the reference's own CPU
+implementation (CommunityDetectionSoftware_CPU, compiled unmodified by
+oracle/Makefile with a fixed srand seed, see oracle/ref_harness.cpp) on seeded
+synthetic graphs.  tests/test_oracle_golden.py checks every stage of this file
+against them.
+
+Each function cites the reference code it restates (paths relative to
+CommunityDetectionSoftware_CPU/CommunityDetection/ unless noted).  The
+reference forms the n x n pair operators explicitly (Util.cpp:54-62); here they
+are applied implicitly as chains of sparse products, which is the same algebra
+in a different association order.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+
+TOLERANCE = 1e-6  # stdafx.h:59
+
+
+def pinv_vector(v, tol=TOLERANCE):
+    """Spectral.cpp:50-57: elementwise 1/x, 0 where |x| <= tol."""
+    v = np.asarray(v, dtype=np.float64)
+    out = np.zeros_like(v)
+    m = np.abs(v) > tol
+    out[m] = 1.0 / v[m]
+    return out
+
+
+def orthogonalize_cols(Y, tol=TOLERANCE):
+    """Spectral.cpp:146-166: modified Gram-Schmidt, columns with norm <= tol -> 0."""
+    Y = np.array(Y, dtype=np.float64, copy=True)
+    c = Y.shape[1]
+    for j in range(c):
+        for i in range(j):
+            Y[:, j] -= (Y[:, i] @ Y[:, j]) * Y[:, i]
+        nrm = np.sqrt(Y[:, j] @ Y[:, j])
+        Y[:, j] *= (1.0 / nrm) if nrm > tol else 0.0
+    return Y
+
+
+def svd_sym_nystrom(M, k, rows_factor=20, tol=TOLERANCE):
+    """Spectral.cpp:169-223 (SVD_symNystrom_sparse) for an n x 2k input.
+
+    Returns (U: n x k, sigma: k).  Nystrom branch when rows > rows_factor*k:
+    Q = orth(M); C = M * Q[:cols]; Z = C^T C; U = C V_k S_k^{-1/2}, sigma = sqrt(S_k).
+    Otherwise the thin SVD of M (Spectral.cpp:216-221)."""
+    M = np.asarray(M, dtype=np.float64)
+    n, cols = M.shape
+    if n > rows_factor * k:
+        if cols > 2 * k:
+            raise NotImplementedError("sketching branch (Spectral.cpp:176-178) is unused here")
+        Q = orthogonalize_cols(M, tol)
+        QQ = Q[:cols, :] if cols < Q.shape[0] else Q
+        C = M @ QQ
+        Z = C.T @ C
+        evals, evecs = np.linalg.eigh(Z)
+        order = np.argsort(evals)[::-1]
+        S = np.maximum(evals[order][:k], 0.0)
+        V = evecs[:, order][:, :k]
+        sigma = np.sqrt(S)
+        U = (C @ V) * pinv_vector(np.sqrt(S), tol)
+        return U, sigma
+    U, s, _ = np.linalg.svd(M, full_matrices=False)
+    return U[:, :k], s[:k]
+
+
+def pinv_component(X, XT, R, k, rows_factor=20, tol=TOLERANCE):
+    """Spectral.cpp:296-315 via SVD_asymNystrom_sparse (:225-246).
+
+    X / XT apply the (implicit) matrix and its transpose to a dense panel.
+    Returns (V: cols x k, U: rows x k, L_inv: k) with pinv(X) ~ V diag(L_inv) U^T."""
+    gram = XT(X(R))                        # X^T (X R)
+    V, s = svd_sym_nystrom(gram, k, rows_factor, tol)
+    Linv_sqrt = np.sqrt(pinv_vector(s, tol))
+    U = X(V) * Linv_sqrt                   # X V L^{-1/2}
+    L = np.sqrt(s)
+    return V, U, pinv_vector(L, tol)
+
+
+def column_means(G, inv):
+    return inv * np.asarray(G.sum(axis=0)).ravel()
+
+
+def second_whiten(Gxa, Gxb, Gxc, k, alpha0, sketches, rows_factor=20, normalize=True,
+                  tol=TOLERANCE):
+    """Util.cpp:38-127.  sketches = (R_c: n_B x 2k, R_b: n_C x 2k, R_a: n_A x 2k).
+
+    Returns dict W, Zb1, Zb2, Zc1, Zc2, mu_a, mu_b, mu_c (+ intermediates)."""
+    nx = Gxa.shape[0]
+    inv = 1.0 / nx if normalize else 1.0
+    mu_a, mu_b, mu_c = column_means(Gxa, inv), column_means(Gxb, inv), column_means(Gxc, inv)
+    Gxa, Gxb, Gxc = (sp.csr_matrix(g, dtype=np.float64) for g in (Gxa, Gxb, Gxc))
+    GaT, GbT, GcT = Gxa.T.tocsr(), Gxb.T.tocsr(), Gxc.T.tocsr()
+    zb_num = lambda P: inv * (GaT @ (Gxc @ P))    # Gx_a^T Gx_c (n_A x n_C)
+    zb_den = lambda P: inv * (GbT @ (Gxc @ P))    # Gx_b^T Gx_c (n_B x n_C)
+    zb_den_T = lambda P: inv * (GcT @ (Gxb @ P))
+    zc_num = lambda P: inv * (GaT @ (Gxb @ P))    # Gx_a^T Gx_b (n_A x n_B)
+    zc_den = lambda P: inv * (GcT @ (Gxb @ P))    # Gx_c^T Gx_b (n_C x n_B)
+    zc_den_T = lambda P: inv * (GbT @ (Gxc @ P))
+    R_c, R_b, R_a = (np.asarray(r, dtype=np.float64) for r in sketches)
+
+    V_c, U_c, Linv_c = pinv_component(zc_den, zc_den_T, R_c, k, rows_factor, tol)
+    V_b, U_b, Linv_b = pinv_component(zb_den, zb_den_T, R_b, k, rows_factor, tol)
+    Zc1 = zc_num(V_c) * Linv_c                     # term_na_k  (Util.cpp:83-84)
+    Zc2 = U_c.T                                    # (Util.cpp:85)
+    core = U_c.T @ zc_den(U_b)                     # term_k_k   (Util.cpp:90)
+    if np.count_nonzero(core) < k:                 # (Util.cpp:91-94)
+        core[np.arange(k), np.arange(k)] = 1.0
+    Zb1 = zb_num(V_b) * Linv_b                     # term_k_na^T (Util.cpp:96-97)
+    Zb2 = U_b.T                                    # (Util.cpp:98)
+    M2 = (alpha0 + 1.0) * ((Zc1 @ core) @ (Zb1.T @ R_a))      # (Util.cpp:103-104)
+    M2 -= alpha0 * np.outer(mu_a, mu_a @ R_a)                  # (Util.cpp:110-112)
+    Uw, sw = svd_sym_nystrom(M2, k, rows_factor, tol)          # (Util.cpp:116)
+    W = Uw * pinv_vector(np.sqrt(sw), tol)                     # (Util.cpp:118-123)
+    return dict(W=W, Zb1=Zb1, Zb2=Zb2, Zc1=Zc1, Zc2=Zc2, mu_a=mu_a, mu_b=mu_b, mu_c=mu_c,
+                core=core, M2=M2, sw=sw, V_c=V_c, U_c=U_c, V_b=V_b, U_b=U_b,
+                Linv_c=Linv_c, Linv_b=Linv_b)
+
+
+def whitened_data(Gxa, Gxb, Gxc, wh):
+    """CommunityDetection.cpp:66-68: Data_P = (effective W_P)^T G_XP^T, k x n_X."""
+    W = wh["W"]
+    Wb = wh["Zb2"].T @ (wh["Zb1"].T @ W)           # ((W^T Zb1) Zb2)^T
+    Wc = wh["Zc2"].T @ (wh["Zc1"].T @ W)
+    Da = np.asarray((Gxa @ W).T)
+    Db = np.asarray((Gxb @ Wb).T)
+    Dc = np.asarray((Gxc @ Wc).T)
+    return dict(Da=Da, Db=Db, Dc=Dc, Da_mu=W.T @ wh["mu_a"], Db_mu=Wb.T @ wh["mu_b"],
+                Dc_mu=Wc.T @ wh["mu_c"], Wb=Wb, Wc=Wc)
+
+
+def alpha_coeffs(alpha0):
+    """Util.cpp:289-291: p0, p1, p2."""
+    return ((alpha0 + 1.0) * (alpha0 + 2.0) / 2.0, alpha0 * alpha0,
+            -alpha0 * (alpha0 + 1.0) / 2.0)
+
+
+def tensor_decomp_batch(y, alpha0, phi0, min_iter=100, max_iter=10000, tol=TOLERANCE):
+    """tensorDecom_alpha0, Util.cpp:131-184 (with tensor_form_* :187-206).
+
+    Returns (lambda, phi, iterations, last_error)."""
+    Da, Db, Dc = y["Da"], y["Db"], y["Dc"]
+    a_mu, b_mu, c_mu = y["Da_mu"], y["Db_mu"], y["Dc_mu"]
+    nx = Da.shape[1]
+    inv_x = 1.0 / nx
+    p_main = (alpha0 + 1.0) * (alpha0 + 2.0) / 2.0 * inv_x
+    p_s1 = -alpha0 * (alpha0 + 1.0) / 2.0 * inv_x
+    p_s0 = alpha0 * alpha0
+    pair_ab, pair_ac, pair_bc = Da @ Db.T, Da @ Dc.T, Db @ Dc.T
+    phi = np.array(phi0, dtype=np.float64, copy=True)
+    it = 1
+    while True:
+        old = phi
+        ZB, ZC = Db.T @ old, Dc.T @ old                       # n_X x k
+        main = Da @ (ZB * ZC)
+        mb, mc = old.T @ b_mu, old.T @ c_mu
+        s1 = (np.outer(a_mu, np.einsum("ji,jl,li->i", old, pair_bc, old))
+              + mb * (pair_ac @ old) + mc * (pair_ab @ old))
+        s0 = np.outer(a_mu, mb * mc)
+        new = p_main * main + p_s1 * s1 + p_s0 * s0
+        lam = np.sum(new ** 2, axis=0) ** 1.5
+        phi = new / np.linalg.norm(new, axis=0)
+        err = np.nan
+        if it >= min_iter:
+            err = np.linalg.norm(phi - old)
+            if err < tol or it > max_iter:
+                break
+        it += 1
+    return lam, phi, it, err
+
+
+def polar(M):
+    """Orthonormal polar factor U V^T of M (M = U S V^T)."""
+    U, _, Vt = np.linalg.svd(M)
+    return U @ Vt
+
+
+def online_grad_terms(phi, y, nodes, alpha0):
+    """Minibatch mean of the reference's per-sample second term
+    (The_second_term, Util.cpp:286-304): column i = mean_x t_i(x)."""
+    p0, p1, p2 = alpha_coeffs(alpha0)
+    A, B, C = y["Da"][:, nodes], y["Db"][:, nodes], y["Dc"][:, nodes]
+    ZA, ZB = phi.T @ A, phi.T @ B
+    mA, mB = phi.T @ y["Da_mu"], phi.T @ y["Db_mu"]
+    coef = p0 * ZA * ZB + p2 * (ZA * mB[:, None] + mA[:, None] * ZB)
+    d = p1 * mA * mB + p2 * np.mean(ZA * ZB, axis=1)
+    return C @ coef.T / A.shape[1] + np.outer(y["Dc_mu"], d)
+
+
+def diff_loss_step(phi, y, nodes, alpha0, lr, theta):
+    """Diff_Loss (Util.cpp:257-284) averaged over a minibatch:
+    Phi - lr * (3 theta Phi (Phi^T Phi)^2 - 3 G)."""
+    S = phi.T @ phi
+    O = phi @ (S * S)
+    G = online_grad_terms(phi, y, nodes, alpha0)
+    return phi - lr * (3.0 * theta * O - 3.0 * G)
+
+
+def loss_fwd(phi, y, nodes, alpha0, theta):
+    """L(Phi) = theta sum_ij (phi_i.phi_j)^3 - 2 sum_i That(phi_i,phi_i,phi_i)."""
+    p0, p1, p2 = alpha_coeffs(alpha0)
+    ZA, ZB, ZC = (phi.T @ y[n][:, nodes] for n in ("Da", "Db", "Dc"))
+    mA, mB, mC = (phi.T @ y[n] for n in ("Da_mu", "Db_mu", "Dc_mu"))
+    t = p0 * ZA * ZB * ZC + p2 * (ZA * ZB * mC[:, None] + ZA * mB[:, None] * ZC
+                                  + mA[:, None] * ZB * ZC)
+    That = t.mean(axis=1) + p1 * mA * mB * mC
+    S = phi.T @ phi
+    return theta * np.sum(S ** 3) - 2.0 * np.sum(That)
+
+
+def loss_bwd(phi, y, nodes, alpha0, theta):
+    """Exact gradient dL/dPhi of loss_fwd (k x k)."""
+    p0, p1, p2 = alpha_coeffs(alpha0)
+    A, B, C = (y[n][:, nodes] for n in ("Da", "Db", "Dc"))
+    ZA, ZB, ZC = phi.T @ A, phi.T @ B, phi.T @ C
+    mA, mB, mC = (phi.T @ y[n] for n in ("Da_mu", "Db_mu", "Dc_mu"))
+    b = A.shape[1]
+    dZA = p0 * ZB * ZC + p2 * (ZB * mC[:, None] + mB[:, None] * ZC)
+    dZB = p0 * ZA * ZC + p2 * (ZA * mC[:, None] + mA[:, None] * ZC)
+    dZC = p0 * ZA * ZB + p2 * (ZA * mB[:, None] + mA[:, None] * ZB)
+    dmA = p2 * np.mean(ZB * ZC, axis=1) + p1 * mB * mC
+    dmB = p2 * np.mean(ZA * ZC, axis=1) + p1 * mA * mC
+    dmC = p2 * np.mean(ZA * ZB, axis=1) + p1 * mA * mB
+    dT = ((A @ dZA.T + B @ dZB.T + C @ dZC.T) / b + np.outer(y["Da_mu"], dmA)
+          + np.outer(y["Db_mu"], dmB) + np.outer(y["Dc_mu"], dmC))
+    S = phi.T @ phi
+    return 6.0 * theta * phi @ (S * S) - 2.0 * dT
+
+
+def stpm_minibatches(nx, minibatch):
+    return [np.arange(s, min(s + minibatch, nx)) for s in range(0, nx, minibatch)]
+
+
+def tensor_values(phi, y, alpha0):
+    """lambda_i = That(phi_i, phi_i, phi_i) over all of X."""
+    nodes = np.arange(y["Da"].shape[1])
+    G = online_grad_terms(phi, y, nodes, alpha0)
+    return np.einsum("ji,ji->i", phi, G)
+
+
+def stpm_online(y, alpha0, phi0, sweeps, minibatch, lr0=1.0, theta=1.0, adjoint=False):
+    """Minibatch STPM: per step Phi <- polar(Phi - beta_t (3 theta O - 3 G))
+    (Diff_Loss, Util.cpp:257-284, minibatch-averaged; re-orthonormalised every
+    step like GPU/stpm.c:774-786), beta_t = lr0/(1+t).  adjoint=True uses
+    half the exact gradient of loss_fwd instead of 3 theta O - 3 G.
+    Returns (lambda, phi, steps) with lambda_i = That(phi_i,phi_i,phi_i) > 0."""
+    nx = y["Da"].shape[1]
+    phi = np.array(phi0, dtype=np.float64, copy=True)
+    t = 0
+    batches = stpm_minibatches(nx, minibatch)
+    for _ in range(sweeps):
+        for nodes in batches:
+            beta = lr0 / (1.0 + t)
+            if adjoint:
+                step = 0.5 * loss_bwd(phi, y, nodes, alpha0, theta)
+            else:
+                S = phi.T @ phi
+                step = 3.0 * theta * (phi @ (S * S)) - 3.0 * online_grad_terms(phi, y, nodes,
+                                                                                 alpha0)
+            phi = polar(phi - beta * step)
+            t += 1
+    phi = polar(phi)
+    lam = tensor_values(phi, y, alpha0)
+    sgn = np.where(lam < 0, -1.0, 1.0)
+    return lam * sgn, phi * sgn, t
+
+
+def norm_prob_matrix(P):
+    """normProbMatrix / normProbVector, Probability.cpp:33-121, column-wise."""
+    P = np.asarray(P, dtype=np.float64)
+    pos = np.where(P > 0, P, 0.0).sum(axis=0)
+    neg = np.where(P > 0, 0.0, P).sum(axis=0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        out = np.where(np.abs(pos) < np.abs(neg), -P / np.abs(neg), P / np.where(pos == 0, 1, np.abs(pos)))
+    out = np.maximum(out, 0.0)
+    zero = ~np.any(P != 0, axis=0)
+    out[:, zero] = P[:, zero]
+    return out
+
+
+def postprocess(Gxa, Gba, Gca, wh, lam, phi, tol=TOLERANCE):
+    """CommunityDetection.cpp:98-139: returns (pi_raw, pi) k x (n_X+n_A+n_B+n_C)."""
+    P_A = wh["W"] @ (phi * pinv_vector(lam, tol))          # (diag(1/lam) Phi^T W^T)^T
+    pi_x = (Gxa @ P_A).T
+    pi_b = (Gba @ P_A).T
+    pi_c = (Gca @ P_A).T
+    P_A2 = wh["Zb2"].T @ (wh["Zb1"].T @ P_A)
+    pi_a = (Gba.T @ P_A2).T
+    raw = np.concatenate([np.asarray(m) for m in (pi_x, pi_a, pi_b, pi_c)], axis=1)
+    return raw, norm_prob_matrix(raw)
+
+
+def community_sets(pi, tau):
+    return pi > tau

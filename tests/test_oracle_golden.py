@@ -1,0 +1,97 @@
+"""Pins the FP64 oracle (oracle/mmsb_oracle.py) to the reference's own outputs.
+
+Every stage is fed the reference's inputs for that stage (tests/golden/*.npz,
+produced by the reference's CPU implementation, see make_golden.py) and must
+reproduce the reference's outputs to FP64 round-off.  Column signs of
+eigenvector-derived matrices are implementation-defined (Eigen's JacobiSVD vs
+LAPACK), so W is compared after sign alignment and the Z factors through their
+sign-invariant products.
+"""
+import numpy as np
+
+from conftest import align_columns
+
+
+def rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
+
+
+def test_means(golden, oracle):
+    Gxa, Gxb, Gxc, _, _ = golden.scipy_blocks()
+    inv = 1.0 / Gxa.shape[0]
+    for G, n in ((Gxa, "mu_a"), (Gxb, "mu_b"), (Gxc, "mu_c")):
+        assert np.array_equal(oracle.column_means(G, inv), golden[n].ravel())
+
+
+def test_second_whiten(golden, oracle):
+    Gxa, Gxb, Gxc, _, _ = golden.scipy_blocks()
+    wh = oracle.second_whiten(Gxa, Gxb, Gxc, golden.k, golden.alpha0, golden.sketches())
+    W = golden["W"]
+    assert rel(align_columns(W, wh["W"]), W) < 1e-8
+    for a, b in (("Zb1", "Zb2"), ("Zc1", "Zc2")):
+        assert rel(wh[a] @ wh[b], golden[a] @ golden[b]) < 1e-8
+
+
+def test_whitened_data(golden, oracle):
+    Gxa, Gxb, Gxc, _, _ = golden.scipy_blocks()
+    y = oracle.whitened_data(Gxa, Gxb, Gxc, golden.whitening())
+    for n in ("Da", "Db", "Dc"):
+        assert rel(y[n], golden[n]) < 1e-10
+    for n in ("Da_mu", "Db_mu", "Dc_mu"):
+        assert rel(y[n], golden[n].ravel()) < 1e-10
+
+
+def test_batch_power(golden, oracle):
+    lam, phi, it, err = oracle.tensor_decomp_batch(golden.whitened(), golden.alpha0,
+                                                   golden["phi0"])
+    assert rel(lam, golden["lambda"].ravel()) < 1e-8
+    assert np.abs(phi - golden["phi"]).max() < 1e-8
+
+
+def test_postprocess(golden, oracle):
+    _, _, _, Gba, Gca = golden.scipy_blocks()
+    Gxa = golden.scipy_blocks()[0]
+    raw, pi = oracle.postprocess(Gxa, Gba, Gca, golden.whitening(), golden["lambda"].ravel(),
+                                 golden["phi"])
+    assert rel(raw, golden["pi_raw"]) < 1e-6
+    assert np.abs(pi - golden["pi"]).max() < 1e-6
+
+
+def test_diff_loss_step(golden, oracle):
+    y = golden.whitened()
+    step = oracle.diff_loss_step(golden["phi0"], y, np.array([0]), golden.alpha0, 1e-7, 10000.0)
+    assert np.abs(step - golden["diffloss_phi"]).max() < 1e-12
+    G = oracle.online_grad_terms(golden["phi0"], y, np.array([0]), golden.alpha0)
+    assert rel(G[:, 0], golden["second_term"].ravel()) < 1e-12
+
+
+def test_norm_prob_edge_cases(golden, oracle):
+    out = oracle.norm_prob_matrix(golden["normprob_in"])
+    assert np.array_equal(out, golden["normprob_out"])
+
+
+def test_loss_gradient_matches_central_differences(golden_cfg1, oracle):
+    """The adjoint's FP64 reference: dL/dPhi against central differences (h = 1e-6)."""
+    g = golden_cfg1
+    y = g.whitened()
+    rng = np.random.default_rng(0)
+    phi = g["phi0"] + 0.05 * rng.standard_normal(g["phi0"].shape)
+    nodes = np.arange(0, 300)
+    grad = oracle.loss_bwd(phi, y, nodes, g.alpha0, 1.0)
+    h = 1e-6
+    for _ in range(20):
+        d = rng.standard_normal(phi.shape)
+        d /= np.linalg.norm(d)
+        fd = (oracle.loss_fwd(phi + h * d, y, nodes, g.alpha0, 1.0)
+              - oracle.loss_fwd(phi - h * d, y, nodes, g.alpha0, 1.0)) / (2 * h)
+        an = np.sum(grad * d)
+        assert abs(fd - an) <= 1e-6 * max(1.0, abs(an))
+
+
+def test_online_stpm_recovers_orthonormal_components(golden_cfg1, oracle):
+    g = golden_cfg1
+    lam, phi, steps = oracle.stpm_online(g.whitened(), g.alpha0, g["phi0"], sweeps=10,
+                                         minibatch=100)
+    assert steps == 100
+    assert np.abs(phi.T @ phi - np.eye(g.k)).max() < 1e-10
+    assert np.all(lam > 0)
