@@ -153,73 +153,82 @@ def peaks():
 
 # ---------------------------------------------------------------------------
 
-def cpu_port_sample(mm, wl, graph=None, max_seconds=30.0):
-    """Times the FP64 oracle port on host cores: whitening once, STPM sweeps
-    until the time budget, unwhitening once; returns node-updates/s of the
-    full workload extrapolated from those measured parts."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import mmsb_oracle as O
-    if graph is None:
-        graph = make_graph(mm, wl)
-    Gxa, Gxb, Gxc, Gba, Gca = graph.scipy_blocks()
-    k, a0 = wl["k"], wl["alpha0"]
-    rng = np.random.default_rng(0)
-    nX, nA, nB, nC = graph.parts
-    sk = (rng.standard_normal((nB, 2 * k)), rng.standard_normal((nC, 2 * k)),
-          rng.standard_normal((nA, 2 * k)))
-    t0 = time.perf_counter()
-    wh = O.second_whiten(Gxa, Gxb, Gxc, k, a0, sk)
-    y = O.whitened_data(Gxa, Gxb, Gxc, wh)
-    t_whiten = time.perf_counter() - t0
-    phi = O.polar(rng.standard_normal((k, k)))
-    batches = O.stpm_minibatches(nX, wl["minibatch"])
-    p0, p1, p2 = O.alpha_coeffs(a0)
-    t1 = time.perf_counter()
-    steps = 0
-    budget = max(1.0, max_seconds - t_whiten)
-    for t, nodes in enumerate(batches):
-        beta = 1.0 / (1.0 + t)
-        S = phi.T @ phi
-        step = 3.0 * (phi @ (S * S)) - 3.0 * O.online_grad_terms(phi, y, nodes, a0)
-        phi = O.polar(phi - beta * step)
-        steps += 1
-        if time.perf_counter() - t1 > budget:
-            break
-    t_steps = time.perf_counter() - t1
-    t_sweep = t_steps / steps * len(batches)
-    t2 = time.perf_counter()
-    lam = O.tensor_values(phi, y, a0)
-    O.postprocess(Gxa, Gba, Gca, wh, lam, phi)
-    t_post = time.perf_counter() - t2
-    total = t_whiten + wl["sweeps"] * t_sweep + t_post
-    nu = nX * wl["sweeps"] / total
-    sample = (f"FP64 numpy/scipy port: whitening {t_whiten:.2f}s, {steps} of {len(batches)} "
-              f"minibatch steps of one sweep {t_steps:.2f}s, post {t_post:.2f}s; "
-              f"extrapolated to {wl['sweeps']} sweeps = {total:.1f}s per step")
-    return nu, sample, total
+class CpuPort:
+    """The FP64 oracle port of the reference path on the host cores.
+
+    Whitening and unwhitening are timed once; the STPM is timed per sweep (one
+    pass of minibatch updates over X).  node_updates_per_s() extrapolates the
+    whole job: n_X * sweeps / (whiten + sweeps * sweep + post)."""
+
+    def __init__(self, mm, wl, graph=None):
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import mmsb_oracle as O
+        O.FAST_GS = True  # vectorised Gram-Schmidt (same result to round-off)
+        self.O, self.wl = O, wl
+        self.graph = graph if graph is not None else make_graph(mm, wl)
+        Gxa, Gxb, Gxc, Gba, Gca = self.graph.scipy_blocks()
+        k, a0 = wl["k"], wl["alpha0"]
+        rng = np.random.default_rng(0)
+        nX, nA, nB, nC = self.graph.parts
+        sk = (rng.standard_normal((nB, 2 * k)), rng.standard_normal((nC, 2 * k)),
+              rng.standard_normal((nA, 2 * k)))
+        t0 = time.perf_counter()
+        self.wh = O.second_whiten(Gxa, Gxb, Gxc, k, a0, sk)
+        self.y = O.whitened_data(Gxa, Gxb, Gxc, self.wh)
+        self.t_whiten = time.perf_counter() - t0
+        self.phi = O.polar(rng.standard_normal((k, k)))
+        self.t = 0
+        self.batches = O.stpm_minibatches(nX, wl["minibatch"])
+        t0 = time.perf_counter()
+        lam = O.tensor_values(self.phi, self.y, a0)
+        O.postprocess(Gxa, Gba, Gca, self.wh, lam, self.phi)
+        self.t_post = time.perf_counter() - t0
+        self.sweeps = []
+
+    def sweep(self):
+        O, a0 = self.O, self.wl["alpha0"]
+        t0 = time.perf_counter()
+        for nodes in self.batches:
+            beta = 1.0 / (1.0 + self.t)
+            S = self.phi.T @ self.phi
+            step = 3.0 * (self.phi @ (S * S)) - 3.0 * O.online_grad_terms(self.phi, self.y,
+                                                                           nodes, a0)
+            self.phi = O.polar(self.phi - beta * step)
+            self.t += 1
+        dt = time.perf_counter() - t0
+        self.sweeps.append(dt)
+        return dt
+
+    def node_updates_per_s(self):
+        t_sweep = statistics.median(self.sweeps)
+        total = self.t_whiten + self.wl["sweeps"] * t_sweep + self.t_post
+        return self.graph.parts[0] * self.wl["sweeps"] / total, total
+
+    def sample(self):
+        _, total = self.node_updates_per_s()
+        return (f"FP64 numpy/scipy port of the reference path: whitening {self.t_whiten:.2f}s and "
+                f"unwhitening {self.t_post:.2f}s timed once, {len(self.sweeps)} STPM sweeps "
+                f"(median {statistics.median(self.sweeps):.3f}s, {len(self.batches)} minibatch "
+                f"steps each); extrapolated to {self.wl['sweeps']} sweeps = {total:.1f}s per step")
 
 
 def run_reference(args, wl, ws, rank):
     if rank != 0:
         return
     mm = load_pkg()
-    graph = make_graph(mm, wl)
-    vals = []
-    sample = ""
+    port = CpuPort(mm, wl)
     for i in range(args.warmup + args.steps):
-        nu, sample, total = cpu_port_sample(mm, wl, graph, max_seconds=args.cpu_seconds)
-        if i >= args.warmup:
-            vals.append(nu)
-        if args.warmup + args.steps > 2 and i == 0 and total > 0:
-            pass
-    v = statistics.median(vals)
+        port.sweep()
+        if i == args.warmup - 1:
+            port.sweeps.clear()
+    v, total = port.node_updates_per_s()
     line = {"impl": "reference", "metric": "stpm_node_updates_per_s", "value": v,
             "unit": "node-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": wl["n"] // 4 * wl["sweeps"] / v * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "ms_per_step": total * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": wl["name"], **{k: wl[k] for k in wl if k != "name"}},
             "cpu_baseline": {"value": v, "unit": "node-updates/s", "cores": os.cpu_count(),
-                             "kind": "port", "sample": sample},
+                             "kind": "port", "sample": port.sample()},
             "e2e": {"value": v, "unit": "node-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -308,9 +317,12 @@ def run_ours(args, wl, ws, rank, local):
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        nu, sample, _ = cpu_port_sample(mm, wl, graph, max_seconds=args.cpu_seconds)
+        port = CpuPort(mm, wl, graph)
+        for _ in range(3):
+            port.sweep()
+        nu, _ = port.node_updates_per_s()
         line["cpu_baseline"] = {"value": nu, "unit": "node-updates/s", "cores": os.cpu_count(),
-                                "kind": "port", "sample": sample}
+                                "kind": "port", "sample": port.sample()}
     if rank == 0:
         print(json.dumps(line), flush=True)
     p.close()
@@ -323,7 +335,6 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n", type=int, default=None, help="override node count (testing)")
     args = ap.parse_args()

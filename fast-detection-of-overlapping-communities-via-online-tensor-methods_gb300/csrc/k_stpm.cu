@@ -295,12 +295,13 @@ __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
 // written into every CTA's next buffer through distributed shared memory,
 // followed by one cluster barrier per iteration.
 
-__host__ __device__ constexpr int step_xld(int KP) { return KP + 4; }
+// leading dimension: multiple of 4 (float4) with an odd float4 stride
+__host__ __device__ constexpr int step_xld(int KP) { return ((KP / 4) % 2) ? KP + 8 : KP + 4; }
 
 template <int KP, int CL>
 struct StepSmem {
   static constexpr int NB = KP / CL;
-  static constexpr size_t floats = (size_t)2 * KP * step_xld(KP) + (size_t)2 * NB * KP + 4 * KP + 4 * CL + 3 * NB + 8;
+  static constexpr size_t floats = (size_t)2 * KP * step_xld(KP) + (size_t)2 * NB * KP + 4 * KP + 6 * CL + 3 * NB + 8;
 };
 
 // Ab[jb * KP + i] = X[:, i] . X[:, c0 + jb]
@@ -308,20 +309,28 @@ template <int KP, int CL>
 __device__ __forceinline__ void step_gram(const float* __restrict__ X, int c0, float* __restrict__ Ab) {
   constexpr int NB = KP / CL, XLD = step_xld(KP), IG = KP / 4;
   for (int t = threadIdx.x; t < IG * NB; t += blockDim.x) {
-    const int i0 = 4 * (t % IG), jb = t / IG;
+    // columns t, t+IG, t+2IG, t+3IG: neighbouring threads read neighbouring
+    // columns, whose float4 addresses differ by XLD/4 (odd) -> no bank conflicts
+    const int i0 = t % IG, jb = t / IG;
     const float* xj = X + (c0 + jb) * XLD;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    float4 acc[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 4
     for (int r = 0; r < KP; r += 4) {
       const float4 b = *reinterpret_cast<const float4*>(xj + r);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const float4 a = *reinterpret_cast<const float4*>(X + (i0 + q) * XLD + r);
-        acc[q] = fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, acc[q]))));
+        const float4 a = *reinterpret_cast<const float4*>(X + (i0 + q * IG) * XLD + r);
+        acc[q].x = fmaf(a.x, b.x, acc[q].x);
+        acc[q].y = fmaf(a.y, b.y, acc[q].y);
+        acc[q].z = fmaf(a.z, b.z, acc[q].z);
+        acc[q].w = fmaf(a.w, b.w, acc[q].w);
       }
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) Ab[jb * KP + i0 + q] = acc[q];
+    for (int q = 0; q < 4; ++q)
+      Ab[jb * KP + i0 + q * IG] = (acc[q].x + acc[q].y) + (acc[q].z + acc[q].w);
   }
 }
 
@@ -336,7 +345,9 @@ __device__ __forceinline__ void step_times(const float* __restrict__ X, const fl
   for (int t = threadIdx.x; t < RG * NB; t += blockDim.x) {
     const int r0 = 4 * (t % RG), jb = t / RG;
     const float* b = B + jb * KP;
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 acc2[2];
+    acc2[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    acc2[1] = acc2[0];
 #pragma unroll 2
     for (int i = 0; i < KP; i += 4) {
       const float4 bb = *reinterpret_cast<const float4*>(b + i);
@@ -344,12 +355,15 @@ __device__ __forceinline__ void step_times(const float* __restrict__ X, const fl
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const float4 x = *reinterpret_cast<const float4*>(X + (i + q) * XLD + r0);
-        acc.x = fmaf(x.x, bv[q], acc.x);
-        acc.y = fmaf(x.y, bv[q], acc.y);
-        acc.z = fmaf(x.z, bv[q], acc.z);
-        acc.w = fmaf(x.w, bv[q], acc.w);
+        float4& ac = acc2[q & 1];
+        ac.x = fmaf(x.x, bv[q], ac.x);
+        ac.y = fmaf(x.y, bv[q], ac.y);
+        ac.z = fmaf(x.z, bv[q], ac.z);
+        ac.w = fmaf(x.w, bv[q], ac.w);
       }
     }
+    const float4 acc = make_float4(acc2[0].x + acc2[1].x, acc2[0].y + acc2[1].y,
+                                   acc2[0].z + acc2[1].z, acc2[0].w + acc2[1].w);
     const int col = c0 + jb;
     const float4 self = *reinterpret_cast<const float4*>(X + col * XLD + r0);
     float v[4] = {beta_self * self.x + alpha * acc.x, beta_self * self.y + alpha * acc.y,
@@ -366,7 +380,7 @@ __device__ __forceinline__ void step_times(const float* __restrict__ X, const fl
 }
 
 template <int KP, int CL>
-__global__ void __launch_bounds__(256) stpm_step_kernel(StpmUpdateArgs a) {
+__global__ void __launch_bounds__(512) stpm_step_kernel(StpmUpdateArgs a) {
   constexpr int NB = KP / CL, XLD = step_xld(KP);
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
@@ -376,7 +390,7 @@ __global__ void __launch_bounds__(256) stpm_step_kernel(StpmUpdateArgs a) {
   float* Ab = Xb + KP * XLD;
   float* Gb = Ab + NB * KP;
   float* mv = Gb + NB * KP;     // m1, m2, m3 (+ pad) for this block
-  float* red = mv + 4 * KP;     // 2*CL stats slots
+  float* red = mv + 4 * KP;     // 3 x 2*CL statistics slots (initial, even, odd)
   __shared__ float s_abs, s_err;
   const int k = a.k;
   const int c0 = rank * NB;
@@ -417,7 +431,7 @@ __global__ void __launch_bounds__(256) stpm_step_kernel(StpmUpdateArgs a) {
     }
     __syncthreads();
     // per-column sums of the d partials (3 x NB), then the contraction block
-    float* dcol = red + 2 * CL;  // 3 * NB floats
+    float* dcol = red + 6 * CL;  // 3 * NB floats
     for (int e = tid / 32; e < 3 * NB; e += blockDim.x / 32) {
       const int which = e / NB, jb = e % NB, i = c0 + jb;
       float sd = 0.f;
@@ -470,10 +484,10 @@ __global__ void __launch_bounds__(256) stpm_step_kernel(StpmUpdateArgs a) {
   // Newton-Schulz polar iteration X <- X (3 I - X^T X) / 2.  With
   // X^T X = I + E the next error is -3/4 E^2 + E^3/4, so once |E| < 1e-3 one
   // more iteration reaches the FP32 floor; the loop stops there.
-  int it = 0;
-  bool done = false, last = false;
-  for (; it < a.max_ns; ++it) {
-    step_gram<KP, CL>(X, c0, Ab);
+  // One cluster barrier per iteration: the statistics of A_t = X_t^T X_t
+  // travel with the broadcast of X_{t+1}; if they show X_t had already
+  // converged, X_{t+1} is discarded.
+  auto block_stats = [&]() {
     if (tid == 0) {
       s_abs = 0.f;
       s_err = 0.f;
@@ -500,47 +514,85 @@ __global__ void __launch_bounds__(256) stpm_step_kernel(StpmUpdateArgs a) {
       }
     }
     __syncthreads();
-    if (tid < CL) {
-      float* r = cluster.map_shared_rank(red, tid);
-      r[rank] = s_abs;
-      r[CL + rank] = s_err;
-    }
-    cluster.sync();
-    float gabs = 0.f, gerr = 0.f;
+  };
+  auto cluster_stats = [&](float& gabs, float& gerr) {
+    gabs = 0.f;
+    gerr = 0.f;
     for (int q = 0; q < CL; ++q) {
       gabs = fmaxf(gabs, red[q]);
       gerr = fmaxf(gerr, red[CL + q]);
     }
+  };
+  // initial scaling: sigma_max^2 <= ||X^T X||_1
+  step_gram<KP, CL>(X, c0, Ab);
+  block_stats();
+  if (tid < CL) {
+    float* r = cluster.map_shared_rank(red, tid);
+    r[rank] = s_abs;
+    r[CL + rank] = s_err;
+  }
+  cluster.sync();
+  int it = 0;
+  bool done = false, last = false;
+  {
+    float gabs, gerr;
+    cluster_stats(gabs, gerr);
     if (!(gerr == gerr) || !(gabs == gabs)) {
       if (tid == 0 && rank == 0) atomicOr(a.flags, kFlagNonFinite);
       done = true;
-      break;
-    }
-    if (gerr < a.ns_tol) {
+    } else if (gerr < a.ns_tol) {
       done = true;
-      break;
-    }
-    if (gerr < 1e-3f) last = true;
-    if (it == 0 && gabs > 0.f) {
-      // sigma_max^2 <= ||X^T X||_1: scale into the convergence region
+    } else if (gabs > 0.f) {
       const float sc = rsqrtf(gabs);
       for (int e = tid; e < KP * NB; e += blockDim.x) Ab[e] *= sc * sc;
       for (int e = tid; e < KP * XLD; e += blockDim.x) X[e] *= sc;
       __syncthreads();
     }
+  }
+  cluster.sync();  // every CTA has read the statistics slots
+  for (; !done && it < a.max_ns; ++it) {
+    if (it > 0) {
+      step_gram<KP, CL>(X, c0, Ab);
+      block_stats();
+    } else {
+      // A_0 of the scaled X is already in Ab; its error decides below
+      block_stats();
+    }
+    // speculative next iterate from A_t, broadcast together with A_t's statistics
     for (int e = tid; e < KP * NB; e += blockDim.x) {
       const int i = e % KP, jb = e / KP;
       Ab[e] = ((i == c0 + jb) ? 1.5f : 0.f) - 0.5f * Ab[e];
     }
     __syncthreads();
     step_times<KP, CL>(X, Ab, c0, 1.f, 0.f, nullptr, 0.f, k, dn);
+    if (tid < CL) {
+      float* r = cluster.map_shared_rank(red, tid) + 2 * CL * (1 + (it & 1));
+      r[rank] = s_abs;
+      r[CL + rank] = s_err;
+    }
     cluster.sync();
+    float gabs = 0.f, gerr = 0.f;
+    for (int q = 0; q < CL; ++q) {
+      const float* rr = red + 2 * CL * (1 + (it & 1));
+      gabs = fmaxf(gabs, rr[q]);
+      gerr = fmaxf(gerr, rr[CL + q]);
+    }
+    if (!(gerr == gerr) || !(gabs == gabs)) {
+      if (tid == 0 && rank == 0) atomicOr(a.flags, kFlagNonFinite);
+      done = true;
+      break;
+    }
+    if (gerr < a.ns_tol) {  // X_t was converged: keep it, drop X_{t+1}
+      done = true;
+      break;
+    }
     swap_buffers();
     if (last) {
       done = true;
       ++it;
       break;
     }
+    if (gerr < 1e-3f) last = true;
   }
   if (!done && rank == 0 && tid == 0) atomicOr(a.flags, kFlagNoConvergence);
   if (rank == 0 && tid == 0 && a.ns_iters) atomicAdd(a.ns_iters, it);
@@ -651,7 +703,7 @@ cudaError_t launch_step_t(const StpmUpdateArgs& a, cudaStream_t s) {
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CL, 1, 1);
-  cfg.blockDim = dim3(256, 1, 1);
+  cfg.blockDim = dim3(512, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];

@@ -135,11 +135,13 @@ void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A
     ck(transpose_f64(n, R, Y, s), "eig R^T");
   }
   ck(eig_from_factor(n, Y, lam, X, work, c->flags, s), "jacobi");
+  double* dstate = c->tbuf<double>(tag + ".edelta", 1);
+  ck(cudaMemsetAsync(dstate, 0, sizeof(double), s), "delta");
   for (int step = 0; step < 3; ++step) {
     ck(dgemm_small(true, false, n, n, n, 1.0, X, n, X, n, 0.0, G, n, s), "X^T X");
     ck(dgemm_small(false, false, n, n, n, 1.0, A, n, X, n, 0.0, AX, n, s), "A X");
     ck(dgemm_small(true, false, n, n, n, 1.0, X, n, AX, n, 0.0, S, n, s), "X^T A X");
-    ck(oa_correction(n, A, G, S, E, lam, s), "oa");
+    ck(oa_correction(n, A, G, S, E, lam, dstate, s), "oa");
     ck(cudaMemcpyAsync(X2, X, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, s), "copy");
     ck(dgemm_small(false, false, n, n, n, 1.0, X, n, E, n, 1.0, X2, n, s), "X + X E");
     std::swap(X, X2);

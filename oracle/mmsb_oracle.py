@@ -45,6 +45,26 @@ def orthogonalize_cols(Y, tol=TOLERANCE):
     return Y
 
 
+def orthogonalize_cols_cgs2(Y, tol=TOLERANCE):
+    """The same column orthonormalisation with classical Gram-Schmidt applied
+    twice per column (vectorised); equal to orthogonalize_cols to round-off.
+    Used where the oracle is timed on large inputs."""
+    Y = np.array(Y, dtype=np.float64, copy=True)
+    n, c = Y.shape
+    Q = np.zeros_like(Y)
+    for j in range(c):
+        v = Y[:, j].copy()
+        for _ in range(2):
+            if j:
+                v -= Q[:, :j] @ (Q[:, :j].T @ v)
+        nrm = np.sqrt(v @ v)
+        Q[:, j] = v * ((1.0 / nrm) if nrm > tol else 0.0)
+    return Q
+
+
+FAST_GS = False  # True: orthogonalize_cols_cgs2 inside svd_sym_nystrom
+
+
 def svd_sym_nystrom(M, k, rows_factor=20, tol=TOLERANCE):
     """Spectral.cpp:169-223 (SVD_symNystrom_sparse) for an n x 2k input.
 
@@ -56,7 +76,7 @@ def svd_sym_nystrom(M, k, rows_factor=20, tol=TOLERANCE):
     if n > rows_factor * k:
         if cols > 2 * k:
             raise NotImplementedError("sketching branch (Spectral.cpp:176-178) is unused here")
-        Q = orthogonalize_cols(M, tol)
+        Q = (orthogonalize_cols_cgs2 if FAST_GS else orthogonalize_cols)(M, tol)
         QQ = Q[:cols, :] if cols < Q.shape[0] else Q
         C = M @ QQ
         Z = C.T @ C

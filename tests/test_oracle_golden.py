@@ -95,3 +95,16 @@ def test_online_stpm_recovers_orthonormal_components(golden_cfg1, oracle):
     assert steps == 100
     assert np.abs(phi.T @ phi - np.eye(g.k)).max() < 1e-10
     assert np.all(lam > 0)
+
+
+def test_fast_gram_schmidt_matches_reference_path(golden, oracle):
+    """The vectorised CGS2 variant (used when the oracle is timed) gives the
+    same whitening as the modified Gram-Schmidt restatement."""
+    Gxa, Gxb, Gxc, _, _ = golden.scipy_blocks()
+    a = oracle.second_whiten(Gxa, Gxb, Gxc, golden.k, golden.alpha0, golden.sketches())
+    oracle.FAST_GS = True
+    try:
+        b = oracle.second_whiten(Gxa, Gxb, Gxc, golden.k, golden.alpha0, golden.sketches())
+    finally:
+        oracle.FAST_GS = False
+    assert rel(align_columns(a["W"], b["W"]), a["W"]) < 1e-8
