@@ -113,8 +113,9 @@ struct Nys {
 }  // namespace
 
 // Symmetric positive semi-definite eigen-decomposition (n <= 512), eigenvalues
-// descending: FP32 one-sided Jacobi on the Cholesky factor, then two FP64
-// Ogita-Aishima refinement steps (quadratic convergence to FP64 accuracy).
+// descending: FP32 one-sided Jacobi on the Cholesky factor (run to
+// convergence), then four FP64 Ogita-Aishima refinement steps (quadratic
+// convergence to FP64 accuracy from a converged FP32 start).
 void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A, double* evals,
                      double* V, const double* factor) {
   cudaStream_t s = c->s;
@@ -137,7 +138,7 @@ void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A
   ck(eig_from_factor(n, Y, lam, X, work, c->flags, s), "jacobi");
   double* dstate = c->tbuf<double>(tag + ".edelta", 1);
   ck(cudaMemsetAsync(dstate, 0, sizeof(double), s), "delta");
-  for (int step = 0; step < 3; ++step) {
+  for (int step = 0; step < 4; ++step) {
     ck(dgemm_small(true, false, n, n, n, 1.0, X, n, X, n, 0.0, G, n, s), "X^T X");
     ck(dgemm_small(false, false, n, n, n, 1.0, A, n, X, n, 0.0, AX, n, s), "A X");
     ck(dgemm_small(true, false, n, n, n, 1.0, X, n, AX, n, 0.0, S, n, s), "X^T A X");
