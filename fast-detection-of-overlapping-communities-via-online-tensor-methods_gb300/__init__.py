@@ -124,6 +124,9 @@ _SIGS = {
     "mmsb_op_spmm": (ctypes.c_int, [ctypes.POINTER(Csr), ctypes.c_int, _F, ctypes.c_int64,
                                     ctypes.c_float, _F]),
     "mmsb_op_symeig": (ctypes.c_int, [_D, ctypes.c_int32, _D, _D]),
+    "mmsb_op_spmm_t_noalloc": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64,
+                                              ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_float,
+                                              _P, _P]),
     "mmsb_generate": (ctypes.c_int, [ctypes.POINTER(GenParams), ctypes.POINTER(_P)]),
     "mmsb_host_graph_free": (None, [_P]),
     "mmsb_host_graph_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64),
@@ -485,3 +488,11 @@ def symeig(A):
     V = np.zeros((n, n), order="F")
     _check(lib().mmsb_op_symeig(_dptr(A), n, _dptr(ev), _dptr(V)))
     return ev, V
+
+
+def spmm_t_noalloc(d_row_ptr, d_col_idx, d_val, n_rows, n_cols, nnz, d_P, p, alpha, d_Y,
+                   stream=0):
+    """Y = alpha G^T P on caller-owned DEVICE buffers (integer addresses); the
+    library allocates nothing (see include/mmsb.h).  Returns the status code."""
+    return lib().mmsb_op_spmm_t_noalloc(d_row_ptr, d_col_idx, d_val or None, n_rows, n_cols, nnz,
+                                        d_P, p, alpha, d_Y, stream or None)

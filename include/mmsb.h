@@ -231,9 +231,27 @@ mmsb_status mmsb_synchronize(mmsb_ctx* ctx);
  * with transpose != 0, Y (n_cols x p) = alpha * G^T * P (P: n_rows x p). */
 mmsb_status mmsb_op_spmm(const mmsb_csr* g, int transpose, const float* P, int64_t p,
                          float alpha, float* Y);
-/* Symmetric eigen-decomposition of an n x n matrix (column-major, n <= 512),
- * eigenvalues descending; vectors column-major n x n. */
+/* Symmetric eigen-decomposition of an n x n positive semi-definite matrix
+ * (column-major, n <= 512), eigenvalues descending; vectors column-major n x n. */
 mmsb_status mmsb_op_symeig(const double* A, int32_t n, double* evals, double* evecs);
+
+/* No counterpart in the reference.  Y = alpha * G^T * P for callers that
+ * cannot allocate device memory (code inside another framework's memory pool,
+ * or running while a stream is captured): same result as mmsb_op_spmm with
+ * transpose != 0, but every pointer is a DEVICE pointer the caller owns and
+ * the call allocates nothing.  G: n_rows x n_cols CSR (d_val NULL = binary);
+ * P: n_rows x p row-major, Y: n_cols x p row-major, p a multiple of 4, 16-byte
+ * aligned.  The transposed copy of G is built in a fixed 8 MiB device array
+ * compiled into the library (held on every GPU that loads it until exit):
+ * blocks needing more (about 16 * (n_cols + 1 + nnz) bytes) return
+ * MMSB_ERR_UNSUPPORTED before any work.  All calls share that array, so calls
+ * that overlap on the GPU race; serialise them.  The first call on a device
+ * looks the array up (this can load the module): make it before any stream
+ * capture.  stream: a cudaStream_t (NULL = default stream). */
+mmsb_status mmsb_op_spmm_t_noalloc(const int64_t* d_row_ptr, const int32_t* d_col_idx,
+                                   const float* d_val, int64_t n_rows, int64_t n_cols,
+                                   int64_t nnz, const float* d_P, int64_t p, float alpha,
+                                   float* d_Y, void* stream);
 
 /* ---- synthetic MMSB graphs ---------------------------------------------- */
 
