@@ -28,6 +28,8 @@ import numpy as np
 
 PKG_DIR = Path(__file__).resolve().parent
 LIB_PATH = PKG_DIR / "lib" / "libmmsb.so"
+# command line with the reference executable's argv and output files
+CLI_PATH = PKG_DIR / "lib" / "mmsb_cli"
 CSRC = PKG_DIR / "csrc"
 
 OK = 0

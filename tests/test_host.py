@@ -94,3 +94,21 @@ def test_triplet_writer_matches_reference_format(mm, golden_cfg1, tmp_path):
     out = tmp_path / "white.txt"
     mm.write_triplets(out, golden_cfg1["W"])
     assert out.read_text().splitlines() == list(golden_cfg1["white_txt"])
+
+
+def test_cli_argv_contract(mm, tmp_path):
+    """The command line keeps CommunityDetection.cpp:16-40's argv: too few
+    arguments or an unreadable input file exit with status 1 before any
+    device work."""
+    import subprocess
+    cli = str(mm.CLI_PATH)
+    r = subprocess.run([cli], capture_output=True, text=True)
+    assert r.returncode == 1 and "usage" in r.stderr
+    missing = [str(tmp_path / f"{n}.txt") for n in ("Gx_a", "Gx_b", "Gx_c", "Gb_a", "Gc_a")]
+    r = subprocess.run([cli, "10", "10", "10", "10", "2", "1.0", "0", *missing,
+                        str(tmp_path / "pi.txt"), str(tmp_path / "white.txt")],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "Gx_a" in r.stderr
+    r = subprocess.run([cli, *(["1"] * 7), *missing, "a", "b", "--bogus=1"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "unknown option" in r.stderr
