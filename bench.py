@@ -252,6 +252,7 @@ def run_ours(args, wl, ws, rank, local):
                           if (ROOT / "gpurun_out").is_dir() else None)
     clocks.start()
     dev_ms, spmm_ms, spmm_bytes, spmm_launch, launches = [], 0.0, 0.0, 0, 0
+    ns_iters, stpm_steps = 0, 0
     stage = {"whiten_ms": 0.0, "stpm_ms": 0.0, "post_ms": 0.0}
     t_host0 = time.perf_counter()
     for _ in range(args.steps):
@@ -266,6 +267,8 @@ def run_ours(args, wl, ws, rank, local):
         spmm_bytes += st["spmm_bytes"]
         spmm_launch += st["spmm_launches"]
         launches += st["kernel_launches"]
+        ns_iters += st["polar_iterations"]
+        stpm_steps += st["stpm_steps"]
     p.synchronize()
     t_host = time.perf_counter() - t_host0
     dist.barrier()
@@ -306,6 +309,7 @@ def run_ours(args, wl, ws, rank, local):
                    "parallelism": f"replicas{ws}"},
         "stages_ms_per_step": {k_: v / args.steps for k_, v in stage.items()},
         "host_wall_ms_per_step": t_host * 1e3 / args.steps,
+        "polar_iterations_per_stpm_step": ns_iters / max(stpm_steps, 1),
         "e2e": {"value": e2e_value, "unit": "node-updates/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_step},
         "gpu_launches": launches,

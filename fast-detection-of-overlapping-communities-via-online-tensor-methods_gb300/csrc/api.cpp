@@ -128,6 +128,9 @@ mmsb_status mmsb_create(const mmsb_config* cfg, mmsb_ctx** out) {
     c->cfg = *cfg;
     ck(cudaSetDevice(cfg->device), "cudaSetDevice");
     ck(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "stream");
+    ck(cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking), "stream");
+    ck(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming), "event");
+    ck(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming), "event");
     for (auto& e : c->ev) ck(cudaEventCreate(&e), "event");
     c->spmm_pool.resize(64);
     for (auto& pr : c->spmm_pool) {

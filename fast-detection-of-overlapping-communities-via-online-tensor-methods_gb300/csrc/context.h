@@ -22,6 +22,9 @@ struct DevCsr {
 struct mmsb_ctx {
   mmsb_config cfg{};
   cudaStream_t s = nullptr;
+  // second stream: the two independent pseudo-inverse sides of the whitening
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   std::string err;
   std::atomic<bool> stop{false};
   mmsb_stats stats{};

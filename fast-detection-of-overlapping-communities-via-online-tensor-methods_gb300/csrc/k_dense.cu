@@ -157,31 +157,32 @@ __global__ void __launch_bounds__(256) panel_small_kernel(
 
 // ---- small FP64 GEMM ------------------------------------------------------------
 
+template <int T>
 __global__ void __launch_bounds__(256) dgemm_small_kernel(bool ta, bool tb, int m, int n, int k,
                                                           double alpha, const double* __restrict__ A,
                                                           int lda, const double* __restrict__ B,
                                                           int ldb, double beta,
                                                           double* __restrict__ C, int ldc) {
-  __shared__ double As[32][33];
-  __shared__ double Bs[32][33];
+  constexpr int KC = 32, RG = 256 / T, RI = T / RG;  // thread: rows ty + RG*i, col tx
+  __shared__ double As[T][KC + 1];
+  __shared__ double Bs[KC][T + 1];
   const int tid = threadIdx.x;
-  const int tx = tid % 32, ty = tid / 32;  // each thread: rows ty + 8*i, col tx
-  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
-  double acc[4] = {0, 0, 0, 0};
-  for (int k0 = 0; k0 < k; k0 += 32) {
-    for (int e = tid; e < 1024; e += 256) {
-      const int a = e % 32, b = e / 32;
-      // As[ii][kk] = op(A)[i0+ii, k0+kk]
-      {
-        const int ii = a, kk = b;
+  const int tx = tid % T, ty = tid / T;
+  const int i0 = blockIdx.x * T, j0 = blockIdx.y * T;
+  double acc[RI];
+#pragma unroll
+  for (int i = 0; i < RI; ++i) acc[i] = 0.0;
+  for (int k0 = 0; k0 < k; k0 += KC) {
+    for (int e = tid; e < T * KC; e += 256) {
+      {  // As[ii][kk] = op(A)[i0+ii, k0+kk]; consecutive threads walk ii (column-major A)
+        const int ii = ta ? e / KC : e % T, kk = ta ? e % KC : e / T;
         const int gi = i0 + ii, gk = k0 + kk;
         double v = 0.0;
         if (gi < m && gk < k) v = ta ? A[(int64_t)gi * lda + gk] : A[(int64_t)gk * lda + gi];
         As[ii][kk] = v;
       }
-      // Bs[kk][jj] = op(B)[k0+kk, j0+jj]
-      {
-        const int kk = a, jj = b;
+      {  // Bs[kk][jj] = op(B)[k0+kk, j0+jj]; consecutive threads walk kk (column-major B)
+        const int kk = tb ? e / T : e % KC, jj = tb ? e % T : e / KC;
         const int gk = k0 + kk, gj = j0 + jj;
         double v = 0.0;
         if (gk < k && gj < n) v = tb ? B[(int64_t)gk * ldb + gj] : B[(int64_t)gj * ldb + gk];
@@ -190,16 +191,16 @@ __global__ void __launch_bounds__(256) dgemm_small_kernel(bool ta, bool tb, int 
     }
     __syncthreads();
 #pragma unroll 4
-    for (int kk = 0; kk < 32; ++kk) {
+    for (int kk = 0; kk < KC; ++kk) {
       const double b = Bs[kk][tx];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) acc[i] = fma(As[ty + 8 * i][kk], b, acc[i]);
+      for (int i = 0; i < RI; ++i) acc[i] = fma(As[ty + RG * i][kk], b, acc[i]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int gi = i0 + ty + 8 * i, gj = j0 + tx;
+  for (int i = 0; i < RI; ++i) {
+    const int gi = i0 + ty + RG * i, gj = j0 + tx;
     if (gi < m && gj < n) {
       double* c = C + (int64_t)gj * ldc + gi;
       *c = alpha * acc[i] + (beta == 0.0 ? 0.0 : beta * *c);
@@ -212,11 +213,10 @@ __global__ void __launch_bounds__(256) dgemm_small_kernel(bool ta, bool tb, int 
 __global__ void __launch_bounds__(1024) chol_upper_kernel(int p, const double* __restrict__ S,
                                                           int lds, double* __restrict__ R,
                                                           double drop2, unsigned* flags) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  for (int64_t e = tid; e < (int64_t)p * p; e += nt) {
-    const int i = (int)(e % p), l = (int)(e / p);
-    R[e] = i <= l ? S[(int64_t)l * lds + i] : 0.0;
-  }
+  extern __shared__ double rowj[];  // row j of R (p values)
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int l = warp; l < p; l += nw)
+    for (int i = lane; i < p; i += 32) R[(int64_t)l * p + i] = i <= l ? S[(int64_t)l * lds + i] : 0.0;
   __syncthreads();
   __shared__ double rjj;
   for (int j = 0; j < p; ++j) {
@@ -234,14 +234,17 @@ __global__ void __launch_bounds__(1024) chol_upper_kernel(int p, const double* _
     const double r = rjj;
     for (int l = j + 1 + tid; l < p; l += nt) {
       double* x = &R[(int64_t)l * p + j];
-      *x = r > 0.0 ? *x / r : 0.0;
+      const double v = r > 0.0 ? *x / r : 0.0;
+      *x = v;
+      rowj[l] = v;
     }
     __syncthreads();
-    const int m = p - j - 1;
-    const int64_t cnt = (int64_t)m * m;
-    for (int64_t e = tid; e < cnt; e += nt) {
-      const int ii = j + 1 + (int)(e % m), ll = j + 1 + (int)(e / m);
-      if (ii <= ll) R[(int64_t)ll * p + ii] -= R[(int64_t)ii * p + j] * R[(int64_t)ll * p + j];
+    // trailing update R[i, l] -= R[j, i] R[j, l] for j < i <= l: a warp per
+    // column l, its lanes along the contiguous rows i
+    for (int l = j + 1 + warp; l < p; l += nw) {
+      const double rl = rowj[l];
+      double* col = R + (int64_t)l * p;
+      for (int i = j + 1 + lane; i <= l; i += 32) col[i] = fma(-rowj[i], rl, col[i]);
     }
     __syncthreads();
   }
@@ -249,28 +252,41 @@ __global__ void __launch_bounds__(1024) chol_upper_kernel(int p, const double* _
 
 // ---- T = R^{-1} (upper), one warp per column ------------------------------------
 
+// Column j of T solves R t = e_j by back substitution in column (axpy) form:
+// for l = j..0: t_l = b_l / R_ll (0 where R_ll == 0), then b_i -= t_l R_il for
+// i < l.  Column l of R is contiguous, so each step is one coalesced axpy;
+// lane i % 32 keeps b_i (and then t_i) in register slot i / 32 (p <= 512).
 __global__ void __launch_bounds__(256) trinv_upper_kernel(int p, const double* __restrict__ R,
                                                           double* __restrict__ T) {
-  extern __shared__ double tcol[];  // [warps][p]
+  constexpr int kSlots = 16;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int j = blockIdx.x * (blockDim.x >> 5) + w;
   if (j >= p) return;
-  double* t = tcol + (int64_t)w * p;
-  for (int i = lane; i < p; i += 32) t[i] = 0.0;
-  __syncwarp();
-  const double rjj = R[(int64_t)j * p + j];
-  if (lane == 0) t[j] = rjj != 0.0 ? 1.0 / rjj : 0.0;
-  __syncwarp();
-  for (int i = j - 1; i >= 0; --i) {
-    double s = 0.0;
-    for (int l = i + 1 + lane; l <= j; l += 32) s += R[(int64_t)l * p + i] * t[l];
+  double b[kSlots];
 #pragma unroll
-    for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-    const double rii = R[(int64_t)i * p + i];
-    if (lane == 0) t[i] = rii != 0.0 ? -s / rii : 0.0;
-    __syncwarp();
+  for (int q = 0; q < kSlots; ++q) b[q] = (lane + 32 * q == j) ? 1.0 : 0.0;
+  for (int l = j; l >= 0; --l) {
+    const int ql = l >> 5, ll = l & 31;
+    double bl = 0.0;
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q)
+      if (q == ql) bl = b[q];
+    bl = __shfl_sync(0xffffffffu, bl, ll);
+    const double* rc = R + (int64_t)l * p;
+    const double rll = rc[l];
+    const double tl = rll != 0.0 ? bl / rll : 0.0;
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) {
+      const int i = lane + 32 * q;
+      if (q == ql && lane == ll) b[q] = tl;
+      if (i < l) b[q] = fma(-tl, rc[i], b[q]);
+    }
   }
-  for (int i = lane; i < p; i += 32) T[(int64_t)j * p + i] = t[i];
+#pragma unroll
+  for (int q = 0; q < kSlots; ++q) {
+    const int i = lane + 32 * q;
+    if (i < p) T[(int64_t)j * p + i] = i <= j ? b[q] : 0.0;
+  }
 }
 
 // ---- one-sided Jacobi: eigenpairs of Y Y^T -------------------------------------
@@ -367,30 +383,42 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __res
 // modified Gram-Schmidt to round-off and turns the inner loop into parallel
 // dot products (m, p <= 512).
 
-__global__ void __launch_bounds__(512) cgs2_cols_kernel(int m, int p, const double* __restrict__ P,
-                                                        int ldp, double* __restrict__ Q, int ldq,
-                                                        double tol) {
+__global__ void __launch_bounds__(1024) cgs2_cols_kernel(int m, int p, const double* __restrict__ P,
+                                                         int ldp, double* __restrict__ Q, int ldq,
+                                                         double tol) {
+  constexpr int kGroups = 8;  // thread groups splitting the projection sum
   extern __shared__ double sh[];
-  double* v = sh;        // m
-  double* d = sh + m;    // p
-  __shared__ double red[16];
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  double* v = sh;                // m
+  double* d = sh + m;            // p
+  double* part = sh + m + p;     // kGroups x m partial projections
+  __shared__ double red[32];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  const int gsz = nt / kGroups, grp = tid / gsz, gt = tid % gsz;
   for (int j = 0; j < p; ++j) {
     for (int r = tid; r < m; r += nt) v[r] = P[(int64_t)j * ldp + r];
     __syncthreads();
     for (int pass = 0; pass < 2; ++pass) {
-      // d_i = Q_i . v for i < j (one thread per previous column)
-      for (int i = tid; i < j; i += nt) {
+      // d_i = Q_i . v for i < j: a warp per previous column, lanes along rows
+      for (int i = warp; i < j; i += nw) {
         const double* qi = Q + (int64_t)i * ldq;
         double s = 0.0;
-        for (int r = 0; r < m; ++r) s = fma(qi[r], v[r], s);
-        d[i] = s;
+        for (int r = lane; r < m; r += 32) s = fma(qi[r], v[r], s);
+#pragma unroll
+        for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (lane == 0) d[i] = s;
       }
       __syncthreads();
-      // v -= sum_i d_i Q_i (one thread per row)
+      // v -= sum_i d_i Q_i: group g sums the columns i = g (mod kGroups)
+      for (int r = gt; r < m; r += gsz) {
+        double s = 0.0;
+        for (int i = grp; i < j; i += kGroups) s = fma(d[i], Q[(int64_t)i * ldq + r], s);
+        part[grp * m + r] = s;
+      }
+      __syncthreads();
       for (int r = tid; r < m; r += nt) {
         double s = 0.0;
-        for (int i = 0; i < j; ++i) s = fma(d[i], Q[(int64_t)i * ldq + r], s);
+#pragma unroll
+        for (int g = 0; g < kGroups; ++g) s += part[g * m + r];
         v[r] -= s;
       }
       __syncthreads();
@@ -402,7 +430,7 @@ __global__ void __launch_bounds__(512) cgs2_cols_kernel(int m, int p, const doub
     if (lane == 0) red[warp] = nrm;
     __syncthreads();
     double tot = 0.0;
-    for (int w = 0; w < (nt >> 5); ++w) tot += red[w];
+    for (int w = 0; w < nw; ++w) tot += red[w];
     const double nn = sqrt(tot);
     const double sc = nn > tol ? 1.0 / nn : 0.0;
     for (int r = tid; r < m; r += nt) Q[(int64_t)j * ldq + r] = v[r] * sc;
@@ -647,20 +675,29 @@ cudaError_t dgemm_small(bool ta, bool tb, int m, int n, int k, double alpha, con
                         int lda, const double* B, int ldb, double beta, double* C, int ldc,
                         cudaStream_t s) {
   if (m == 0 || n == 0) return cudaSuccess;
-  dim3 grid((unsigned)ceil_div(m, 32), (unsigned)ceil_div(n, 32));
-  dgemm_small_kernel<<<grid, 256, 0, s>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  // FP64 runs at 1/64 of the FP32 rate: spread the tiles over the SMs, with
+  // 16 x 16 tiles where 32 x 32 tiles would leave most SMs idle
+  if (ceil_div(m, 32) * ceil_div(n, 32) < (int64_t)(2 * kNumSMs) / 3) {
+    dim3 grid((unsigned)ceil_div(m, 16), (unsigned)ceil_div(n, 16));
+    dgemm_small_kernel<16><<<grid, 256, 0, s>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  } else {
+    dim3 grid((unsigned)ceil_div(m, 32), (unsigned)ceil_div(n, 32));
+    dgemm_small_kernel<32><<<grid, 256, 0, s>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  }
   ++g_launch_count;
   return cudaGetLastError();
 }
 
 cudaError_t chol_upper_drop(int p, const double* S, int lds, double* R, double drop2,
                             unsigned* flags, cudaStream_t s) {
-  chol_upper_kernel<<<1, 1024, 0, s>>>(p, S, lds, R, drop2, flags);
+  if (p > 4096) return cudaErrorInvalidValue;
+  chol_upper_kernel<<<1, 1024, sizeof(double) * p, s>>>(p, S, lds, R, drop2, flags);
   ++g_launch_count;
   return cudaGetLastError();
 }
 
 cudaError_t trinv_upper(int p, const double* R, double* T, cudaStream_t s) {
+  if (p > 512) return cudaErrorInvalidValue;
   const int warps = 8;
   trinv_upper_kernel<<<(unsigned)ceil_div(p, warps), warps * 32, (size_t)warps * p * sizeof(double),
                        s>>>(p, R, T);
@@ -741,7 +778,9 @@ cudaError_t axpy_f64(int64_t n, double a, const double* x, double* y, cudaStream
 cudaError_t mgs_cols(int m, int p, const double* P, int ldp, double* Q, int ldq, double tol,
                      cudaStream_t s) {
   if (m > 4096 || p > 4096) return cudaErrorInvalidValue;
-  cgs2_cols_kernel<<<1, 512, sizeof(double) * (m + p), s>>>(m, p, P, ldp, Q, ldq, tol);
+  const size_t sm = sizeof(double) * ((size_t)9 * m + p);
+  if (sm > 48 * 1024) return cudaErrorInvalidValue;
+  cgs2_cols_kernel<<<1, 1024, sm, s>>>(m, p, P, ldp, Q, ldq, tol);
   ++g_launch_count;
   return cudaGetLastError();
 }

@@ -58,17 +58,30 @@ __global__ void __launch_bounds__(256) stpm_partial_kernel(StpmPartialArgs a) {
     const int j = e / KP, i = e % KP;
     Phis[e] = (i < k && j < k) ? a.phi[(int64_t)i * k + j] : 0.f;
   }
-  for (int e = tid; e < 3 * KP; e += 256) dsum[e] = 0.f;
+  // stage mu_1..3 in dsum (zeroed again below)
+  for (int e = tid; e < 3 * KP; e += 256) {
+    const int which = e / KP, j = e % KP;
+    const float* mu = which == 0 ? a.mu1 : which == 1 ? a.mu2 : a.mu3;
+    dsum[e] = (mu && j < k) ? mu[j] : 0.f;
+  }
   __syncthreads();
   // m_P = Phi^T mu_P
   for (int e = tid; e < 3 * KP; e += 256) {
     const int which = e / KP, i = e % KP;
-    const float* mu = which == 0 ? a.mu1 : which == 1 ? a.mu2 : a.mu3;
-    float s = 0.f;
-    if (i < k && mu)
-      for (int j = 0; j < k; ++j) s = fmaf(Phis[j * KP + i], mu[j], s);
-    mv[e] = s;
+    const float* mu = dsum + which * KP;
+    float s0 = 0.f, s1 = 0.f;
+    if (i < k) {
+      int j = 0;
+      for (; j + 1 < k; j += 2) {
+        s0 = fmaf(Phis[j * KP + i], mu[j], s0);
+        s1 = fmaf(Phis[(j + 1) * KP + i], mu[j + 1], s1);
+      }
+      if (j < k) s0 = fmaf(Phis[j * KP + i], mu[j], s0);
+    }
+    mv[e] = s0 + s1;
   }
+  __syncthreads();
+  for (int e = tid; e < 3 * KP; e += 256) dsum[e] = 0.f;
   __syncthreads();
 
   const int pj = tid / 16, pi = tid % 16;  // contraction patch (rows j, cols i)
@@ -290,148 +303,272 @@ __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
 // ---- k x k step on one thread-block cluster -------------------------------------
 //
 // Every CTA of the cluster holds the whole current matrix X (column-major,
-// leading dimension KP + 4) and owns NB = KP / CL of its columns.  Products
-// X^T X[:, blk] and X B[:, blk] are formed locally; the new column block is
-// written into every CTA's next buffer through distributed shared memory,
-// followed by one cluster barrier per iteration.
+// leading dimension KP + 4) and owns NB = 8 or 16 of its columns.  The
+// products X^T X[:, blk] and X B[:, blk] run on the tensor cores as warp-level
+// m16n8k8 TF32 MMAs with the 3xTF32 split (a = a_hi + a_lo; hi*hi + hi*lo +
+// lo*hi accumulated in FP32, relative error ~1e-6 per product), one warp per
+// 16 x 8 output tile.  The new column block is staged in shared memory and
+// sent to every CTA's next buffer by bulk asynchronous copies
+// (cp.async.bulk shared::cta -> shared::cluster), which complete on the
+// receiver's mbarrier; a CTA proceeds once all CL blocks of the next
+// iterate have arrived, so the data exchange itself is the per-iteration
+// synchronisation.  A block sent at broadcast n is rewritten only at
+// broadcast n + 2, after every receiver has finished waiting for broadcast
+// n (two staging buffers alternate).
 
-// leading dimension: multiple of 4 (float4) with an odd float4 stride
-__host__ __device__ constexpr int step_xld(int KP) { return ((KP / 4) % 2) ? KP + 8 : KP + 4; }
+// scaled Newton-Schulz: first guess of the smallest singular value after
+// the initial scaling, the error below which the plain step is used, and a
+// cap on the scale that keeps f(a sigma) > 0 for sigma slightly above 1
+constexpr float kNsLowerGuess = 2e-2f;
+constexpr float kNsPlainBelow = 0.1f;
+constexpr float kNsMaxScale = 1.7f;
+__device__ __forceinline__ float ns_poly(float y) { return y * (1.5f - 0.5f * y * y); }
 
+// column stride of X, B and the output tile: KP + 4 (== 4 mod 8 for KP a
+// multiple of 16) makes the fragment loads of the Gram product conflict-free
+__host__ __device__ constexpr int step_xld(int KP) { return KP + 4; }
+
+// NB = 8 (one n-tile) when the cluster has KP / 8 CTAs, else 16
 template <int KP, int CL>
 struct StepSmem {
-  static constexpr int NB = KP / CL;
-  static constexpr size_t floats = (size_t)2 * KP * step_xld(KP) + (size_t)2 * NB * KP + 4 * KP + 6 * CL + 3 * NB + 8;
+  static constexpr int NB = KP / CL, XLD = step_xld(KP), MT = KP / 16, NT = NB / 8;
+  static constexpr int TILES = MT * NT, KS = TILES <= 8 ? 2 : 1;  // K split over warps
+  static constexpr size_t floats = (size_t)2 * KP * XLD    // X, next X
+                                   + (size_t)4 * NB * XLD  // B (Ab), G block, 2 output tiles
+                                   + (size_t)TILES * 128   // K-split partial tiles
+                                   + 4 * KP + 3 * CL + 3 * NB + 2 * NB + 8;
 };
 
-// Ab[jb * KP + i] = X[:, i] . X[:, c0 + jb]
-template <int KP, int CL>
-__device__ __forceinline__ void step_gram(const float* __restrict__ X, int c0, float* __restrict__ Ab) {
-  constexpr int NB = KP / CL, XLD = step_xld(KP), IG = KP / 4;
-  for (int t = threadIdx.x; t < IG * NB; t += blockDim.x) {
-    // columns t, t+IG, t+2IG, t+3IG: neighbouring threads read neighbouring
-    // columns, whose float4 addresses differ by XLD/4 (odd) -> no bank conflicts
-    const int i0 = t % IG, jb = t / IG;
-    const float* xj = X + (c0 + jb) * XLD;
-    float4 acc[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll 4
-    for (int r = 0; r < KP; r += 4) {
-      const float4 b = *reinterpret_cast<const float4*>(xj + r);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float4 a = *reinterpret_cast<const float4*>(X + (i0 + q * IG) * XLD + r);
-        acc[q].x = fmaf(a.x, b.x, acc[q].x);
-        acc[q].y = fmaf(a.y, b.y, acc[q].y);
-        acc[q].z = fmaf(a.z, b.z, acc[q].z);
-        acc[q].w = fmaf(a.w, b.w, acc[q].w);
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      Ab[jb * KP + i0 + q * IG] = (acc[q].x + acc[q].y) + (acc[q].z + acc[q].w);
+__device__ __forceinline__ uint32_t tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4],
+                                         const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// waits for the phase with the given parity to complete; false after about
+// one second (then the caller reports kFlagTimeout instead of hanging)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  const long long start = clock64();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - start > 2000000000LL) return false;
   }
 }
 
-// value(r, c0+jb) = beta_self X[r, c0+jb] + alpha (X B)[r, jb] + gamma Gb[jb*KP + r],
-// zero outside k x k, written to every cluster rank's buffer
-template <int KP, int CL>
-__device__ __forceinline__ void step_times(const float* __restrict__ X, const float* __restrict__ B,
-                                           int c0, float alpha, float beta_self,
-                                           const float* __restrict__ Gb, float gamma, int k,
-                                           float* const* dst) {
-  constexpr int NB = KP / CL, XLD = step_xld(KP), RG = KP / 4;
-  for (int t = threadIdx.x; t < RG * NB; t += blockDim.x) {
-    const int r0 = 4 * (t % RG), jb = t / RG;
-    const float* b = B + jb * KP;
-    float4 acc2[2];
-    acc2[0] = make_float4(0.f, 0.f, 0.f, 0.f);
-    acc2[1] = acc2[0];
+// bulk copy of `bytes` (multiple of 16, 16-byte aligned) from this CTA's
+// shared memory to the same offset as dst_local in cluster rank `rank`,
+// completing on that rank's copy of the mbarrier at bar_local
+__device__ __forceinline__ void bulk_copy_to_rank(const void* dst_local, const void* src,
+                                                  uint32_t bytes, uint64_t* bar_local,
+                                                  uint32_t rank) {
+  uint32_t dst, bar;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(dst) : "r"(smem_addr(dst_local)), "r"(rank));
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(bar) : "r"(smem_addr(bar_local)), "r"(rank));
+  asm volatile(
+      "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "r"(smem_addr(src)), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+// One warp: acc = sum over k in [kb, ke) of A(m, k) B(k, n) for the 16 x 8
+// tile at pa = &A(0, 0) of the tile, pb = &B(0, 0) of the tile, with
+// A(m, k) = pa[m AM + k AK] and B(k, n) = pb[k BK + n BN].  Fragments of
+// m16n8k8 (g = lane / 4, t = lane % 4): a = A(g|g+8, t|t+4), b = B(t|t+4, g),
+// acc = C(g|g+8, 2t|2t+1).
+template <int AM, int AK, int BK, int BN>
+__device__ __forceinline__ void warp_tile_3xtf32(const float* __restrict__ pa,
+                                                 const float* __restrict__ pb, int kb, int ke,
+                                                 float (&acc)[4]) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f}, c2[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 2
-    for (int i = 0; i < KP; i += 4) {
-      const float4 bb = *reinterpret_cast<const float4*>(b + i);
-      const float bv[4] = {bb.x, bb.y, bb.z, bb.w};
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float4 x = *reinterpret_cast<const float4*>(X + (i + q) * XLD + r0);
-        float4& ac = acc2[q & 1];
-        ac.x = fmaf(x.x, bv[q], ac.x);
-        ac.y = fmaf(x.y, bv[q], ac.y);
-        ac.z = fmaf(x.z, bv[q], ac.z);
-        ac.w = fmaf(x.w, bv[q], ac.w);
-      }
-    }
-    const float4 acc = make_float4(acc2[0].x + acc2[1].x, acc2[0].y + acc2[1].y,
-                                   acc2[0].z + acc2[1].z, acc2[0].w + acc2[1].w);
-    const int col = c0 + jb;
-    const float4 self = *reinterpret_cast<const float4*>(X + col * XLD + r0);
-    float v[4] = {beta_self * self.x + alpha * acc.x, beta_self * self.y + alpha * acc.y,
-                  beta_self * self.z + alpha * acc.z, beta_self * self.w + alpha * acc.w};
+  for (int k0 = kb; k0 < ke; k0 += 8) {
+    const float av[4] = {pa[g * AM + (k0 + t) * AK], pa[(g + 8) * AM + (k0 + t) * AK],
+                         pa[g * AM + (k0 + t + 4) * AK], pa[(g + 8) * AM + (k0 + t + 4) * AK]};
+    const float bv[2] = {pb[(k0 + t) * BK + g * BN], pb[(k0 + t + 4) * BK + g * BN]};
+    uint32_t ah[4], al[4], bh[2], bl[2];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      if (Gb) v[q] += gamma * Gb[jb * KP + r0 + q];
-      if (r0 + q >= k || col >= k) v[q] = 0.f;
+      ah[q] = tf32_round(av[q]);
+      al[q] = tf32_round(av[q] - __uint_as_float(ah[q]));
     }
-    const float4 out = make_float4(v[0], v[1], v[2], v[3]);
 #pragma unroll
-    for (int q = 0; q < CL; ++q) *reinterpret_cast<float4*>(dst[q] + col * XLD + r0) = out;
+    for (int q = 0; q < 2; ++q) {
+      bh[q] = tf32_round(bv[q]);
+      bl[q] = tf32_round(bv[q] - __uint_as_float(bh[q]));
+    }
+    mma_tf32(c0, ah, bh);
+    mma_tf32(c1, ah, bl);
+    mma_tf32(c2, al, bh);
   }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) acc[q] = c0[q] + (c1[q] + c2[q]);
+}
+
+// Tile products of the step.  Warp w < TILES * KS owns tile w % TILES and
+// half w / TILES of the K range (KS = 2); the halves meet in `part`.
+// kProdGram:  A_blk = X^T X[:, c0 .. c0+NB)   (A(m=i, k=r) = X[i XLD + r])
+// kProdTimes: P_blk = X B_blk                 (A(m=r, k=i) = X[i XLD + r])
+enum StepProd : int { kProdGram = 0, kProdTimes = 1 };
+
+template <int KP, int CL, int PROD>
+__device__ __forceinline__ bool step_product(const float* __restrict__ X, const float* __restrict__ Bm,
+                                             int c0, float* __restrict__ part, float (&acc)[4],
+                                             int& m0, int& n0) {
+  using S = StepSmem<KP, CL>;
+  constexpr int XLD = S::XLD;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = warp % S::TILES, ks = warp / S::TILES;
+  const bool active = warp < S::TILES * S::KS;
+  m0 = (tile % S::MT) * 16;
+  n0 = (tile / S::MT) * 8;
+  const int kb = ks * (KP / S::KS), ke = kb + KP / S::KS;
+  if (active) {
+    if (PROD == kProdGram)
+      warp_tile_3xtf32<XLD, 1, 1, XLD>(X + m0 * XLD, X + (c0 + n0) * XLD, kb, ke, acc);
+    else
+      warp_tile_3xtf32<1, XLD, 1, XLD>(X + m0, Bm + n0 * XLD, kb, ke, acc);
+    if (S::KS == 2 && ks == 1) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) part[tile * 128 + q * 32 + lane] = acc[q];
+    }
+  }
+  __syncthreads();
+  if (!active || ks != 0) return false;
+  if (S::KS == 2) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[q] += part[tile * 128 + q * 32 + lane];
+  }
+  return true;
 }
 
 template <int KP, int CL>
-__global__ void __launch_bounds__(512) stpm_step_kernel(StpmUpdateArgs a) {
-  constexpr int NB = KP / CL, XLD = step_xld(KP);
+__global__ void __launch_bounds__(512, 1) stpm_step_kernel(StpmUpdateArgs a) {
+  using S = StepSmem<KP, CL>;
+  constexpr int NB = S::NB, XLD = S::XLD;
+  static_assert(NB == 8 || NB == 16, "column block of 8 or 16");
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   extern __shared__ __align__(16) float sm[];
   float* Xa = sm;
   float* Xb = Xa + KP * XLD;
-  float* Ab = Xb + KP * XLD;
-  float* Gb = Ab + NB * KP;
-  float* mv = Gb + NB * KP;     // m1, m2, m3 (+ pad) for this block
-  float* red = mv + 4 * KP;     // 3 x 2*CL statistics slots (initial, even, odd)
-  __shared__ float s_abs, s_err;
+  float* Ab = Xb + KP * XLD;      // B (or A) block, column jb at Ab + jb * XLD
+  float* Gb = Ab + NB * XLD;      // G block (online step)
+  float* Ot = Gb + NB * XLD;      // 2 staging tiles of the cluster broadcast
+  float* part = Ot + 2 * NB * XLD;    // K-split partial tiles
+  float* mv = part + S::TILES * 128;  // m1, m2, m3 (+ pad) for this block
+  float* red = mv + 4 * KP;       // initial statistics of the CL ranks (3 x CL)
+  float* dcol = red + 3 * CL;     // 3 * NB d-sums (online step)
+  float* colabs = dcol + 3 * NB;  // NB column abs sums (+ NB spare)
+  __shared__ float s_abs, s_err, s_fro;
+  __shared__ __align__(8) uint64_t s_full[2];  // "next iterate arrived" for Xa / Xb
   const int k = a.k;
   const int c0 = rank * NB;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
   for (int e = tid; e < KP * XLD; e += blockDim.x) {
     const int r = e % XLD, c = e / XLD;
     Xa[e] = (r < k && c < k) ? a.phi[(int64_t)c * k + r] : 0.f;
     Xb[e] = 0.f;
   }
-  float* dstA[CL];
-  float* dstB[CL];
-#pragma unroll
-  for (int q = 0; q < CL; ++q) {
-    dstA[q] = cluster.map_shared_rank(Xa, q);
-    dstB[q] = cluster.map_shared_rank(Xb, q);
+  for (int e = tid; e < 2 * NB * XLD; e += blockDim.x) Ot[e] = 0.f;
+  if (tid == 0) {
+    mbar_init(&s_full[0], 1);
+    mbar_init(&s_full[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  cluster.sync();  // every CTA has read Phi before anyone writes it back
+  cluster.sync();  // Phi read and barriers initialised everywhere before any copy
+  uint32_t parity[2] = {0u, 0u};
+  int nbcast = 0;
+  bool timed_out = false;
 
-  float* X = Xa;
-  float* const* dn = dstB;
-  float* const* dc = dstA;
+  float* X = Xa;   // current iterate
+  float* dn = Xb;  // next iterate (the same offset in every CTA of the cluster)
   auto swap_buffers = [&]() {
-    X = (X == Xa) ? Xb : Xa;
-    float* const* td = dc;
-    dc = dn;
-    dn = td;
+    float* tt = X;
+    X = dn;
+    dn = tt;
+  };
+  // P = alpha X B_blk + beta_self X[:, blk] + gamma Gb, zero outside k x k,
+  // staged (with this CTA's statistics s_abs, s_err, s_fro in the padding
+  // rows KP.. of its first column) and sent to every rank's next buffer;
+  // returns once the whole next iterate has arrived (false on a timeout)
+  auto times_and_broadcast = [&](float alpha, float beta_self, const float* Gsrc, float gamma) {
+    float* Otc = Ot + (nbcast & 1) * NB * XLD;
+    ++nbcast;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    int m0, n0;
+    if (step_product<KP, CL, kProdTimes>(X, Ab, c0, part, acc, m0, n0)) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
+        float v = alpha * acc[q] + beta_self * X[col * XLD + r];
+        if (Gsrc) v += gamma * Gsrc[jb * XLD + r];
+        Otc[jb * XLD + r] = (r < k && col < k) ? v : 0.f;
+      }
+    }
+    if (tid == 0) {
+      Otc[KP] = s_abs;
+      Otc[KP + 1] = s_err;
+      Otc[KP + 2] = s_fro;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // staging -> async proxy
+    __syncthreads();
+    const int bi = dn == Xa ? 0 : 1;
+    if (tid < CL)
+      bulk_copy_to_rank(dn + c0 * XLD, Otc, (uint32_t)(sizeof(float) * NB * XLD), &s_full[bi],
+                        (uint32_t)tid);
+    if (tid == 0) mbar_arrive_expect_tx(&s_full[bi], (uint32_t)(sizeof(float) * KP * XLD));
+    const bool ok = mbar_wait_bounded(&s_full[bi], parity[bi]);
+    parity[bi] ^= 1u;
+    return !__syncthreads_or(!ok);
   };
   if (a.step_mode == kStepOnline) {
-    // G block (columns c0 .. c0+NB) from the per-CTA partials, plus the mean terms
-    for (int e = tid; e < 3 * NB; e += blockDim.x) {
+    // G block (columns c0 .. c0+NB) from the per-CTA partials, plus the mean
+    // terms phi_i . mu (a warp per dot product, lanes along the k entries)
+    for (int e = tid / 32; e < 3 * NB; e += blockDim.x / 32) {
       const int which = e / NB, jb = e % NB, i = c0 + jb;
       const float* mu = which == 0 ? a.mu1 : which == 1 ? a.mu2 : a.mu3;
       float sv = 0.f;
       if (i < k && mu)
-        for (int j = 0; j < k; ++j) sv = fmaf(X[i * XLD + j], mu[j], sv);
-      mv[which * KP + jb] = sv;
+        for (int j = lane; j < k; j += 32) sv = fmaf(X[i * XLD + j], mu[j], sv);
+#pragma unroll
+      for (int off = 16; off; off >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, off);
+      if (lane == 0) mv[which * KP + jb] = sv;
     }
     __syncthreads();
     // per-column sums of the d partials (3 x NB), then the contraction block
-    float* dcol = red + 6 * CL;  // 3 * NB floats
     for (int e = tid / 32; e < 3 * NB; e += blockDim.x / 32) {
       const int which = e / NB, jb = e % NB, i = c0 + jb;
       float sd = 0.f;
@@ -445,7 +582,7 @@ __global__ void __launch_bounds__(512) stpm_step_kernel(StpmUpdateArgs a) {
     __syncthreads();
     for (int e = tid; e < NB * KP; e += blockDim.x) {
       const int jb = e / KP, j = e % KP, i = c0 + jb;
-      float g = 0.f;
+      float gval = 0.f;
       if (i < k && j < k) {
         const float* gp = a.gpart + (int64_t)i * k + j;
         float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
@@ -468,75 +605,130 @@ __global__ void __launch_bounds__(512) stpm_step_kernel(StpmUpdateArgs a) {
                 a.mu2[j] * (c2 * dcol[NB + jb] * ic + c1 * m1 * m3) +
                 a.mu3[j] * (c2 * dcol[2 * NB + jb] * ic + c1 * m1 * m2);
         }
-        g = gv;
+        gval = gv;
       }
-      Gb[e] = g;
+      Gb[jb * XLD + j] = gval;
     }
     // Phi' = Phi - beta (3 theta Phi (Phi^T Phi)^.2 - gscale G)   (Util.cpp:259-272)
-    step_gram<KP, CL>(X, c0, Ab);
-    __syncthreads();
-    for (int e = tid; e < KP * NB; e += blockDim.x) Ab[e] = Ab[e] * Ab[e];
-    __syncthreads();
-    step_times<KP, CL>(X, Ab, c0, -a.beta * a.theta3, 1.f, Gb, a.beta * a.gscale, k, dn);
-    cluster.sync();
+    {
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      int m0, n0;
+      if (step_product<KP, CL, kProdGram>(X, nullptr, c0, part, acc, m0, n0)) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1);
+          Ab[jb * XLD + i] = acc[q] * acc[q];
+        }
+      }
+      __syncthreads();
+    }
+    if (!times_and_broadcast(-a.beta * a.theta3, 1.f, Gb, a.beta * a.gscale)) timed_out = true;
     swap_buffers();
   }
-  // Newton-Schulz polar iteration X <- X (3 I - X^T X) / 2.  With
-  // X^T X = I + E the next error is -3/4 E^2 + E^3/4, so once |E| < 1e-3 one
-  // more iteration reaches the FP32 floor; the loop stops there.
-  // One cluster barrier per iteration: the statistics of A_t = X_t^T X_t
-  // travel with the broadcast of X_{t+1}; if they show X_t had already
-  // converged, X_{t+1} is discarded.
-  auto block_stats = [&]() {
+  // Scaled Newton-Schulz polar iteration X <- X (3 a I - a^3 X^T X) / 2.
+  // After the first scaling every singular value of X lies in [l, 1]; with
+  // f(y) = 3y/2 - y^3/2 the step maps sigma to f(a sigma), and
+  // a = sqrt(3 / (1 + l + l^2)) makes f(a l) = f(a), so the lower end grows by
+  // up to sqrt(3) * 3/2 ~ 2.6x per iteration instead of 3/2 (the scaled
+  // Newton-Schulz iteration; l starts from the guess kNsLowerGuess and is
+  // tightened by sigma_min^2 >= 1 - ||X^T X - I||_F).  Once max|X^T X - I|
+  // < kNsPlainBelow the plain step (a = 1) takes over: with X^T X = I + E the
+  // next error is -3/4 E^2 + E^3/4, so after |E| < 1e-3 one more iteration
+  // reaches the FP32 floor and the loop stops there.
+  // One exchange per iteration: the statistics of A_t = X_t^T X_t travel
+  // with the broadcast of X_{t+1}; if they show X_t had already converged,
+  // X_{t+1} is discarded.  The scale of step t therefore uses
+  // the statistics of A_{t-1}; every CTA derives the same a from the same
+  // exchanged numbers.
+  //
+  // gram_stats: A_blk = X^T X[:, blk] with its statistics (max column abs
+  // sum, max |A - I|, ||A - I||_F^2 over the block) in s_abs, s_err, s_fro,
+  // and Ab = d0 I + d1 A_blk.
+  auto gram_stats = [&](float d0, float d1) {
+    if (tid < NB) colabs[tid] = 0.f;
     if (tid == 0) {
-      s_abs = 0.f;
       s_err = 0.f;
+      s_fro = 0.f;
     }
-    __syncthreads();
-    for (int jb = tid / 32; jb < NB; jb += blockDim.x / 32) {
-      const int col = c0 + jb;
-      float cs = 0.f, er = 0.f;
-      for (int i = tid % 32; i < KP; i += 32) {
-        const float v = Ab[jb * KP + i];
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    int m0, n0;
+    // (step_product's barrier also orders the resets above before the atomics)
+    const bool own = step_product<KP, CL, kProdGram>(X, nullptr, c0, part, acc, m0, n0);
+    if (own) {
+      float er = 0.f, fr = 0.f, ca[2] = {0.f, 0.f};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
+        const float v = acc[q];
+        const bool diag = i == col;
         if (i < k && col < k) {
-          cs += fabsf(v);
-          er = fmaxf(er, fabsf(v - (i == col ? 1.f : 0.f)));
+          const float d = v - (diag ? 1.f : 0.f);
+          er = fmaxf(er, fabsf(d));
+          fr = fmaf(d, d, fr);
+          ca[q & 1] += fabsf(v);
         }
+        Ab[jb * XLD + i] = (diag ? d0 : 0.f) + d1 * v;
+      }
+#pragma unroll
+      for (int off = 4; off < 32; off <<= 1) {  // over g: lanes with the same t4
+        ca[0] += __shfl_xor_sync(0xffffffffu, ca[0], off);
+        ca[1] += __shfl_xor_sync(0xffffffffu, ca[1], off);
       }
 #pragma unroll
       for (int off = 16; off; off >>= 1) {
-        cs += __shfl_xor_sync(0xffffffffu, cs, off);
         er = fmaxf(er, __shfl_xor_sync(0xffffffffu, er, off));
+        fr += __shfl_xor_sync(0xffffffffu, fr, off);
       }
-      if ((tid & 31) == 0) {
-        atomicMax(reinterpret_cast<int*>(&s_abs), __float_as_int(cs));
+      if (g == 0) {
+        atomicAdd(&colabs[n0 + 2 * t4], ca[0]);
+        atomicAdd(&colabs[n0 + 2 * t4 + 1], ca[1]);
+      }
+      if (lane == 0) {
         atomicMax(reinterpret_cast<int*>(&s_err), __float_as_int(er));
+        atomicAdd(&s_fro, fr);
       }
     }
     __syncthreads();
+    if (tid == 0) {
+      float m = 0.f;
+      for (int jb = 0; jb < NB; ++jb) m = fmaxf(m, colabs[jb]);
+      s_abs = m;
+    }
+    __syncthreads();
   };
-  auto cluster_stats = [&](float& gabs, float& gerr) {
+  // initial statistics: rank q's [abs sum | max error | Frobenius^2] go to
+  // red[q], red[CL + q], red[2 CL + q] of every rank
+  auto post_stats = [&]() {
+    if (tid < CL) {
+      float* r = cluster.map_shared_rank(red, tid);
+      r[rank] = s_abs;
+      r[CL + rank] = s_err;
+      r[2 * CL + rank] = s_fro;
+    }
+  };
+  auto reduce_stats = [&](const float* src, int stride, float& gabs, float& gerr, float& gfro) {
     gabs = 0.f;
     gerr = 0.f;
+    gfro = 0.f;
     for (int q = 0; q < CL; ++q) {
-      gabs = fmaxf(gabs, red[q]);
-      gerr = fmaxf(gerr, red[CL + q]);
+      gabs = fmaxf(gabs, src[q * stride]);
+      gerr = fmaxf(gerr, src[q * stride + 1]);
+      gfro += src[q * stride + 2];
     }
   };
   // initial scaling: sigma_max^2 <= ||X^T X||_1
-  step_gram<KP, CL>(X, c0, Ab);
-  block_stats();
-  if (tid < CL) {
-    float* r = cluster.map_shared_rank(red, tid);
-    r[rank] = s_abs;
-    r[CL + rank] = s_err;
-  }
+  gram_stats(0.f, 1.f);
+  post_stats();
   cluster.sync();
   int it = 0;
-  bool done = false, last = false;
-  {
-    float gabs, gerr;
-    cluster_stats(gabs, gerr);
+  bool done = timed_out, last = false;
+  if (!done) {
+    float gabs = 0.f, gerr = 0.f, gfro = 0.f;
+    for (int q = 0; q < CL; ++q) {
+      gabs = fmaxf(gabs, red[q]);
+      gerr = fmaxf(gerr, red[CL + q]);
+      gfro += red[2 * CL + q];
+    }
     if (!(gerr == gerr) || !(gabs == gabs)) {
       if (tid == 0 && rank == 0) atomicOr(a.flags, kFlagNonFinite);
       done = true;
@@ -544,40 +736,24 @@ __global__ void __launch_bounds__(512) stpm_step_kernel(StpmUpdateArgs a) {
       done = true;
     } else if (gabs > 0.f) {
       const float sc = rsqrtf(gabs);
-      for (int e = tid; e < KP * NB; e += blockDim.x) Ab[e] *= sc * sc;
       for (int e = tid; e < KP * XLD; e += blockDim.x) X[e] *= sc;
       __syncthreads();
     }
   }
   cluster.sync();  // every CTA has read the statistics slots
+  float lo = kNsLowerGuess;  // lower bound (guess at first) on sigma(X_t)
+  float prev_err = 1e30f;    // max|A_{t-1} - I|
   for (; !done && it < a.max_ns; ++it) {
-    if (it > 0) {
-      step_gram<KP, CL>(X, c0, Ab);
-      block_stats();
-    } else {
-      // A_0 of the scaled X is already in Ab; its error decides below
-      block_stats();
+    const float al = prev_err < kNsPlainBelow ? 1.f : fminf(sqrtf(3.f / (1.f + lo + lo * lo)), kNsMaxScale);
+    // A_t, its statistics and the speculative B_t in one pass
+    gram_stats(1.5f * al, -0.5f * al * al * al);
+    if (!times_and_broadcast(1.f, 0.f, nullptr, 0.f)) {
+      timed_out = true;
+      break;
     }
-    // speculative next iterate from A_t, broadcast together with A_t's statistics
-    for (int e = tid; e < KP * NB; e += blockDim.x) {
-      const int i = e % KP, jb = e / KP;
-      Ab[e] = ((i == c0 + jb) ? 1.5f : 0.f) - 0.5f * Ab[e];
-    }
-    __syncthreads();
-    step_times<KP, CL>(X, Ab, c0, 1.f, 0.f, nullptr, 0.f, k, dn);
-    if (tid < CL) {
-      float* r = cluster.map_shared_rank(red, tid) + 2 * CL * (1 + (it & 1));
-      r[rank] = s_abs;
-      r[CL + rank] = s_err;
-    }
-    cluster.sync();
-    float gabs = 0.f, gerr = 0.f;
-    for (int q = 0; q < CL; ++q) {
-      const float* rr = red + 2 * CL * (1 + (it & 1));
-      gabs = fmaxf(gabs, rr[q]);
-      gerr = fmaxf(gerr, rr[CL + q]);
-    }
-    if (!(gerr == gerr) || !(gabs == gabs)) {
+    float gabs, gerr, gfro;
+    reduce_stats(dn + KP, NB * XLD, gabs, gerr, gfro);  // A_t's statistics, from every rank
+    if (!(gerr == gerr) || !(gabs == gabs) || !(gfro == gfro)) {
       if (tid == 0 && rank == 0) atomicOr(a.flags, kFlagNonFinite);
       done = true;
       break;
@@ -586,6 +762,10 @@ __global__ void __launch_bounds__(512) stpm_step_kernel(StpmUpdateArgs a) {
       done = true;
       break;
     }
+    // bound for X_{t+1}: [lb, 1] -> [min(f(a lb), f(a)), 1]
+    const float lb = fmaxf(lo, sqrtf(fmaxf(0.f, 1.f - sqrtf(gfro))));
+    lo = al > 1.f ? fminf(ns_poly(al * lb), ns_poly(al)) : ns_poly(lb);
+    prev_err = gerr;
     swap_buffers();
     if (last) {
       done = true;
@@ -594,13 +774,18 @@ __global__ void __launch_bounds__(512) stpm_step_kernel(StpmUpdateArgs a) {
     }
     if (gerr < 1e-3f) last = true;
   }
-  if (!done && rank == 0 && tid == 0) atomicOr(a.flags, kFlagNoConvergence);
+  if (timed_out) {
+    if (tid == 0) atomicOr(a.flags, kFlagTimeout);
+  } else if (!done && rank == 0 && tid == 0) {
+    atomicOr(a.flags, kFlagNoConvergence);
+  }
   if (rank == 0 && tid == 0 && a.ns_iters) atomicAdd(a.ns_iters, it);
   for (int e = tid; e < KP * NB; e += blockDim.x) {
     const int r = e % KP, col = c0 + e / KP;
     if (r < k && col < k) a.phi[(int64_t)col * k + r] = X[col * XLD + r];
   }
   cluster.sync();  // keep shared memory alive until remote writers are done
+  if (timed_out) __nanosleep(100000);  // let copies a stalled exchange left in flight land
 }
 
 // batch power: Phi_new = G (already includes the shift terms), lambda = ||col||^3,
@@ -720,18 +905,20 @@ cudaError_t launch_step_t(const StpmUpdateArgs& a, cudaStream_t s) {
 
 template <int KP>
 cudaError_t launch_step_k(const StpmUpdateArgs& a, cudaStream_t s) {
-  static int use16 = -1;  // 16-CTA clusters where the device allows them
-  if (use16 != 0) {
-    cudaError_t e = launch_step_t<KP, 16>(a, s);
+  // KP / 8 CTAs (8 columns each; up to 16, a non-portable cluster size) where
+  // the device can co-schedule them, else KP / 16 CTAs of 16 columns
+  static int wide = -1;
+  if (wide != 0) {
+    cudaError_t e = launch_step_t<KP, KP / 8>(a, s);
     if (e == cudaSuccess) {
-      use16 = 1;
+      wide = 1;
       return e;
     }
-    if (use16 == 1) return e;
+    if (wide == 1) return e;
     cudaGetLastError();
-    use16 = 0;
+    wide = 0;
   }
-  return launch_step_t<KP, 8>(a, s);
+  return launch_step_t<KP, KP / 16>(a, s);
 }
 
 }  // namespace

@@ -13,6 +13,7 @@ using namespace mmsb;
 
 mmsb_ctx::~mmsb_ctx() {
   if (s) cudaStreamSynchronize(s);
+  if (s2) cudaStreamSynchronize(s2);
   for (auto& kv : ws) cudaFree(kv.second.first);
   for (auto& e : ev)
     if (e) cudaEventDestroy(e);
@@ -20,6 +21,9 @@ mmsb_ctx::~mmsb_ctx() {
     if (pr.first) cudaEventDestroy(pr.first);
     if (pr.second) cudaEventDestroy(pr.second);
   }
+  if (fork_ev) cudaEventDestroy(fork_ev);
+  if (join_ev) cudaEventDestroy(join_ev);
+  if (s2) cudaStreamDestroy(s2);
   if (s) cudaStreamDestroy(s);
 }
 
@@ -90,15 +94,17 @@ void check_flags(mmsb_ctx* c, const char* stage) {
 
 // SpMM with timing bookkeeping (algorithmic bytes: CSR + one panel-row
 // gather per nonzero + output)
-void spmm(mmsb_ctx* c, const DevCsr& g, const float* P, int ld, float alpha, float* Y) {
+void spmm(mmsb_ctx* c, const DevCsr& g, const float* P, int ld, float alpha, float* Y,
+          cudaStream_t st = nullptr) {
+  if (!st) st = c->s;
   const size_t slot = c->spmm_events.size();
   if (slot < c->spmm_pool.size()) {
-    ck(cudaEventRecord(c->spmm_pool[slot].first, c->s), "event");
-    ck(spmm_f32(g.rp, g.ci, g.val, g.n_rows, P, ld, alpha, Y, c->s), "spmm");
-    ck(cudaEventRecord(c->spmm_pool[slot].second, c->s), "event");
+    ck(cudaEventRecord(c->spmm_pool[slot].first, st), "event");
+    ck(spmm_f32(g.rp, g.ci, g.val, g.n_rows, P, ld, alpha, Y, st), "spmm");
+    ck(cudaEventRecord(c->spmm_pool[slot].second, st), "event");
     c->spmm_events.push_back(slot);
   } else {
-    ck(spmm_f32(g.rp, g.ci, g.val, g.n_rows, P, ld, alpha, Y, c->s), "spmm");
+    ck(spmm_f32(g.rp, g.ci, g.val, g.n_rows, P, ld, alpha, Y, st), "spmm");
   }
   c->stats.spmm_launches += 1;
   c->stats.spmm_bytes += 8.0 * (g.n_rows + 1) + 4.0 * g.nnz * (g.val ? 2 : 1) +
@@ -117,8 +123,8 @@ struct Nys {
 // convergence), then four FP64 Ogita-Aishima refinement steps (quadratic
 // convergence to FP64 accuracy from a converged FP32 start).
 void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A, double* evals,
-                     double* V, const double* factor) {
-  cudaStream_t s = c->s;
+                     double* V, const double* factor, cudaStream_t stream) {
+  cudaStream_t s = stream ? stream : c->s;
   double* R = c->tbuf<double>(tag + ".eR", (size_t)n * n);
   double* Y = c->tbuf<double>(tag + ".eY", (size_t)n * n);
   double* X = c->tbuf<double>(tag + ".eX", (size_t)n * n);
@@ -128,7 +134,7 @@ void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A
   double* S = c->tbuf<double>(tag + ".eS", (size_t)n * n);
   double* E = c->tbuf<double>(tag + ".eE", (size_t)n * n);
   double* lam = c->tbuf<double>(tag + ".elam", (size_t)n);
-  float* work = c->tbuf<float>("jacobi_work", (size_t)n * n);
+  float* work = c->tbuf<float>(tag + ".jw", (size_t)n * n);
   if (factor) {
     Y = const_cast<double*>(factor);  // A = Y Y^T given
   } else {
@@ -162,12 +168,11 @@ namespace {
 // The eigen-pairs (sigma^2, W) of H H^T give U = C V diag(1/sigma) = Q_A W
 // = A R_A^{-1} W and sigma.
 Nys svd_sym_nystrom(mmsb_ctx* c, const std::string& tag, const float* A, int lda, int m,
-                    const double* B, int64_t n) {
+                    const double* B, int64_t n, cudaStream_t s) {
   const int p = c->p, k = c->k, ldk = c->ldk;
-  cudaStream_t s = c->s;
   const double tol = c->cfg.pinv_tol;
   const int64_t cap = (int64_t)gram_tsk_partials(std::max<int64_t>(n, 1), m, m);
-  double* part = c->tbuf<double>("gram_part", (size_t)cap);
+  double* part = c->tbuf<double>(tag + ".gram_part", (size_t)cap);
   double* S1 = c->tbuf<double>(tag + ".S1", (size_t)m * m);
   double* S2 = c->tbuf<double>(tag + ".S2", (size_t)m * m);
   double* R1 = c->tbuf<double>(tag + ".R1", (size_t)m * m);
@@ -182,7 +187,7 @@ Nys svd_sym_nystrom(mmsb_ctx* c, const std::string& tag, const float* A, int lda
   double* F = c->tbuf<double>(tag + ".F", (size_t)m * k);
   double* sig = c->tbuf<double>(tag + ".sig", (size_t)k);
   float* U = c->tbuf<float>(tag + ".U", (size_t)n * ldk);
-  float* Q1 = c->tbuf<float>("nys.Q1", (size_t)n * round_up(m, 4));
+  float* Q1 = c->tbuf<float>(tag + ".Q1", (size_t)n * round_up(m, 4));
   const int ldq = (int)round_up(m, 4);
   // CholQR2: A = Q_A R_A
   ck(gram_tsk(A, lda, m, A, lda, m, n, 1.0, S1, part, cap, s), "gram1");
@@ -220,7 +225,7 @@ Nys svd_sym_nystrom(mmsb_ctx* c, const std::string& tag, const float* A, int lda
   }
   ck(dgemm_small(false, true, m, m, p, 1.0, Hm, m, Hm, m, 0.0, Zs, m, s), "H H^T");
   // Zs = H H^T: with a square H the one-sided Jacobi runs on H directly
-  sym_eig_refined(c, tag, m, Zs, ev, Wv, m == p ? Hm : nullptr);
+  sym_eig_refined(c, tag, m, Zs, ev, Wv, m == p ? Hm : nullptr, s);
   // sigma = sqrt(ev_k); U = Q_A W_k diag(sigma > tol) = Q1 (R2^{-1} W_k) (masked)
   ck(sig_from_evals(k, ev, sig, s), "sig");
   ck(dgemm_small(false, false, m, k, m, 1.0, T2, m, Wv, m, 0.0, F, m, s), "F");
@@ -354,7 +359,7 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches) {
   alloc_results(c);
   const double inv = c->cfg.normalize ? 1.0 / (double)c->nX : 1.0;
   const double tol = c->cfg.pinv_tol;
-  const DevCsr &XA = c->g[0], &XB = c->g[1], &XC = c->g[2];
+  const DevCsr &XB = c->g[1], &XC = c->g[2];
   const DevCsr &XAt = c->gt[0], &XBt = c->gt[1], &XCt = c->gt[2];
   const int64_t nmax = std::max(std::max(c->nX, c->nA), std::max(c->nB, c->nC));
   float* R[3];
@@ -374,12 +379,6 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches) {
   ck(row_sums_f64(XBt.rp, XBt.val, c->nB, inv, c->mu + c->nA, s), "mu_b");
   ck(row_sums_f64(XCt.rp, XCt.val, c->nC, inv, c->mu + c->nA + c->nB, s), "mu_c");
 
-  float* T1 = c->tbuf<float>("T1", (size_t)c->nX * ldp);
-  float* XR = c->tbuf<float>("XR", (size_t)nmax * ldp);
-  float* Gram = c->tbuf<float>("Gram", (size_t)nmax * ldp);
-  float* T3 = c->tbuf<float>("T3", (size_t)c->nX * ldk);
-  float* VL = c->tbuf<float>("VL", (size_t)nmax * ldk);
-  double* Linv_sqrt = c->tbuf<double>("Linv_sqrt", (size_t)k);
   double* Linv_c = c->tbuf<double>("Linv_c", (size_t)k);
   double* Linv_b = c->tbuf<double>("Linv_b", (size_t)k);
   c->Ub = c->tbuf<float>("Ub", (size_t)c->nB * ldk);
@@ -390,6 +389,8 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches) {
   // pinv_Nystrom_sparse_component (Spectral.cpp:296-315) of
   //   Zc_den = inv Gx_c^T Gx_b (n_C x n_B), sketch R_c (n_B x 2k)
   //   Zb_den = inv Gx_b^T Gx_c (n_B x n_C), sketch R_b (n_C x 2k)
+  // The two sides are independent: each runs on its own stream with its own
+  // workspace (their small latency-bound factorisations overlap).
   struct Side {
     const DevCsr *Gin, *Gout_t, *Gout, *Gin_t;
     int64_t n_in, n_out;
@@ -398,25 +399,41 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches) {
     float* U;
     double* Linv;
     const char* tag;
+    cudaStream_t st;
   } sides[2] = {
-      {&XB, &XCt, &XC, &XBt, c->nB, c->nC, R[0], Vc, c->Uc, Linv_c, "zc"},
-      {&XC, &XBt, &XB, &XCt, c->nC, c->nB, R[1], Vb, c->Ub, Linv_b, "zb"},
+      {&XB, &XCt, &XC, &XBt, c->nB, c->nC, R[0], Vc, c->Uc, Linv_c, "zc", s},
+      {&XC, &XBt, &XB, &XCt, c->nC, c->nB, R[1], Vb, c->Ub, Linv_b, "zb", c->s2},
   };
+  ck(cudaEventRecord(c->fork_ev, s), "fork");
+  ck(cudaStreamWaitEvent(c->s2, c->fork_ev, 0), "fork wait");
   for (auto& sd : sides) {
+    const std::string t = sd.tag;
+    cudaStream_t st = sd.st;
+    float* T1 = c->tbuf<float>(t + ".T1", (size_t)c->nX * ldp);
+    float* XR = c->tbuf<float>(t + ".XR", (size_t)sd.n_out * ldp);
+    float* Gram = c->tbuf<float>(t + ".Gram", (size_t)sd.n_in * ldp);
+    float* T3 = c->tbuf<float>(t + ".T3", (size_t)c->nX * ldk);
+    float* VL = c->tbuf<float>(t + ".VL", (size_t)sd.n_in * ldk);
+    double* Linv_sqrt = c->tbuf<double>(t + ".Linv_sqrt", (size_t)k);
     // X = inv Gout^T Gin  (n_out x n_in):  XR = X R ; Gram = X^T XR
-    spmm(c, *sd.Gin, sd.Rk, ldp, 1.f, T1);                  // Gin R       (n_X x p)
-    spmm(c, *sd.Gout_t, T1, ldp, (float)inv, XR);           // X R         (n_out x p)
-    spmm(c, *sd.Gout, XR, ldp, 1.f, T1);                    // Gout XR     (n_X x p)
-    spmm(c, *sd.Gin_t, T1, ldp, (float)inv, Gram);          // X^T X R     (n_in x p)
-    Nys ny = svd_sym_nystrom(c, sd.tag, Gram, ldp, p, nullptr, sd.n_in);  // V, sigma
-    ck(cudaMemcpyAsync(sd.V, ny.U, sizeof(float) * sd.n_in * ldk, cudaMemcpyDeviceToDevice, s), "V");
+    spmm(c, *sd.Gin, sd.Rk, ldp, 1.f, T1, st);                  // Gin R       (n_X x p)
+    spmm(c, *sd.Gout_t, T1, ldp, (float)inv, XR, st);           // X R         (n_out x p)
+    spmm(c, *sd.Gout, XR, ldp, 1.f, T1, st);                    // Gout XR     (n_X x p)
+    spmm(c, *sd.Gin_t, T1, ldp, (float)inv, Gram, st);          // X^T X R     (n_in x p)
+    Nys ny = svd_sym_nystrom(c, sd.tag, Gram, ldp, p, nullptr, sd.n_in, st);  // V, sigma
+    ck(cudaMemcpyAsync(sd.V, ny.U, sizeof(float) * sd.n_in * ldk, cudaMemcpyDeviceToDevice, st), "V");
     // U = X V diag(sqrt(pinv(sigma)));  Linv = pinv(sqrt(sigma))  (Spectral.cpp:235-244, 307)
-    ck(sqrt_pinv(k, ny.sig, tol, Linv_sqrt, sd.Linv, s), "Linv");
-    ck(cudaMemcpyAsync(VL, sd.V, sizeof(float) * sd.n_in * ldk, cudaMemcpyDeviceToDevice, s), "VL");
-    ck(panel_scale_cols(VL, ldk, sd.n_in, k, Linv_sqrt, s), "VL scale");
-    spmm(c, *sd.Gin, VL, ldk, 1.f, T3);
-    spmm(c, *sd.Gout_t, T3, ldk, (float)inv, sd.U);
+    ck(sqrt_pinv(k, ny.sig, tol, Linv_sqrt, sd.Linv, st), "Linv");
+    ck(cudaMemcpyAsync(VL, sd.V, sizeof(float) * sd.n_in * ldk, cudaMemcpyDeviceToDevice, st), "VL");
+    ck(panel_scale_cols(VL, ldk, sd.n_in, k, Linv_sqrt, st), "VL scale");
+    spmm(c, *sd.Gin, VL, ldk, 1.f, T3, st);
+    spmm(c, *sd.Gout_t, T3, ldk, (float)inv, sd.U, st);
   }
+  ck(cudaEventRecord(c->join_ev, c->s2), "join");
+  ck(cudaStreamWaitEvent(s, c->join_ev, 0), "join wait");
+  float* T3 = c->tbuf<float>("zc.T3", (size_t)c->nX * ldk);
+  float* VL = c->tbuf<float>("VL", (size_t)nmax * ldk);
+  double* Linv_sqrt = c->tbuf<double>("Linv_sqrt", (size_t)k);
   // Z_C_part1 = Zc_num V_c diag(Linv_c), Zc_num = inv Gx_a^T Gx_b (Util.cpp:83-84)
   ck(cudaMemcpyAsync(VL, Vc, sizeof(float) * c->nB * ldk, cudaMemcpyDeviceToDevice, s), "VL");
   ck(panel_scale_cols(VL, ldk, c->nB, k, Linv_c, s), "Vc scale");
@@ -453,7 +470,7 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches) {
   ck(panel_copy(c->Zc1, ldk, c->nA, k, Am, ldm2, s), "A_M");
   ck(panel_set_col(Am, ldm2, c->nA, k, c->mu, s), "A_M mu");
   // W = U_w diag(pinv(sqrt(sigma_w)))  (Util.cpp:116-123)
-  Nys nw = svd_sym_nystrom(c, "w", Am, ldm2, m2, Bm, c->nA);
+  Nys nw = svd_sym_nystrom(c, "w", Am, ldm2, m2, Bm, c->nA, s);
   ck(sqrt_pinv(k, nw.sig, tol, nullptr, Linv_sqrt, s), "Lw");
   ck(cudaMemcpyAsync(c->W, nw.U, sizeof(float) * c->nA * ldk, cudaMemcpyDeviceToDevice, s), "W");
   ck(panel_scale_cols(c->W, ldk, c->nA, k, Linv_sqrt, s), "W scale");

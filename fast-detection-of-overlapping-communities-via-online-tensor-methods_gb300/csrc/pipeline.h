@@ -15,7 +15,7 @@ void ck(cudaError_t e, const char* what);
 // eigen-pairs (descending) of a symmetric PSD n x n device matrix (n <= 512)
 // factor: optional Y with A = Y Y^T (skips the Cholesky)
 void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A, double* evals,
-                     double* V, const double* factor = nullptr);
+                     double* V, const double* factor = nullptr, cudaStream_t stream = nullptr);
 
 void pipeline_upload(mmsb_ctx* c, const mmsb_csr* blocks);
 void pipeline_whiten(mmsb_ctx* c, const double* const* sketches);
