@@ -112,6 +112,9 @@ cudaError_t panel_rank1(float* P, int ld, int64_t n, int q, double alpha, const 
                         const double* v, cudaStream_t s);
 cudaError_t f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
 cudaError_t f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t s);
+// row-major rows x cols FP32 panel (stride ld) -> BF16 panel (stride ldh >= cols, zero padded)
+cudaError_t panel_to_bf16(const float* src, int64_t ld, int64_t rows, int cols, void* dst,
+                          int64_t ldh, cudaStream_t s);
 cudaError_t phi_scaled(int k, const float* phi, const double* lambda, double tol, double* F,
                        cudaStream_t s);
 cudaError_t transpose_f64(int p, const double* A, double* At, cudaStream_t s);

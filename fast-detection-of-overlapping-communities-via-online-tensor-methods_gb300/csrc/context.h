@@ -45,6 +45,8 @@ struct mmsb_ctx {
   float* Uc = nullptr;   // n_C x ldk   (Z_C_part2 = Uc^T)
   double* mu = nullptr;  // mu_a | mu_b | mu_c (n_A + n_B + n_C)
   float* y[3] = {nullptr, nullptr, nullptr};  // n_X x ldk each
+  void* yh[3] = {nullptr, nullptr, nullptr};  // BF16 copies, n_X x ldkh (BF16 form)
+  int ldkh = 0;                               // round_up(k, 8)
   float* ymu = nullptr;                       // 3 x k (FP32)
   double* ymu64 = nullptr;                    // 3 x k
   float* phi = nullptr;                       // k x k column-major

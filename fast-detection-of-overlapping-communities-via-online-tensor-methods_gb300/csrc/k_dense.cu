@@ -308,41 +308,48 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __res
   const int m = p + (p & 1);  // players in the round-robin tournament
   __syncthreads();
   int sweep = 0;
+  // a group of 8 lanes per column pair: up to nt / 8 pairs of a round at once
+  const int grp = tid >> 3, l8 = tid & 7, ngrp = nt >> 3;
   for (; sweep < max_sweeps; ++sweep) {
     if (tid == 0) rot_count = 0;
     __syncthreads();
     for (int r = 0; r < m - 1; ++r) {
-      for (int s = warp; s < m / 2; s += nw) {
+      for (int s0 = 0; s0 < m / 2; s0 += ngrp) {
+        const int s = s0 + grp;
         // circle method: player 0 fixed, the rest rotate by r
         const int a = s == 0 ? 0 : 1 + ((s - 1 + r) % (m - 1));
         const int b = 1 + ((m - 2 - s + r) % (m - 1));
         const int i = min(a, b), j = max(a, b);
-        if (j >= p) continue;
-        float* xi = X + (int64_t)i * p;
-        float* xj = X + (int64_t)j * p;
+        const bool live = s < m / 2 && j < p;
+        float* xi = X + (int64_t)(live ? i : 0) * p;
+        float* xj = X + (int64_t)(live ? j : 0) * p;
         float al = 0.f, be = 0.f, ga = 0.f;
-        for (int t = lane; t < p; t += 32) {
-          const float u = xi[t], v = xj[t];
-          al = fmaf(u, u, al);
-          be = fmaf(v, v, be);
-          ga = fmaf(u, v, ga);
+        if (live) {
+#pragma unroll 4
+          for (int t = l8; t < p; t += 8) {
+            const float u = xi[t], v = xj[t];
+            al = fmaf(u, u, al);
+            be = fmaf(v, v, be);
+            ga = fmaf(u, v, ga);
+          }
         }
 #pragma unroll
-        for (int off = 16; off; off >>= 1) {
+        for (int off = 4; off; off >>= 1) {
           al += __shfl_xor_sync(0xffffffffu, al, off);
           be += __shfl_xor_sync(0xffffffffu, be, off);
           ga += __shfl_xor_sync(0xffffffffu, ga, off);
         }
-        if (fabsf(ga) > tol * sqrtf(al * be) && ga != 0.f) {
+        if (live && fabsf(ga) > tol * sqrtf(al * be) && ga != 0.f) {
           const float zeta = (be - al) / (2.f * ga);
           const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
           const float c = rsqrtf(1.f + t * t), sn = c * t;
-          for (int u = lane; u < p; u += 32) {
+#pragma unroll 4
+          for (int u = l8; u < p; u += 8) {
             const float x = xi[u], y = xj[u];
             xi[u] = c * x - sn * y;
             xj[u] = sn * x + c * y;
           }
-          if (lane == 0) atomicAdd(&rot_count, 1);
+          if (l8 == 0) atomicAdd(&rot_count, 1);
         }
       }
       __syncthreads();
@@ -394,9 +401,33 @@ __global__ void __launch_bounds__(1024) cgs2_cols_kernel(int m, int p, const dou
   __shared__ double red[32];
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   const int gsz = nt / kGroups, grp = tid / gsz, gt = tid % gsz;
+  __shared__ int kept;
+  __shared__ bool skip;
+  if (tid == 0) kept = 0;
   for (int j = 0; j < p; ++j) {
     for (int r = tid; r < m; r += nt) v[r] = P[(int64_t)j * ldp + r];
     __syncthreads();
+    if (kept == m) {
+      // the kept columns span R^m: the residual of v is round-off, about
+      // 1e-15 |v|, below tol whenever |v| < 1e10 tol, and the column is
+      // dropped without the projections
+      double nv = 0.0;
+      for (int r = tid; r < m; r += nt) nv = fma(v[r], v[r], nv);
+#pragma unroll
+      for (int off = 16; off; off >>= 1) nv += __shfl_xor_sync(0xffffffffu, nv, off);
+      if (lane == 0) red[warp] = nv;
+      __syncthreads();
+      if (tid == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < nw; ++w) tot += red[w];
+        skip = sqrt(tot) < 1e10 * tol;
+      }
+      __syncthreads();
+      if (skip) {
+        for (int r = tid; r < m; r += nt) Q[(int64_t)j * ldq + r] = 0.0;
+        continue;  // (no shared state written below before the next barrier)
+      }
+    }
     for (int pass = 0; pass < 2; ++pass) {
       // d_i = Q_i . v for i < j: a warp per previous column, lanes along rows
       for (int i = warp; i < j; i += nw) {
@@ -434,6 +465,7 @@ __global__ void __launch_bounds__(1024) cgs2_cols_kernel(int m, int p, const dou
     const double nn = sqrt(tot);
     const double sc = nn > tol ? 1.0 / nn : 0.0;
     for (int r = tid; r < m; r += nt) Q[(int64_t)j * ldq + r] = v[r] * sc;
+    if (tid == 0 && nn > tol) ++kept;
     __syncthreads();
   }
 }

@@ -2,6 +2,8 @@
 // post-processing chains (pinv thresholds, scaling, guards, conversions).
 #include "common.cuh"
 
+#include <cuda_bf16.h>
+
 #include <algorithm>
 
 namespace mmsb {
@@ -70,6 +72,18 @@ __global__ void f32_to_f64_kernel(const float* __restrict__ a, double* __restric
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (int64_t)gridDim.x * blockDim.x)
     b[e] = (double)a[e];
+}
+
+// dst[r, c] = bf16(src[r, c]) for c < cols, 0 for cols <= c < ldh
+__global__ void panel_to_bf16_kernel(const float* __restrict__ src, int64_t ld, int64_t rows,
+                                     int cols, __nv_bfloat16* __restrict__ dst, int64_t ldh) {
+  const int64_t n = rows * ldh;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / ldh;
+    const int c = (int)(e % ldh);
+    dst[e] = __float2bfloat16_rn(c < cols ? src[r * ld + c] : 0.f);
+  }
 }
 
 // F[:, i] = phi[:, i] * pinv(lambda_i)   (CommunityDetection.cpp:98-99)
@@ -180,6 +194,14 @@ cudaError_t panel_rank1(float* P, int ld, int64_t n, int q, double alpha, const 
 
 cudaError_t f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t s) {
   f64_to_f32_kernel<<<blocks(n), 256, 0, s>>>(a, b, n);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t panel_to_bf16(const float* src, int64_t ld, int64_t rows, int cols, void* dst,
+                          int64_t ldh, cudaStream_t s) {
+  panel_to_bf16_kernel<<<blocks(rows * ldh), 256, 0, s>>>(src, ld, rows, cols,
+                                                          static_cast<__nv_bfloat16*>(dst), ldh);
   ++g_launch_count;
   return cudaGetLastError();
 }

@@ -1,4 +1,4 @@
-// Tensor power method kernels (FP32 path).
+// Tensor power method kernels (FP32 form and BF16 form).
 //
 // The reference's STPM (GPU/stpm.c:497-790) issues ~2k+10 tiny library calls
 // per sample; tensorDecom_alpha0 (CPU/Util.cpp:131-184) runs k sparse
@@ -16,13 +16,18 @@
 // the cubic form (three Z's, three coefficient matrices, one stacked
 // contraction) and the loss.
 //
-// Partials are reduced deterministically by stpm_reduce; the k x k update
+// The contraction runs on the tensor cores (stpm_contract_kernel); partials
+// of 8-CTA clusters are summed through distributed shared memory and reduced
+// deterministically by stpm_reduce or by the step kernel.  The k x k update
 // (orthogonality term, step, Newton-Schulz polar orthonormalisation) runs on
-// one 8-CTA cluster exchanging column blocks through distributed shared memory.
+// one cluster of KP / 8 CTAs exchanging column blocks by bulk copies.
 #include "common.cuh"
 #include "k_stpm.cuh"
 
 #include <cooperative_groups.h>
+#include <cuda_bf16.h>
+
+#include <type_traits>
 
 namespace cg = cooperative_groups;
 
@@ -30,228 +35,9 @@ namespace mmsb {
 
 namespace {
 
-constexpr int TN = 32;  // nodes per tile
 constexpr int kPartialCluster = 8;  // CTAs whose partials are summed through DSMEM
 
 __device__ __forceinline__ int64_t ceil_div_dev(int64_t a, int64_t b) { return (a + b - 1) / b; }
-
-// dynamic smem layout helpers
-__host__ __device__ constexpr int ys_ld(int KP) { return KP + 1; }
-
-template <int KP, int MODE>
-__global__ void __launch_bounds__(256) stpm_partial_kernel(StpmPartialArgs a) {
-  constexpr int NZ = MODE == kModeAdjoint || MODE == kModeLoss ? 3 : 2;
-  constexpr int NY = 3;
-  constexpr int LD = ys_ld(KP);
-  constexpr int PT = KP / 16;  // contraction patch edge
-  constexpr int ZC = KP / 8;   // Z columns per thread
-  extern __shared__ float sm[];
-  float* Phis = sm;                          // KP x KP, row j = component j (Phis[j*KP+i] = Phi_ji)
-  float* Ys = Phis + KP * KP;                // NY tiles, each TN x LD
-  float* Cs = Ys + NY * TN * LD;             // NZ coefficient tiles (TN x LD) [plain: 1]
-  float* mv = Cs + (MODE == kModePlain ? 1 : 3) * TN * LD;  // m1, m2, m3 (KP each)
-  float* dsum = mv + 3 * KP;                 // 3 x KP accumulators of sum Z_a Z_b
-  const int tid = threadIdx.x;
-  const int k = a.k;
-
-  for (int e = tid; e < KP * KP; e += 256) {
-    const int j = e / KP, i = e % KP;
-    Phis[e] = (i < k && j < k) ? a.phi[(int64_t)i * k + j] : 0.f;
-  }
-  // stage mu_1..3 in dsum (zeroed again below)
-  for (int e = tid; e < 3 * KP; e += 256) {
-    const int which = e / KP, j = e % KP;
-    const float* mu = which == 0 ? a.mu1 : which == 1 ? a.mu2 : a.mu3;
-    dsum[e] = (mu && j < k) ? mu[j] : 0.f;
-  }
-  __syncthreads();
-  // m_P = Phi^T mu_P
-  for (int e = tid; e < 3 * KP; e += 256) {
-    const int which = e / KP, i = e % KP;
-    const float* mu = dsum + which * KP;
-    float s0 = 0.f, s1 = 0.f;
-    if (i < k) {
-      int j = 0;
-      for (; j + 1 < k; j += 2) {
-        s0 = fmaf(Phis[j * KP + i], mu[j], s0);
-        s1 = fmaf(Phis[(j + 1) * KP + i], mu[j + 1], s1);
-      }
-      if (j < k) s0 = fmaf(Phis[j * KP + i], mu[j], s0);
-    }
-    mv[e] = s0 + s1;
-  }
-  __syncthreads();
-  for (int e = tid; e < 3 * KP; e += 256) dsum[e] = 0.f;
-  __syncthreads();
-
-  const int pj = tid / 16, pi = tid % 16;  // contraction patch (rows j, cols i)
-  float acc[PT][PT];
-#pragma unroll
-  for (int r = 0; r < PT; ++r)
-#pragma unroll
-    for (int c = 0; c < PT; ++c) acc[r][c] = 0.f;
-  float tsum = 0.f;  // loss mode: sum of t over this thread's entries
-  float dloc[3][ZC];
-#pragma unroll
-  for (int q = 0; q < 3; ++q)
-#pragma unroll
-    for (int c = 0; c < ZC; ++c) dloc[q][c] = 0.f;
-
-  const int x_lane = tid % TN, grp = tid / TN;
-  const int64_t ntiles = ceil_div_dev(a.count, TN);
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t x0 = a.begin + tile * TN;
-    const int64_t left = a.begin + a.count - x0;
-    const int nvalid = left < TN ? (int)left : TN;
-    // load the node tiles (row-major y, ld = a.ldy)
-    for (int q = 0; q < NY; ++q) {
-      const float* Y = q == 0 ? a.y1 : q == 1 ? a.y2 : a.y3;
-      float* dst = Ys + q * TN * LD;
-      for (int e = tid; e < TN * KP; e += 256) {
-        const int xx = e / KP, j = e % KP;
-        dst[xx * LD + j] = (xx < nvalid && j < k) ? Y[(x0 + xx) * a.ldy + j] : 0.f;
-      }
-    }
-    __syncthreads();
-    // Z = Y Phi for this thread's node and columns
-    float z[NZ][ZC];
-#pragma unroll
-    for (int q = 0; q < NZ; ++q)
-#pragma unroll
-      for (int c = 0; c < ZC; ++c) z[q][c] = 0.f;
-    {
-      const float* y0 = Ys + 0 * TN * LD + x_lane * LD;
-      const float* y1 = Ys + 1 * TN * LD + x_lane * LD;
-      const float* y2 = Ys + 2 * TN * LD + x_lane * LD;
-      for (int j = 0; j < KP; ++j) {
-        const float v0 = y0[j], v1 = y1[j];
-        const float v2 = NZ == 3 ? y2[j] : 0.f;
-        const float* ph = Phis + j * KP + grp;
-#pragma unroll
-        for (int c = 0; c < ZC; ++c) {
-          const float f = ph[8 * c];
-          z[0][c] = fmaf(v0, f, z[0][c]);
-          z[1][c] = fmaf(v1, f, z[1][c]);
-          if (NZ == 3) z[NZ - 1][c] = fmaf(v2, f, z[NZ - 1][c]);
-        }
-      }
-    }
-    const bool valid = x_lane < nvalid;
-#pragma unroll
-    for (int c = 0; c < ZC; ++c) {
-      const int i = grp + 8 * c;
-      const float m1 = mv[i], m2 = mv[KP + i];
-      if (MODE == kModePlain) {
-        const float z1 = z[0][c], z2 = z[1][c];
-        const float cf = a.c0 * z1 * z2 + a.c2 * (z1 * m2 + m1 * z2);
-        Cs[x_lane * LD + i] = valid ? cf : 0.f;
-        if (valid) dloc[0][c] = fmaf(z1, z2, dloc[0][c]);
-      } else {
-        const float m3 = mv[2 * KP + i];
-        const float z1 = z[0][c], z2 = z[1][c], z3 = z[2][c];
-        const float p0 = a.c0, p2 = a.c2;
-        if (MODE == kModeAdjoint) {
-          Cs[0 * TN * LD + x_lane * LD + i] = valid ? p0 * z2 * z3 + p2 * (z2 * m3 + m2 * z3) : 0.f;
-          Cs[1 * TN * LD + x_lane * LD + i] = valid ? p0 * z1 * z3 + p2 * (z1 * m3 + m1 * z3) : 0.f;
-          Cs[2 * TN * LD + x_lane * LD + i] = valid ? p0 * z1 * z2 + p2 * (z1 * m2 + m1 * z2) : 0.f;
-        }
-        if (valid) {
-          dloc[0][c] = fmaf(z2, z3, dloc[0][c]);
-          dloc[1][c] = fmaf(z1, z3, dloc[1][c]);
-          dloc[2][c] = fmaf(z1, z2, dloc[2][c]);
-          if (MODE == kModeLoss && i < k)
-            tsum += p0 * z1 * z2 * z3 + p2 * (z1 * z2 * m3 + z1 * m2 * z3 + m1 * z2 * z3);
-        }
-      }
-    }
-    __syncthreads();
-    if (MODE != kModeLoss) {
-      // G[j, i] += sum_x Yout[x, j] C[x, i]   (adjoint: sum over the three pairs)
-      constexpr int NPAIR = MODE == kModePlain ? 1 : 3;
-#pragma unroll
-      for (int q = 0; q < NPAIR; ++q) {
-        const float* Yo = Ys + (MODE == kModePlain ? 2 : q) * TN * LD;
-        const float* Cq = Cs + q * TN * LD;
-        for (int xx = 0; xx < TN; ++xx) {
-          float yv[PT], cv[PT];
-#pragma unroll
-          for (int r = 0; r < PT; ++r) yv[r] = Yo[xx * LD + pj * PT + r];
-#pragma unroll
-          for (int c = 0; c < PT; ++c) cv[c] = Cq[xx * LD + pi * PT + c];
-#pragma unroll
-          for (int r = 0; r < PT; ++r)
-#pragma unroll
-            for (int c = 0; c < PT; ++c) acc[r][c] = fmaf(yv[r], cv[c], acc[r][c]);
-        }
-      }
-    }
-    __syncthreads();
-  }
-  // d sums: reduce over the 32 node lanes of each group via smem atomics
-#pragma unroll
-  for (int q = 0; q < 3; ++q)
-#pragma unroll
-    for (int c = 0; c < ZC; ++c) {
-      float v = dloc[q][c];
-#pragma unroll
-      for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-      if (x_lane == 0 && (q == 0 || MODE != kModePlain)) dsum[q * KP + grp + 8 * c] = v;
-    }
-  if (MODE == kModeLoss) {
-#pragma unroll
-    for (int off = 16; off; off >>= 1) tsum += __shfl_xor_sync(0xffffffffu, tsum, off);
-  }
-  __syncthreads();
-  // cluster reduction: every CTA stages its partial (k x k column-major
-  // contraction, 3 d-sums, loss) in shared memory; CTA r of the cluster sums a
-  // 1/CLP slice over the cluster's CTAs through DSMEM and writes it out.
-  cg::cluster_group cluster = cg::this_cluster();
-  const int crank = (int)cluster.block_rank();
-  constexpr int CLP = kPartialCluster;
-  constexpr int STAGE = KP * KP + 3 * KP + 4;
-  float* stage = sm;  // Phi, y and C tiles are dead from here on
-  {
-    // dsum lives after the stage area (see layout), copy it in place first
-    float dtmp[3 * KP / 256 + 1];
-    int cnt = 0;
-    for (int e = tid; e < 3 * KP; e += 256) dtmp[cnt++] = dsum[e];
-    __shared__ float tred[8];
-    if (MODE == kModeLoss) {
-      if (x_lane == 0) tred[grp] = tsum;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < PT; ++r)
-#pragma unroll
-      for (int c = 0; c < PT; ++c) stage[(pi * PT + c) * KP + pj * PT + r] = acc[r][c];
-    cnt = 0;
-    for (int e = tid; e < 3 * KP; e += 256) stage[KP * KP + e] = dtmp[cnt++];
-    if (tid == 0) {
-      float t = 0.f;
-      if (MODE == kModeLoss)
-        for (int g8 = 0; g8 < 8; ++g8) t += tred[g8];
-      stage[KP * KP + 3 * KP] = t;
-    }
-  }
-  cluster.sync();
-  float* gp = a.gpart + (int64_t)(blockIdx.x / CLP) * a.part_stride;
-  const int slice = (STAGE + CLP - 1) / CLP;
-  for (int e = crank * slice + tid; e < min(STAGE, (crank + 1) * slice); e += 256) {
-    float v = 0.f;
-#pragma unroll
-    for (int q = 0; q < CLP; ++q) v += cluster.map_shared_rank(stage, q)[e];
-    if (e < KP * KP) {
-      const int i = e / KP, j = e % KP;
-      if (i < k && j < k && MODE != kModeLoss) gp[(int64_t)i * k + j] = v;
-    } else if (e < KP * KP + 3 * KP) {
-      const int q = (e - KP * KP) / KP, i = (e - KP * KP) % KP;
-      if (i < k) gp[(int64_t)k * k + q * k + i] = v;
-    } else if (e == KP * KP + 3 * KP) {
-      gp[(int64_t)k * k + 3 * k] = v;
-    }
-  }
-  cluster.sync();  // keep shared memory alive until every remote read is done
-}
 
 // G = sum_parts gpart + mu-terms; d-vectors folded in (see stpm_reduce doc).
 __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
@@ -496,10 +282,23 @@ __global__ void __launch_bounds__(512, 1) stpm_step_kernel(StpmUpdateArgs a) {
   const int k = a.k;
   const int c0 = rank * NB;
   const int tid = threadIdx.x, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
-  for (int e = tid; e < KP * XLD; e += blockDim.x) {
-    const int r = e % XLD, c = e / XLD;
-    Xa[e] = (r < k && c < k) ? a.phi[(int64_t)c * k + r] : 0.f;
-    Xb[e] = 0.f;
+  {
+    // Phi: loads issued in batches of 8 per thread so that their latencies overlap
+    constexpr int N = KP * XLD, B = 8;
+    for (int e0 = tid; e0 < N; e0 += 512 * B) {
+      float v[B];
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        const int e = e0 + 512 * u, r = e % XLD, c = e / XLD;
+        v[u] = (e < N && r < k && c < k) ? __ldg(a.phi + (int64_t)c * k + r) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < B; ++u)
+        if (e0 + 512 * u < N) {
+          Xa[e0 + 512 * u] = v[u];
+          Xb[e0 + 512 * u] = 0.f;
+        }
+    }
   }
   for (int e = tid; e < 2 * NB * XLD; e += blockDim.x) Ot[e] = 0.f;
   if (tid == 0) {
@@ -587,13 +386,16 @@ __global__ void __launch_bounds__(512, 1) stpm_step_kernel(StpmUpdateArgs a) {
         const float* gp = a.gpart + (int64_t)i * k + j;
         float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
         int pp = 0;
-        for (; pp + 4 <= a.nparts; pp += 4) {
-          s0 += gp[(int64_t)pp * a.part_stride];
-          s1 += gp[(int64_t)(pp + 1) * a.part_stride];
-          s2 += gp[(int64_t)(pp + 2) * a.part_stride];
-          s3 += gp[(int64_t)(pp + 3) * a.part_stride];
+        for (; pp + 8 <= a.nparts; pp += 8) {
+          float v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) v[u] = __ldg(gp + (int64_t)(pp + u) * a.part_stride);
+          s0 += v[0] + v[4];
+          s1 += v[1] + v[5];
+          s2 += v[2] + v[6];
+          s3 += v[3] + v[7];
         }
-        for (; pp < a.nparts; ++pp) s0 += gp[(int64_t)pp * a.part_stride];
+        for (; pp < a.nparts; ++pp) s0 += __ldg(gp + (int64_t)pp * a.part_stride);
         float gv = ((s0 + s1) + (s2 + s3)) * (float)a.scale;
         const float m1 = mv[jb], m2 = mv[KP + jb], m3 = mv[2 * KP + jb];
         const float c1 = (float)a.c1, c2 = (float)a.c2;
@@ -788,6 +590,375 @@ __global__ void __launch_bounds__(512, 1) stpm_step_kernel(StpmUpdateArgs a) {
   if (timed_out) __nanosleep(100000);  // let copies a stalled exchange left in flight land
 }
 
+// ---- partial contractions on the tensor cores -----------------------------------
+//
+// Per tile of TM nodes, with Phi resident in shared memory:
+//   Z_q^T = Phi^T Y_q^T           (k x TM, m16n8k8 3xTF32 or m16n8k16 BF16 MMAs;
+//                                  both operands contiguous along j)
+//   C = c0 Z1.Z2 + c2 (Z1 m2 + m1 Z2)   (on the Z fragments; stored i-major)
+//   G += Yout^T C                 (k x k, accumulated in registers over the
+//                                  CTA's tiles; the Yout operand is read
+//                                  transposed: strided loads in FP32,
+//                                  ldmatrix.trans in BF16)
+//   d_i += sum_x Z1 Z2            (per column i)
+// The FP32 form keeps FP32 accuracy through the 3xTF32 split; the BF16 form
+// reads y and Phi rounded to BF16 and accumulates in FP32.
+template <int KP, int MODE, bool BF>
+struct Contract {
+  using T = typename std::conditional<BF, __nv_bfloat16, float>::type;
+  static constexpr int TM = BF ? 64 : 32;  // nodes per tile
+  static constexpr int NZ = MODE == kModePlain ? 2 : 3;
+  static constexpr int NC = MODE == kModePlain ? 1 : MODE == kModeAdjoint ? 3 : 0;
+  static constexpr int PAD = BF ? 8 : 4;   // row strides == 4 words mod 8: conflict-free fragments
+  static constexpr int PLD = KP + PAD, LDY = KP + PAD, LDC = TM + PAD;
+  static constexpr int MTI = KP / 16, NTX = TM / 8, NTI = KP / 8;
+  static constexpr int GT = MTI * NTI, GPW = (GT + 7) / 8;  // G tiles (16 x 8), per warp
+  static constexpr int KSTEP = BF ? 16 : 8;
+  static constexpr size_t tile_bytes =
+      sizeof(T) * ((size_t)KP * PLD + (size_t)3 * TM * LDY + (size_t)NC * KP * LDC);
+  static constexpr size_t stage_bytes = sizeof(float) * ((size_t)KP * KP + 3 * KP + 4);
+  static constexpr size_t region = ((tile_bytes > stage_bytes ? tile_bytes : stage_bytes) + 15) / 16 * 16;
+  static constexpr size_t smem = region + sizeof(float) * (3 * KP + 8 + 8 * 3 * KP);
+};
+
+template <typename T>
+__device__ __forceinline__ T to_elem(float v);
+template <>
+__device__ __forceinline__ float to_elem<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ __nv_bfloat16 to_elem<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+__device__ __forceinline__ uint32_t ld_b32(const void* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(smem_addr(p)));
+}
+
+__device__ __forceinline__ void split_tf32(float v, uint32_t& hi, uint32_t& lo) {
+  hi = tf32_round(v);
+  lo = tf32_round(v - __uint_as_float(hi));
+}
+
+template <int KP, int MODE, bool BF>
+__global__ void __launch_bounds__(256) stpm_contract_kernel(StpmPartialArgs a) {
+  using Cfg = Contract<KP, MODE, BF>;
+  using T = typename Cfg::T;
+  constexpr int TM = Cfg::TM, NZ = Cfg::NZ, NC = Cfg::NC, PLD = Cfg::PLD, LDY = Cfg::LDY,
+                LDC = Cfg::LDC;
+  static_assert(KP % 16 == 0 && KP <= 128, "KP");
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* Phis = reinterpret_cast<T*>(smraw);  // Phis[i PLD + j] = Phi_ji (column i of Phi)
+  T* Ys = Phis + KP * PLD;                // 3 node-major tiles: Ys[q TM LDY + x LDY + j]
+  T* CT = Ys + 3 * TM * LDY;              // NC coefficient tiles, i-major: CT[c KP LDC + i LDC + x]
+  float* mv = reinterpret_cast<float*>(smraw + Cfg::region);  // m1 | m2 | m3
+  float* tred = mv + 3 * KP;                                  // 8 loss partials
+  float* dw = tred + 8;  // per-warp d-sums (3 KP each), summed in a fixed order at the end
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, g = lane >> 2, t4 = lane & 3;
+  const int k = a.k;
+
+  // Phi: loads issued in batches of 8 per thread so that their latencies overlap
+  {
+    constexpr int N = KP * PLD, B = 8;
+    for (int e0 = tid; e0 < N; e0 += 256 * B) {
+      float v[B];
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        const int e = e0 + 256 * u, i = e / PLD, j = e % PLD;
+        v[u] = (e < N && i < k && j < k) ? __ldg(a.phi + (int64_t)i * k + j) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < B; ++u)
+        if (e0 + 256 * u < N) Phis[e0 + 256 * u] = to_elem<T>(v[u]);
+    }
+  }
+  // m_P = Phi^T mu_P with Phi as staged (mu_1..3 staged in dw, which is
+  // free until the d-sums start)
+  for (int e = tid; e < 3 * KP; e += 256) {
+    const int which = e / KP, j = e % KP;
+    const float* mu = which == 0 ? a.mu1 : which == 1 ? a.mu2 : a.mu3;
+    dw[e] = (mu && j < k) ? mu[j] : 0.f;
+  }
+  __syncthreads();
+  for (int e = tid; e < 3 * KP; e += 256) {
+    const float* mu = dw + (e / KP) * KP;
+    const T* ph = Phis + (e % KP) * PLD;
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll 4
+    for (int j = 0; j < KP; j += 2) {
+      s0 = fmaf(to_f32(ph[j]), mu[j], s0);
+      s1 = fmaf(to_f32(ph[j + 1]), mu[j + 1], s1);
+    }
+    mv[e] = s0 + s1;
+  }
+  __syncthreads();
+  for (int e = tid; e < 8 * 3 * KP; e += 256) dw[e] = 0.f;
+  if (tid < 8) tred[tid] = 0.f;
+  __syncthreads();
+
+  float gacc[Cfg::GPW][4];
+#pragma unroll
+  for (int u = 0; u < Cfg::GPW; ++u)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) gacc[u][q] = 0.f;
+  float tsum = 0.f;
+  const float cc0 = a.c0, cc2 = a.c2;
+
+  const int64_t ntiles = ceil_div_dev(a.count, TM);
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t x0 = a.begin + tile * TM;
+    const int64_t left = a.begin + a.count - x0;
+    const int nvalid = left < TM ? (int)left : TM;
+    // node tiles, 16-byte chunks; columns past the stored row are zero
+    constexpr int CH = 16 / (int)sizeof(T), NCH = KP / CH;
+    {
+      constexpr int N = 3 * TM * NCH, B = 4;
+      for (int e0 = tid; e0 < N; e0 += 256 * B) {
+        uint4 v[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+          const int e = e0 + 256 * u;
+          const int q = e / (TM * NCH), rem = e % (TM * NCH), xx = rem / NCH, c = rem % NCH;
+          v[u] = make_uint4(0u, 0u, 0u, 0u);
+          if (e < N) {
+            if (BF) {
+              const T* Y = static_cast<const T*>(q == 0 ? a.yh1 : q == 1 ? a.yh2 : a.yh3);
+              if (xx < nvalid && c * CH < a.ldyh)
+                v[u] = __ldg(reinterpret_cast<const uint4*>(Y + (x0 + xx) * a.ldyh + c * CH));
+            } else {
+              const float* Y = q == 0 ? a.y1 : q == 1 ? a.y2 : a.y3;
+              if (xx < nvalid && c * CH < a.ldy)
+                v[u] = __ldg(reinterpret_cast<const uint4*>(Y + (x0 + xx) * a.ldy + c * CH));
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+          const int e = e0 + 256 * u;
+          if (e >= N) break;
+          const int q = e / (TM * NCH), rem = e % (TM * NCH), xx = rem / NCH, c = rem % NCH;
+          *reinterpret_cast<uint4*>(Ys + q * TM * LDY + xx * LDY + c * CH) = v[u];
+        }
+      }
+    }
+    __syncthreads();
+
+    // ---- Z^T tiles (16 i x 8 x), C and the d-sums
+    for (int p = warp; p < Cfg::MTI * Cfg::NTX; p += 8) {
+      const int m0 = (p % Cfg::MTI) * 16, n0 = (p / Cfg::MTI) * 8;
+      float z[NZ][4];
+#pragma unroll
+      for (int q = 0; q < NZ; ++q)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) z[q][r] = 0.f;
+      if (BF) {
+#pragma unroll 2
+        for (int k0 = 0; k0 < KP; k0 += 16) {
+          const T* pa = Phis + m0 * PLD + k0 + 2 * t4;
+          const uint32_t af[4] = {ld_b32(pa + g * PLD), ld_b32(pa + (g + 8) * PLD),
+                                  ld_b32(pa + g * PLD + 8), ld_b32(pa + (g + 8) * PLD + 8)};
+#pragma unroll
+          for (int q = 0; q < NZ; ++q) {
+            const T* pb = Ys + q * TM * LDY + (n0 + g) * LDY + k0 + 2 * t4;
+            const uint32_t bf[2] = {ld_b32(pb), ld_b32(pb + 8)};
+            mma_bf16(z[q], af, bf);
+          }
+        }
+      } else {
+        float zc[NZ][4];
+#pragma unroll
+        for (int q = 0; q < NZ; ++q)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) zc[q][r] = 0.f;
+#pragma unroll 2
+        for (int k0 = 0; k0 < KP; k0 += 8) {
+          const float* pa = reinterpret_cast<const float*>(Phis) + m0 * PLD + k0 + t4;
+          uint32_t ah[4], al[4];
+          split_tf32(pa[g * PLD], ah[0], al[0]);
+          split_tf32(pa[(g + 8) * PLD], ah[1], al[1]);
+          split_tf32(pa[g * PLD + 4], ah[2], al[2]);
+          split_tf32(pa[(g + 8) * PLD + 4], ah[3], al[3]);
+#pragma unroll
+          for (int q = 0; q < NZ; ++q) {
+            const float* pb = reinterpret_cast<const float*>(Ys) + q * TM * LDY + (n0 + g) * LDY + k0 + t4;
+            uint32_t bh[2], bl[2];
+            split_tf32(pb[0], bh[0], bl[0]);
+            split_tf32(pb[4], bh[1], bl[1]);
+            mma_tf32(z[q], ah, bh);
+            mma_tf32(zc[q], ah, bl);
+            mma_tf32(zc[q], al, bh);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < NZ; ++q)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) z[q][r] += zc[q][r];
+      }
+      // epilogue: fragment r holds (i = m0 + g + 8 (r >> 1), x = n0 + 2 t4 + (r & 1))
+      float dl[3][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      float cv[3][4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int i = m0 + g + 8 * (r >> 1), x = n0 + 2 * t4 + (r & 1);
+        const bool valid = x < nvalid && i < k;
+        const float m1 = mv[i], m2 = mv[KP + i];
+        const float z1 = z[0][r], z2 = z[1][r];
+        if (MODE == kModePlain) {
+          cv[0][r] = valid ? cc0 * z1 * z2 + cc2 * (z1 * m2 + m1 * z2) : 0.f;
+          if (valid) dl[0][r >> 1] = fmaf(z1, z2, dl[0][r >> 1]);
+        } else {
+          const float m3 = mv[2 * KP + i], z3 = z[NZ - 1][r];
+          if (MODE == kModeAdjoint) {
+            cv[0][r] = valid ? cc0 * z2 * z3 + cc2 * (z2 * m3 + m2 * z3) : 0.f;
+            cv[1][r] = valid ? cc0 * z1 * z3 + cc2 * (z1 * m3 + m1 * z3) : 0.f;
+            cv[2][r] = valid ? cc0 * z1 * z2 + cc2 * (z1 * m2 + m1 * z2) : 0.f;
+          }
+          if (valid) {
+            dl[0][r >> 1] = fmaf(z2, z3, dl[0][r >> 1]);
+            dl[1][r >> 1] = fmaf(z1, z3, dl[1][r >> 1]);
+            dl[2][r >> 1] = fmaf(z1, z2, dl[2][r >> 1]);
+            if (MODE == kModeLoss)
+              tsum += cc0 * z1 * z2 * z3 + cc2 * (z1 * z2 * m3 + z1 * m2 * z3 + m1 * z2 * z3);
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          T* dst = CT + c * KP * LDC + (m0 + g + 8 * h) * LDC + n0 + 2 * t4;
+          if (BF) {
+            *reinterpret_cast<__nv_bfloat162*>(dst) = __floats2bfloat162_rn(cv[c][2 * h], cv[c][2 * h + 1]);
+          } else {
+            *reinterpret_cast<float2*>(dst) = make_float2(cv[c][2 * h], cv[c][2 * h + 1]);
+          }
+        }
+#pragma unroll
+      for (int qd = 0; qd < 3; ++qd) {
+        if (MODE == kModePlain && qd > 0) continue;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          float v = dl[qd][h];
+          v += __shfl_xor_sync(0xffffffffu, v, 1);
+          v += __shfl_xor_sync(0xffffffffu, v, 2);
+          if (t4 == 0) dw[warp * 3 * KP + qd * KP + m0 + g + 8 * h] += v;
+        }
+      }
+    }
+    __syncthreads();
+
+    // ---- G (16 j x 8 i tiles) += Yout^T C over this tile's nodes
+    if (NC > 0) {
+#pragma unroll
+      for (int k0 = 0; k0 < TM; k0 += Cfg::KSTEP) {
+#pragma unroll
+        for (int u = 0; u < Cfg::GPW; ++u) {
+          const int tt = warp + 8 * u;
+          if (tt >= Cfg::GT) continue;
+          const int m0 = (tt % Cfg::MTI) * 16, n0 = (tt / Cfg::MTI) * 8;
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            const T* Yo = Ys + (MODE == kModePlain ? 2 : c) * TM * LDY;
+            const T* Cc = CT + c * KP * LDC;
+            if (BF) {
+              uint32_t af[4];
+              const int q = lane >> 3, rr = lane & 7;
+              ldsm_x4_trans(af, Yo + (k0 + (q >> 1) * 8 + rr) * LDY + m0 + (q & 1) * 8);
+              const T* pb = Cc + (n0 + g) * LDC + k0 + 2 * t4;
+              const uint32_t bf[2] = {ld_b32(pb), ld_b32(pb + 8)};
+              mma_bf16(gacc[u], af, bf);
+            } else {
+              const float* pa = reinterpret_cast<const float*>(Yo) + (k0 + t4) * LDY + m0 + g;
+              uint32_t ah[4], al[4];
+              split_tf32(pa[0], ah[0], al[0]);
+              split_tf32(pa[8], ah[1], al[1]);
+              split_tf32(pa[4 * LDY], ah[2], al[2]);
+              split_tf32(pa[4 * LDY + 8], ah[3], al[3]);
+              const float* pb = reinterpret_cast<const float*>(Cc) + (n0 + g) * LDC + k0 + t4;
+              uint32_t bh[2], bl[2];
+              split_tf32(pb[0], bh[0], bl[0]);
+              split_tf32(pb[4], bh[1], bl[1]);
+              mma_tf32(gacc[u], ah, bh);
+              mma_tf32(gacc[u], ah, bl);
+              mma_tf32(gacc[u], al, bh);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (MODE == kModeLoss) {
+#pragma unroll
+    for (int off = 16; off; off >>= 1) tsum += __shfl_xor_sync(0xffffffffu, tsum, off);
+    if (lane == 0) tred[warp] = tsum;
+  }
+  // cluster reduction: every CTA stages its partial (k x k column-major
+  // contraction, 3 d-sums, loss) in shared memory; CTA r of the cluster sums a
+  // 1/CLP slice over the cluster's CTAs through DSMEM and writes it out.
+  float* stage = reinterpret_cast<float*>(smraw);  // tiles are dead from here on
+  if (NC > 0) {
+#pragma unroll
+    for (int u = 0; u < Cfg::GPW; ++u) {
+      const int tt = warp + 8 * u;
+      if (tt >= Cfg::GT) continue;
+      const int m0 = (tt % Cfg::MTI) * 16, n0 = (tt / Cfg::MTI) * 8;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int j = m0 + g + 8 * (r >> 1), i = n0 + 2 * t4 + (r & 1);
+        stage[i * KP + j] = gacc[u][r];
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < 3 * KP; e += 256) {
+    float v = 0.f;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) v += dw[w * 3 * KP + e];
+    stage[KP * KP + e] = v;
+  }
+  if (tid == 0) {
+    float t = 0.f;
+    if (MODE == kModeLoss)
+      for (int w = 0; w < 8; ++w) t += tred[w];
+    stage[KP * KP + 3 * KP] = t;
+  }
+  cg::cluster_group cluster = cg::this_cluster();
+  const int crank = (int)cluster.block_rank();
+  constexpr int CLP = kPartialCluster;
+  constexpr int STAGE = KP * KP + 3 * KP + 4;
+  cluster.sync();
+  float* gp = a.gpart + (int64_t)(blockIdx.x / CLP) * a.part_stride;
+  const int slice = (STAGE + CLP - 1) / CLP;
+  for (int e = crank * slice + tid; e < min(STAGE, (crank + 1) * slice); e += 256) {
+    float v = 0.f;
+#pragma unroll
+    for (int q = 0; q < CLP; ++q) v += cluster.map_shared_rank(stage, q)[e];
+    if (e < KP * KP) {
+      const int i = e / KP, j = e % KP;
+      if (i < k && j < k && MODE != kModeLoss) gp[(int64_t)i * k + j] = v;
+    } else if (e < KP * KP + 3 * KP) {
+      const int q = (e - KP * KP) / KP, i = (e - KP * KP) % KP;
+      if (i < k) gp[(int64_t)k * k + q * k + i] = v;
+    } else if (e == KP * KP + 3 * KP) {
+      gp[(int64_t)k * k + 3 * k] = v;
+    }
+  }
+  cluster.sync();  // keep shared memory alive until every remote read is done
+}
+
 // batch power: Phi_new = G (already includes the shift terms), lambda = ||col||^3,
 // column normalisation, error = ||Phi_new - Phi_old||_F
 __global__ void __launch_bounds__(1024) batch_update_kernel(int k, float* __restrict__ phi,
@@ -834,12 +1005,12 @@ __global__ void tensor_value_kernel(int k, float* __restrict__ phi, const float*
     for (int j = lane; j < k; j += 32) phi[(int64_t)i * k + j] = -phi[(int64_t)i * k + j];
 }
 
-template <int KP, int MODE>
+template <int KP, int MODE, bool BF>
 cudaError_t launch_partial_t(const StpmPartialArgs& a, int grid, cudaStream_t s) {
-  const size_t smem = stpm_partial_smem(KP, MODE);
+  const size_t smem = Contract<KP, MODE, BF>::smem;
   static bool set = false;
   if (!set) {
-    MMSB_CUDA_TRY(cudaFuncSetAttribute(stpm_partial_kernel<KP, MODE>,
+    MMSB_CUDA_TRY(cudaFuncSetAttribute(stpm_contract_kernel<KP, MODE, BF>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     set = true;
   }
@@ -855,21 +1026,31 @@ cudaError_t launch_partial_t(const StpmPartialArgs& a, int grid, cudaStream_t s)
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  MMSB_CUDA_TRY(cudaLaunchKernelEx(&cfg, stpm_partial_kernel<KP, MODE>, a));
+  MMSB_CUDA_TRY(cudaLaunchKernelEx(&cfg, stpm_contract_kernel<KP, MODE, BF>, a));
   ++g_launch_count;
   return cudaGetLastError();
 }
 
-template <int MODE>
+template <int MODE, bool BF>
 cudaError_t launch_partial_m(int KP, const StpmPartialArgs& a, int grid, cudaStream_t s) {
   switch (KP) {
-    case 32: return launch_partial_t<32, MODE>(a, grid, s);
-    case 48: return launch_partial_t<48, MODE>(a, grid, s);
-    case 64: return launch_partial_t<64, MODE>(a, grid, s);
-    case 80: return launch_partial_t<80, MODE>(a, grid, s);
-    case 96: return launch_partial_t<96, MODE>(a, grid, s);
-    case 112: return launch_partial_t<112, MODE>(a, grid, s);
-    case 128: return launch_partial_t<128, MODE>(a, grid, s);
+    case 32: return launch_partial_t<32, MODE, BF>(a, grid, s);
+    case 48: return launch_partial_t<48, MODE, BF>(a, grid, s);
+    case 64: return launch_partial_t<64, MODE, BF>(a, grid, s);
+    case 80: return launch_partial_t<80, MODE, BF>(a, grid, s);
+    case 96: return launch_partial_t<96, MODE, BF>(a, grid, s);
+    case 112: return launch_partial_t<112, MODE, BF>(a, grid, s);
+    case 128: return launch_partial_t<128, MODE, BF>(a, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <bool BF>
+cudaError_t launch_partial_p(int mode, int KP, const StpmPartialArgs& a, int grid, cudaStream_t s) {
+  switch (mode) {
+    case kModePlain: return launch_partial_m<kModePlain, BF>(KP, a, grid, s);
+    case kModeAdjoint: return launch_partial_m<kModeAdjoint, BF>(KP, a, grid, s);
+    case kModeLoss: return launch_partial_m<kModeLoss, BF>(KP, a, grid, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -927,28 +1108,19 @@ int stpm_partial_cluster() { return kPartialCluster; }
 
 int stpm_kp(int k) { return (int)round_up(k, 16) < 32 ? 32 : (int)round_up(k, 16); }
 
-size_t stpm_partial_smem(int KP, int mode) {
-  const int LD = ys_ld(KP);
-  const int ncs = mode == kModePlain ? 1 : 3;
-  return sizeof(float) * ((size_t)KP * KP + (size_t)3 * TN * LD + (size_t)ncs * TN * LD + 3 * KP +
-                          3 * KP);
-}
-
-int stpm_partial_grid(int64_t count) {
-  const int64_t tiles = ceil_div(count, TN);
+int stpm_partial_grid(int64_t count, bool bf16) {
+  const int64_t tiles = ceil_div(count, bf16 ? 64 : 32);
   const int64_t g = std::max<int64_t>(1, std::min<int64_t>(tiles, 2 * kNumSMs));
   return (int)round_up(g, kPartialCluster);
 }
 
-cudaError_t stpm_partial(int mode, const StpmPartialArgs& a, int grid, cudaStream_t s) {
+cudaError_t stpm_partial(int mode, const StpmPartialArgs& a, int grid, bool bf16, cudaStream_t s) {
   const int KP = stpm_kp(a.k);
   if (KP > 128) return cudaErrorInvalidValue;
-  switch (mode) {
-    case kModePlain: return launch_partial_m<kModePlain>(KP, a, grid, s);
-    case kModeAdjoint: return launch_partial_m<kModeAdjoint>(KP, a, grid, s);
-    case kModeLoss: return launch_partial_m<kModeLoss>(KP, a, grid, s);
-    default: return cudaErrorInvalidValue;
-  }
+  if (bf16 && (!a.yh1 || !a.yh2 || !a.yh3 || a.ldyh % 8 != 0)) return cudaErrorInvalidValue;
+  if (!bf16 && a.ldy % 4 != 0) return cudaErrorInvalidValue;
+  return bf16 ? launch_partial_p<true>(mode, KP, a, grid, s)
+              : launch_partial_p<false>(mode, KP, a, grid, s);
 }
 
 cudaError_t stpm_reduce(const StpmReduceArgs& a, cudaStream_t s) {

@@ -20,7 +20,11 @@ struct StpmPartialArgs {
   const float* y1;
   const float* y2;
   const float* y3;  // plain: Yout
-  int64_t ldy;      // row stride of the node-major y arrays
+  int64_t ldy;      // row stride of the node-major y arrays (multiple of 4)
+  const void* yh1;  // BF16 copies of y1..y3 (BF16 form), row stride ldyh (multiple of 8)
+  const void* yh2;
+  const void* yh3;
+  int64_t ldyh;
   const float* phi; // k x k column-major
   const float* mu1;
   const float* mu2;
@@ -75,12 +79,13 @@ struct StpmUpdateArgs {
 
 int stpm_kp(int k);
 int stpm_step_kp(int k);
-size_t stpm_partial_smem(int KP, int mode);
 // grid of the partial kernel (a multiple of its cluster size); partial
 // blocks written = grid / stpm_partial_cluster()
-int stpm_partial_grid(int64_t count);
+int stpm_partial_grid(int64_t count, bool bf16);
 int stpm_partial_cluster();
-cudaError_t stpm_partial(int mode, const StpmPartialArgs& a, int grid, cudaStream_t s);
+// bf16: y read from yh1..yh3 and Phi rounded to BF16 (FP32 accumulation);
+// otherwise FP32 operands through the 3xTF32 split
+cudaError_t stpm_partial(int mode, const StpmPartialArgs& a, int grid, bool bf16, cudaStream_t s);
 cudaError_t stpm_reduce(const StpmReduceArgs& a, cudaStream_t s);
 cudaError_t stpm_update(const StpmUpdateArgs& a, cudaStream_t s);
 cudaError_t stpm_batch_update(int k, float* phi, const float* G, double* lambda, double* err,

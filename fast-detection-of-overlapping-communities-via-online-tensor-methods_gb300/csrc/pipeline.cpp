@@ -490,9 +490,9 @@ struct PartialOut {
 
 // per-CTA partial contractions over nodes [begin, begin+count)
 static PartialOut stpm_partials(mmsb_ctx* c, int mode, int q1, int q2, int q3, int64_t begin,
-                                int64_t count, double c0, double c2) {
+                                int64_t count, double c0, double c2, bool bf16 = false) {
   const int k = c->k;
-  const int grid = stpm_partial_grid(count);
+  const int grid = stpm_partial_grid(count, bf16);
   const int64_t stride = (int64_t)k * k + 3 * k + 4;
   float* gpart = c->tbuf<float>("gpart", (size_t)grid * stride);
   StpmPartialArgs a{};
@@ -500,6 +500,12 @@ static PartialOut stpm_partials(mmsb_ctx* c, int mode, int q1, int q2, int q3, i
   a.y2 = c->y[q2];
   a.y3 = c->y[q3];
   a.ldy = c->ldk;
+  if (bf16) {
+    a.yh1 = c->yh[q1];
+    a.yh2 = c->yh[q2];
+    a.yh3 = c->yh[q3];
+    a.ldyh = c->ldkh;
+  }
   a.phi = c->phi;
   a.mu1 = c->ymu + q1 * k;
   a.mu2 = c->ymu + q2 * k;
@@ -511,7 +517,7 @@ static PartialOut stpm_partials(mmsb_ctx* c, int mode, int q1, int q2, int q3, i
   a.c2 = (float)c2;
   a.gpart = gpart;
   a.part_stride = stride;
-  ck(stpm_partial(mode, a, grid, c->s), "stpm_partial");
+  ck(stpm_partial(mode, a, grid, bf16, c->s), "stpm_partial");
   return PartialOut{gpart, grid / stpm_partial_cluster(), stride};
 }
 
@@ -560,9 +566,10 @@ static void polar_only(mmsb_ctx* c, int* ns_iters) {
 // one minibatch update: partial contractions, then the fused reduction +
 // Phi - beta (3 theta O - gscale G) + polar orthonormalisation on one cluster
 static void stpm_step(mmsb_ctx* c, int mode, int64_t x0, int64_t cnt, double c0, double c1,
-                      double c2, double scale, double beta, double gscale, int* ns_iters) {
+                      double c2, double scale, double beta, double gscale, int* ns_iters,
+                      bool bf16) {
   const int k = c->k;
-  PartialOut po = stpm_partials(c, mode, 0, 1, 2, x0, cnt, c0, c2);
+  PartialOut po = stpm_partials(c, mode, 0, 1, 2, x0, cnt, c0, c2, bf16);
   StpmUpdateArgs u = step_args(c, kStepOnline, ns_iters);
   u.mode = mode;
   u.gpart = po.gpart;
@@ -622,16 +629,27 @@ void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
   } else {
     const bool adj = c->cfg.stpm_method == MMSB_STPM_ADJOINT;
     const int64_t b = std::max<int64_t>(1, std::min<int64_t>(c->cfg.minibatch, nx));
+    // BF16 form: y and Phi enter the contraction in BF16 (FP32 accumulation)
+    // for every sweep but the last, which refines in FP32
+    const bool bf16_form = c->cfg.precision == MMSB_PREC_BF16;
+    if (bf16_form) {
+      c->ldkh = (int)round_up(k, 8);
+      for (int q = 0; q < 3; ++q) {
+        c->yh[q] = c->buf("yh" + std::to_string(q), sizeof(uint16_t) * (size_t)nx * c->ldkh);
+        ck(panel_to_bf16(c->y[q], c->ldk, nx, k, c->yh[q], c->ldkh, s), "y bf16");
+      }
+    }
     int64_t t = 0;
     for (int sw = 0; sw < c->cfg.sweeps; ++sw) {
+      const bool bf = bf16_form && sw + 1 < c->cfg.sweeps;
       for (int64_t x0 = 0; x0 < nx; x0 += b) {
         if (c->stop.load()) throw MmsbError(MMSB_ERR_STOPPED, "stop requested");
         const int64_t cnt = std::min<int64_t>(b, nx - x0);
         const double beta = c->cfg.lr0 / (1.0 + (double)t);
         if (adj)  // dT (column i = d That_i / d phi_i); step = 3 theta O - dT
-          stpm_step(c, kModeAdjoint, x0, cnt, p0, p1, p2, 1.0 / cnt, beta, 1.0, ns_it);
+          stpm_step(c, kModeAdjoint, x0, cnt, p0, p1, p2, 1.0 / cnt, beta, 1.0, ns_it, bf);
         else  // G = mean of The_second_term; step = 3 theta O - 3 G
-          stpm_step(c, kModePlain, x0, cnt, p0 / cnt, p1, p2 / cnt, 1.0, beta, 3.0, ns_it);
+          stpm_step(c, kModePlain, x0, cnt, p0 / cnt, p1, p2 / cnt, 1.0, beta, 3.0, ns_it, bf);
         ++t;
       }
     }
