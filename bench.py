@@ -144,11 +144,21 @@ def make_graph(mm, wl):
 
 
 def peaks():
+    """Roofline denominators: the measured copy bandwidth and bf16 GEMM rate
+    (sustained: every kernel here is timed inside a long pipeline step)."""
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return d.get("hbm_gbs", 6800.0), "measured"
-    return 6800.0, "fallback"
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0),
+                "tflops": d.get("bf16_tflops_sustained", d.get("bf16_tflops", 1700.0)),
+                "source": "measured (hbm copy; bf16 GEMM sustained)"}
+    return {"hbm_gbs": 6800.0, "tflops": 1700.0, "source": "fallback"}
+
+
+# DRAM bytes (read + write) per launch of the STPM kernels, from the ncu
+# capture summarised in profiles/stpm_kernels_tensor_n20k_full.md (k = 100,
+# 4,096-node minibatches: the same per-launch shapes as the full workload)
+NCU_TRAFFIC_PER_LAUNCH = {"stpm_step_kernel": 270592, "stpm_contract_kernel": 5031424}
 
 
 # ---------------------------------------------------------------------------
@@ -253,6 +263,8 @@ def run_ours(args, wl, ws, rank, local):
     clocks.start()
     dev_ms, spmm_ms, spmm_bytes, spmm_launch, launches = [], 0.0, 0.0, 0, 0
     ns_iters, stpm_steps = 0, 0
+    kern = {"contract_ms": 0.0, "contract_flops": 0.0, "contract_launches": 0,
+            "step_ms": 0.0, "step_flops": 0.0, "step_launches": 0}
     stage = {"whiten_ms": 0.0, "stpm_ms": 0.0, "post_ms": 0.0}
     t_host0 = time.perf_counter()
     for _ in range(args.steps):
@@ -269,6 +281,8 @@ def run_ours(args, wl, ws, rank, local):
         launches += st["kernel_launches"]
         ns_iters += st["polar_iterations"]
         stpm_steps += st["stpm_steps"]
+        for key in kern:
+            kern[key] += st[key]
     p.synchronize()
     t_host = time.perf_counter() - t_host0
     dist.barrier()
@@ -294,8 +308,58 @@ def run_ours(args, wl, ws, rank, local):
     e2e_step = dist.max(statistics.median(e2e_ms))
     e2e_value = nX * wl["sweeps"] / (e2e_step / 1e3) * ws
 
-    peak, peak_kind = peaks()
-    achieved = (spmm_bytes / max(spmm_ms, 1e-9) / 1e6) if spmm_ms > 0 else None
+    # BF16 adjoint form on the same graph: y and Phi in BF16 on the tensor
+    # cores for all sweeps but the last (FP32 refinement)
+    cfg_bf = mm.default_config(k=wl["k"], alpha0=wl["alpha0"], stpm_method=mm.STPM_ADJOINT,
+                               sweeps=wl["sweeps"], minibatch=wl["minibatch"], seed=wl["seed"],
+                               device=local, tau=0.1, precision=mm.PREC_BF16)
+    pb = mm.Pipeline(cfg_bf)
+    pb.upload(graph)
+    for _ in range(max(1, min(args.warmup, 2))):
+        pb.run()
+    bf_ms, bf_stage = [], {"whiten_ms": 0.0, "stpm_ms": 0.0, "post_ms": 0.0}
+    for _ in range(args.steps):
+        pb.flush_l2()
+        pb.synchronize()
+        pb.run()
+        st = pb.stats()
+        bf_ms.append(st["total_ms"])
+        for key in bf_stage:
+            bf_stage[key] += st[key]
+    pb.close()
+    bf_step = dist.max(sum(bf_ms) / len(bf_ms))
+    bf_value = nX * wl["sweeps"] / (bf_step / 1e3) * ws
+
+    pk = peaks()
+
+    def tensor_entry(name, ms, flops, launches):
+        if launches == 0 or ms <= 0:
+            return None
+        per_launch_ms = ms / launches
+        achieved = flops / launches / (per_launch_ms / 1e3) / 1e12
+        traffic = NCU_TRAFFIC_PER_LAUNCH.get(name.split(" ")[0])
+        return {"kernel": name, "bound": "tensor", "achieved": achieved, "peak": pk["tflops"],
+                "unit": "TFLOP/s", "frac": achieved / pk["tflops"], "traffic": traffic,
+                "launches_per_step": launches / args.steps, "ms_per_step": ms / args.steps,
+                "algorithmic_flops_per_launch": flops / launches, "peak_source": pk["source"]}
+
+    step_rf = tensor_entry("stpm_step_kernel (k x k update + scaled Newton-Schulz polar, "
+                           "3xTF32 mma.sync on a KP/8-CTA cluster)", kern["step_ms"],
+                           kern["step_flops"], kern["step_launches"])
+    contract_rf = tensor_entry("stpm_contract_kernel (Z = Phi^T y, alpha0 terms, G += y^T C; "
+                               "3xTF32 mma.sync)", kern["contract_ms"], kern["contract_flops"],
+                               kern["contract_launches"])
+    spmm_achieved = (spmm_bytes / max(spmm_ms, 1e-9) / 1e6) if spmm_ms > 0 else None
+    spmm_rf = {"kernel": "spmm_rows_kernel (whitening CSR SpMM)", "bound": "hbm",
+               "achieved": spmm_achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+               "frac": (spmm_achieved / pk["hbm_gbs"]) if spmm_achieved else None,
+               "traffic": None, "launches_per_step": spmm_launch / args.steps,
+               "ms_per_step": spmm_ms / args.steps,
+               "algorithmic_bytes_per_step": spmm_bytes / args.steps,
+               "note": "algorithmic bytes count one panel-row gather per nonzero; the 2k-wide "
+                       "panels (<= 160 MB) stay largely L2-resident, so frac can exceed 1"}
+    entries = [e for e in (step_rf, contract_rf, spmm_rf) if e]
+    dominant = max(entries, key=lambda e: e["ms_per_step"])
     line = {
         "metric": "stpm_node_updates_per_s", "value": value, "unit": "node-updates/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
@@ -313,11 +377,13 @@ def run_ours(args, wl, ws, rank, local):
         "e2e": {"value": e2e_value, "unit": "node-updates/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_step},
         "gpu_launches": launches,
-        "roofline": {"kernel": "spmm_rows_kernel (whitening SpMM)", "bound": "hbm",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
-                     "peak_source": peak_kind, "launches_per_step": spmm_launch / args.steps,
-                     "algorithmic_bytes_per_step": spmm_bytes / args.steps},
+        "roofline": dominant,
+        "roofline_kernels": entries,
+        "whitening_spmm_gbs": spmm_achieved,
+        "bf16_adjoint": {"value": bf_value, "unit": "node-updates/s", "ms_per_step": bf_step,
+                         "stages_ms_per_step": {k_: v / args.steps for k_, v in bf_stage.items()},
+                         "over_fp32_online": bf_value / value,
+                         "schedule": "BF16 y/Phi contraction for sweeps 1..19, FP32 sweep 20"},
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -61,6 +61,9 @@ struct mmsb_ctx {
   // event pairs around whitening SpMM launches (roofline timing)
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spmm_pool;
   std::vector<size_t> spmm_events;
+  // event pairs around the STPM contraction (0) and step (1) launches
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kpool[2];
+  size_t kused[2] = {0, 0};
 
   ~mmsb_ctx();
   // grow-only named workspace buffer of at least `bytes` bytes

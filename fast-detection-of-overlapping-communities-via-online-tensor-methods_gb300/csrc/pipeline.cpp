@@ -21,6 +21,11 @@ mmsb_ctx::~mmsb_ctx() {
     if (pr.first) cudaEventDestroy(pr.first);
     if (pr.second) cudaEventDestroy(pr.second);
   }
+  for (auto& pool : kpool)
+    for (auto& pr : pool) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
   if (fork_ev) cudaEventDestroy(fork_ev);
   if (join_ev) cudaEventDestroy(join_ev);
   if (s2) cudaStreamDestroy(s2);
@@ -488,6 +493,40 @@ struct PartialOut {
   int64_t stride;
 };
 
+// event pair around one STPM kernel launch (which: 0 contraction, 1 step);
+// summed by collect_kernel_times after the STPM loop
+template <typename F>
+static void timed_launch(mmsb_ctx* c, int which, F&& launch) {
+  auto& pool = c->kpool[which];
+  if (c->kused[which] == pool.size()) {
+    std::pair<cudaEvent_t, cudaEvent_t> pr{};
+    ck(cudaEventCreate(&pr.first), "event");
+    ck(cudaEventCreate(&pr.second), "event");
+    pool.push_back(pr);
+  }
+  auto& pr = pool[c->kused[which]++];
+  ck(cudaEventRecord(pr.first, c->s), "event");
+  launch();
+  ck(cudaEventRecord(pr.second, c->s), "event");
+}
+
+static void collect_kernel_times(mmsb_ctx* c) {
+  double* out[2] = {&c->stats.contract_ms, &c->stats.step_ms};
+  int64_t* cnt[2] = {&c->stats.contract_launches, &c->stats.step_launches};
+  for (int w = 0; w < 2; ++w) {
+    double ms = 0.0;
+    for (size_t i = 0; i < c->kused[w]; ++i) {
+      ck(cudaEventSynchronize(c->kpool[w][i].second), "event sync");
+      float t = 0.f;
+      ck(cudaEventElapsedTime(&t, c->kpool[w][i].first, c->kpool[w][i].second), "elapsed");
+      ms += t;
+    }
+    *out[w] += ms;
+    *cnt[w] += (int64_t)c->kused[w];
+    c->kused[w] = 0;
+  }
+}
+
 // per-CTA partial contractions over nodes [begin, begin+count)
 static PartialOut stpm_partials(mmsb_ctx* c, int mode, int q1, int q2, int q3, int64_t begin,
                                 int64_t count, double c0, double c2, bool bf16 = false) {
@@ -517,7 +556,9 @@ static PartialOut stpm_partials(mmsb_ctx* c, int mode, int q1, int q2, int q3, i
   a.c2 = (float)c2;
   a.gpart = gpart;
   a.part_stride = stride;
-  ck(stpm_partial(mode, a, grid, bf16, c->s), "stpm_partial");
+  timed_launch(c, 0, [&]() { ck(stpm_partial(mode, a, grid, bf16, c->s), "stpm_partial"); });
+  const int products = mode == kModePlain ? 3 : mode == kModeAdjoint ? 6 : 3;
+  c->stats.contract_flops += 2.0 * k * k * (double)count * products;
   return PartialOut{gpart, grid / stpm_partial_cluster(), stride};
 }
 
@@ -584,7 +625,7 @@ static void stpm_step(mmsb_ctx* c, int mode, int64_t x0, int64_t cnt, double c0,
   u.count = (double)cnt;
   u.beta = (float)beta;
   u.gscale = (float)gscale;
-  ck(stpm_update(u, c->s), "stpm_step");
+  timed_launch(c, 1, [&]() { ck(stpm_update(u, c->s), "stpm_step"); });
 }
 
 void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
@@ -604,10 +645,13 @@ void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
   } else {
     // orthonormal start: polar factor of a seeded Gaussian matrix
     ck(gaussian_panel(c->phi, k, k, k, c->cfg.seed, 7, s), "phi0");
-    polar_only(c, ns_it);
+    polar_only(c, nullptr);  // (not counted: the statistics cover the minibatch steps)
   }
   const int64_t nx = c->nX;
   c->stats.stpm_steps = 0;
+  c->stats.contract_ms = c->stats.step_ms = c->stats.contract_flops = c->stats.step_flops = 0.0;
+  c->stats.contract_launches = c->stats.step_launches = 0;
+  c->kused[0] = c->kused[1] = 0;
   if (c->cfg.stpm_method == MMSB_STPM_BATCH_POWER) {
     // tensorDecom_alpha0 (Util.cpp:131-184)
     const double inv_x = 1.0 / (double)nx;
@@ -659,11 +703,14 @@ void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
     ck(cudaMemcpyAsync(&nsit, ns_it, sizeof(int), cudaMemcpyDeviceToHost, s), "ns counter");
     ck(cudaStreamSynchronize(s), "sync");
     c->stats.polar_iterations = nsit;
+    // gram + product of every Newton-Schulz iteration and of every online update
+    c->stats.step_flops = 4.0 * (double)k * k * k * (double)(nsit + t);
     // lambda_i = That(phi_i, phi_i, phi_i) over all of X; sign fixed so lambda > 0
     stpm_pass(c, kModePlain, 0, 1, 2, 0, nx, p0 / nx, p1, p2 / nx, 1.0, G, nullptr);
     ck(stpm_tensor_values(k, c->phi, G, c->lambda, s), "lambda");
   }
   check_flags(c, "stpm");
+  collect_kernel_times(c);
   c->have_phi = true;
 }
 

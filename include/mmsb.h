@@ -118,6 +118,16 @@ typedef struct mmsb_stats {
   double stpm_last_error;  /* batch power: last ||Phi - Phi_old||_F */
   int64_t kernel_launches; /* launches of this library's kernels by the last call */
   int64_t polar_iterations; /* Newton-Schulz iterations summed over the STPM steps */
+  /* STPM kernels of the last mmsb_stpm, timed with CUDA events around each
+   * launch; flops are algorithmic (k, not the padded tile size):
+   * contraction 2 k^2 per node per Z and per G product, step 4 k^3 per
+   * Newton-Schulz iteration and per online update */
+  double contract_ms;
+  double contract_flops;
+  int64_t contract_launches;
+  double step_ms;
+  double step_flops;
+  int64_t step_launches;
 } mmsb_stats;
 
 typedef struct mmsb_ctx mmsb_ctx;
