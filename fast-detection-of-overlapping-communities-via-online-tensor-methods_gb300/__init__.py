@@ -87,6 +87,23 @@ class Stats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class BatchStats(ctypes.Structure):
+    _fields_ = [("total_ms", ctypes.c_double), ("stpm_end_ms", ctypes.c_double),
+                ("wall_ms", ctypes.c_double), ("latency_p50_ms", ctypes.c_double),
+                ("latency_p99_ms", ctypes.c_double), ("latency_max_ms", ctypes.c_double),
+                ("rounds", ctypes.c_int64), ("batched_launches", ctypes.c_int64),
+                ("graph_replayed", ctypes.c_int32), ("buckets", ctypes.c_int32),
+                ("bucket_kp", ctypes.c_int32 * 8), ("bucket_ctas", ctypes.c_int32 * 8),
+                ("bucket_graphs", ctypes.c_int32 * 8)]
+
+    def as_dict(self):
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v)[:self.buckets] if name.startswith("bucket_") else v
+        return d
+
+
 class GenParams(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("k", ctypes.c_int32), ("alpha0", ctypes.c_double),
                 ("p_in", ctypes.c_double), ("p_out", ctypes.c_double),
@@ -132,6 +149,19 @@ _SIGS = {
     "mmsb_op_spmm_t_noalloc": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64,
                                               ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_float,
                                               _P, _P]),
+    "mmsb_batch_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_int32,
+                                         ctypes.POINTER(ctypes.c_int32), _D,
+                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(_P)]),
+    "mmsb_batch_destroy": (None, [_P]),
+    "mmsb_batch_upload": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(Csr)]),
+    "mmsb_batch_run": (ctypes.c_int, [_P]),
+    "mmsb_batch_run_sequential": (ctypes.c_int, [_P]),
+    "mmsb_batch_count": (ctypes.c_int32, [_P]),
+    "mmsb_batch_set_contract_ctas": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "mmsb_batch_graph": (_P, [_P, ctypes.c_int32]),
+    "mmsb_batch_latencies": (ctypes.c_int, [_P, _D]),
+    "mmsb_batch_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(BatchStats)]),
+    "mmsb_batch_last_error": (ctypes.c_char_p, [_P]),
     "mmsb_generate": (ctypes.c_int, [ctypes.POINTER(GenParams), ctypes.POINTER(_P)]),
     "mmsb_host_graph_free": (None, [_P]),
     "mmsb_host_graph_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64),
@@ -324,9 +354,9 @@ class Pipeline:
         self.parts = None
 
     def close(self):
-        if getattr(self, "_h", None):
+        if getattr(self, "_h", None) and not getattr(self, "_borrowed", False):
             lib().mmsb_destroy(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:
@@ -466,6 +496,89 @@ class Pipeline:
 
 
 # ---- reference-named convenience wrappers ----------------------------------------
+
+class Batch:
+    """Many independent graphs solved together (mmsb_batch_*): per-graph k and
+    alpha0, every other setting from the keyword arguments."""
+
+    def __init__(self, ks, alpha0s=None, minibatches=None, **kw):
+        self.cfg = default_config(**kw)
+        ks = np.ascontiguousarray(ks, dtype=np.int32)
+        a0 = None if alpha0s is None else np.ascontiguousarray(alpha0s, dtype=np.float64)
+        mbs = None if minibatches is None else np.ascontiguousarray(minibatches, dtype=np.int32)
+        h = _P()
+        i32 = ctypes.POINTER(ctypes.c_int32)
+        st = lib().mmsb_batch_create(ctypes.byref(self.cfg), len(ks), ks.ctypes.data_as(i32),
+                                     _dptr(a0), None if mbs is None else mbs.ctypes.data_as(i32),
+                                     ctypes.byref(h))
+        _check(st)
+        self._h = h
+        self.ks = ks
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mmsb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __len__(self):
+        return len(self.ks)
+
+    def _ck(self, st):
+        if st != 0:
+            msg = lib().mmsb_batch_last_error(self._h).decode()
+            raise MmsbError(st, msg)
+
+    def upload(self, i, graph: Graph):
+        arr = (Csr * 5)(*[b.ctype() for b in graph.blocks])
+        self._keep[i] = graph
+        self._ck(lib().mmsb_batch_upload(self._h, i, arr))
+        return self
+
+    def set_contract_ctas(self, ctas):
+        self._ck(lib().mmsb_batch_set_contract_ctas(self._h, ctas))
+        return self
+
+    def run(self):
+        self._ck(lib().mmsb_batch_run(self._h))
+        return self
+
+    def run_sequential(self):
+        self._ck(lib().mmsb_batch_run_sequential(self._h))
+        return self
+
+    def stats(self):
+        s = BatchStats()
+        self._ck(lib().mmsb_batch_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def latencies(self):
+        out = np.zeros(len(self.ks))
+        self._ck(lib().mmsb_batch_latencies(self._h, _dptr(out)))
+        return out
+
+    def graph(self, i):
+        """Results view of graph i (a Pipeline sharing the batch's context)."""
+        v = Pipeline.__new__(Pipeline)
+        v._h = lib().mmsb_batch_graph(self._h, i)
+        v.k = int(self.ks[i])
+        v.parts = self._keep[i].parts
+        v.cfg = self.cfg
+        v._borrowed = True
+        return v
+
 
 def second_whiten(graph: Graph, k, alpha0, sketches=None, **cfg):
     """second_whiten (Util.cpp:38-127) on the GPU; returns W, Z parts and means."""

@@ -80,7 +80,7 @@ cudaError_t mgs_cols(int m, int p, const double* P, int ldp, double* Q, int ldq,
 cudaError_t oa_correction(int n, const double* A, const double* XtX, const double* S, double* E,
                           double* lam, double* delta_state, cudaStream_t s);
 cudaError_t sort_eigen(int n, const double* lam, const double* X, double* evals, double* evecs,
-                       cudaStream_t s);
+                       unsigned* flags, cudaStream_t s);
 cudaError_t panel_set_col(float* P, int ld, int64_t rows, int col, const double* v,
                           cudaStream_t s);
 cudaError_t panel_copy(const float* src, int lds, int64_t rows, int q, float* dst, int ldd,

@@ -366,10 +366,16 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __res
     if (lane == 0) nrm2[i] = s;
   }
   __syncthreads();
-  // descending order by rank (ties broken by index)
+  // descending order by rank (ties broken by index); NaN ranks below
+  // everything, so the ranks always form a permutation, and is reported
   for (int i = tid; i < p; i += nt) {
+    const float ki = isnan(nrm2[i]) ? -INFINITY : nrm2[i];
+    if (!isfinite(nrm2[i])) atomicOr(flags, kFlagNonFinite);
     int rank = 0;
-    for (int j = 0; j < p; ++j) rank += (nrm2[j] > nrm2[i]) || (nrm2[j] == nrm2[i] && j < i);
+    for (int j = 0; j < p; ++j) {
+      const float kj = isnan(nrm2[j]) ? -INFINITY : nrm2[j];
+      rank += (kj > ki) || (kj == ki && j < i);
+    }
     order[rank] = i;
   }
   __syncthreads();
@@ -379,6 +385,60 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __res
     const float inv = s > 0.f ? rsqrtf(s) : 0.f;
     if (lane == 0) evals[r] = (double)s;
     for (int t = lane; t < p; t += 32) evecs[(int64_t)r * p + t] = (double)(X[(int64_t)i * p + t] * inv);
+  }
+  // Exactly zero columns (null directions of a rank-deficient factor, ranked
+  // last) carry no direction: complete the basis so that the refinement
+  // starts from an orthonormal matrix.  Column r becomes e_t minus its
+  // projection on columns 0..r-1 (twice), for the t with the smallest
+  // weight sum_c X_tc^2 (the unit vector farthest from their span).
+  __shared__ double wsm[512], vsm[512];
+  __shared__ int s_t;
+  __syncthreads();  // evecs (global) complete
+  for (int r = 0; r < p; ++r) {
+    if (nrm2[order[r]] > 0.f) continue;  // uniform: every thread reads the same value
+    for (int t = tid; t < p; t += nt) {
+      double w = 0.0;
+      for (int c = 0; c < r; ++c) {
+        const double x = evecs[(int64_t)c * p + t];
+        w = fma(x, x, w);
+      }
+      wsm[t] = w;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      int best = 0;
+      for (int t = 1; t < p; ++t)
+        if (wsm[t] < wsm[best]) best = t;
+      s_t = best;
+    }
+    __syncthreads();
+    const int tb = s_t;
+    for (int u = tid; u < p; u += nt) {
+      double v = u == tb ? 1.0 : 0.0;
+      for (int c = 0; c < r; ++c) v -= evecs[(int64_t)c * p + u] * evecs[(int64_t)c * p + tb];
+      vsm[u] = v;
+    }
+    __syncthreads();
+    for (int c = tid; c < r; c += nt) {  // second projection: wsm[c] = X_c . v
+      double d = 0.0;
+      for (int u = 0; u < p; ++u) d = fma(evecs[(int64_t)c * p + u], vsm[u], d);
+      wsm[c] = d;
+    }
+    __syncthreads();
+    for (int u = tid; u < p; u += nt) {
+      double v = vsm[u];
+      for (int c = 0; c < r; ++c) v -= wsm[c] * evecs[(int64_t)c * p + u];
+      vsm[u] = v;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double nn = 0.0;
+      for (int u = 0; u < p; ++u) nn = fma(vsm[u], vsm[u], nn);
+      wsm[0] = nn > 0.0 ? 1.0 / sqrt(nn) : 0.0;
+    }
+    __syncthreads();
+    for (int u = tid; u < p; u += nt) evecs[(int64_t)r * p + u] = vsm[u] * wsm[0];
+    __syncthreads();
   }
 }
 
@@ -485,8 +545,8 @@ __global__ void __launch_bounds__(1024) oa_correction_kernel(int n, const double
   __shared__ double delta;
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int i = tid; i < n; i += nt) {
-    const double rii = 1.0 - XtX[(int64_t)i * n + i];
-    lam[i] = S[(int64_t)i * n + i] / (1.0 - rii);
+    const double xx = XtX[(int64_t)i * n + i];  // = 1 - R_ii
+    lam[i] = xx > 0.0 ? S[(int64_t)i * n + i] / xx : 0.0;
   }
   __syncthreads();
   // spectral-norm bounds: ||M||_2 <= max column abs-sum for symmetric M,
@@ -542,12 +602,20 @@ __global__ void __launch_bounds__(1024) oa_correction_kernel(int n, const double
 }
 
 // columns of X reordered by descending lam (stable on ties by index)
+// (descending, ties by index; NaN ranks last so the ranks always form a
+// permutation, and is reported through the flag word)
 __global__ void sort_eigen_kernel(int n, const double* __restrict__ lam, const double* __restrict__ X,
-                                  double* __restrict__ evals, double* __restrict__ evecs) {
+                                  double* __restrict__ evals, double* __restrict__ evecs,
+                                  unsigned* flags) {
   extern __shared__ int order[];
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double ki = isnan(lam[i]) ? -INFINITY : lam[i];
+    if (!isfinite(lam[i]) && flags) atomicOr(flags, kFlagNonFinite);
     int rank = 0;
-    for (int j = 0; j < n; ++j) rank += (lam[j] > lam[i]) || (lam[j] == lam[i] && j < i);
+    for (int j = 0; j < n; ++j) {
+      const double kj = isnan(lam[j]) ? -INFINITY : lam[j];
+      rank += (kj > ki) || (kj == ki && j < i);
+    }
     order[rank] = i;
   }
   __syncthreads();
@@ -825,8 +893,8 @@ cudaError_t oa_correction(int n, const double* A, const double* XtX, const doubl
 }
 
 cudaError_t sort_eigen(int n, const double* lam, const double* X, double* evals, double* evecs,
-                       cudaStream_t s) {
-  sort_eigen_kernel<<<1, 1024, sizeof(int) * n, s>>>(n, lam, X, evals, evecs);
+                       unsigned* flags, cudaStream_t s) {
+  sort_eigen_kernel<<<1, 1024, sizeof(int) * n, s>>>(n, lam, X, evals, evecs, flags);
   ++g_launch_count;
   return cudaGetLastError();
 }

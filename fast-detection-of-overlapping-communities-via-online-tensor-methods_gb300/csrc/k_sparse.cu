@@ -137,7 +137,8 @@ __global__ void scatter_kernel(const int64_t* __restrict__ rp, const int32_t* __
 }
 
 // Sorts every row segment of the transposed CSR by column (rank sort, one
-// warp per segment; entries within a segment are distinct).
+// warp per segment; equal columns, from duplicate entries of the input, keep
+// their input order, so the ranks always form a permutation).
 __global__ void segment_sort_kernel(const int64_t* __restrict__ rpT, int64_t n_rowsT,
                                     const int32_t* __restrict__ in_c, const float* __restrict__ in_v,
                                     int32_t* __restrict__ out_c, float* __restrict__ out_v) {
@@ -149,7 +150,10 @@ __global__ void segment_sort_kernel(const int64_t* __restrict__ rpT, int64_t n_r
   for (int64_t i = lane; i < L; i += 32) {
     const int32_t x = in_c[b + i];
     int64_t rank = 0;
-    for (int64_t j = 0; j < L; ++j) rank += in_c[b + j] < x;
+    for (int64_t j = 0; j < L; ++j) {
+      const int32_t y = in_c[b + j];
+      rank += (y < x) || (y == x && j < i);
+    }
     out_c[b + rank] = x;
     if (out_v) out_v[b + rank] = in_v[b + i];
   }

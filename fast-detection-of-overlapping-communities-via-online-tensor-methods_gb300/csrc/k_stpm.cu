@@ -260,7 +260,7 @@ __device__ __forceinline__ bool step_product(const float* __restrict__ X, const 
 }
 
 template <int KP, int CL>
-__global__ void __launch_bounds__(512, 1) stpm_step_kernel(StpmUpdateArgs a) {
+__device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   using S = StepSmem<KP, CL>;
   constexpr int NB = S::NB, XLD = S::XLD;
   static_assert(NB == 8 || NB == 16, "column block of 8 or 16");
@@ -276,7 +276,6 @@ __global__ void __launch_bounds__(512, 1) stpm_step_kernel(StpmUpdateArgs a) {
   float* mv = part + S::TILES * 128;  // m1, m2, m3 (+ pad) for this block
   float* red = mv + 4 * KP;       // initial statistics of the CL ranks (3 x CL)
   float* dcol = red + 3 * CL;     // 3 * NB d-sums (online step)
-  float* colabs = dcol + 3 * NB;  // NB column abs sums (+ NB spare)
   __shared__ float s_abs, s_err, s_fro;
   __shared__ __align__(8) uint64_t s_full[2];  // "next iterate arrived" for Xa / Xb
   const int k = a.k;
@@ -446,15 +445,12 @@ __global__ void __launch_bounds__(512, 1) stpm_step_kernel(StpmUpdateArgs a) {
   // gram_stats: A_blk = X^T X[:, blk] with its statistics (max column abs
   // sum, max |A - I|, ||A - I||_F^2 over the block) in s_abs, s_err, s_fro,
   // and Ab = d0 I + d1 A_blk.
+  // (per-tile partial statistics are summed by one thread in a fixed order,
+  // so the result does not depend on warp timing)
+  __shared__ float colpart[S::MT * NB], errpart[S::TILES], fropart[S::TILES];
   auto gram_stats = [&](float d0, float d1) {
-    if (tid < NB) colabs[tid] = 0.f;
-    if (tid == 0) {
-      s_err = 0.f;
-      s_fro = 0.f;
-    }
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     int m0, n0;
-    // (step_product's barrier also orders the resets above before the atomics)
     const bool own = step_product<KP, CL, kProdGram>(X, nullptr, c0, part, acc, m0, n0);
     if (own) {
       float er = 0.f, fr = 0.f, ca[2] = {0.f, 0.f};
@@ -481,20 +477,31 @@ __global__ void __launch_bounds__(512, 1) stpm_step_kernel(StpmUpdateArgs a) {
         er = fmaxf(er, __shfl_xor_sync(0xffffffffu, er, off));
         fr += __shfl_xor_sync(0xffffffffu, fr, off);
       }
+      const int mt = m0 / 16, tile = (tid >> 5) % S::TILES;
       if (g == 0) {
-        atomicAdd(&colabs[n0 + 2 * t4], ca[0]);
-        atomicAdd(&colabs[n0 + 2 * t4 + 1], ca[1]);
+        colpart[mt * NB + n0 + 2 * t4] = ca[0];
+        colpart[mt * NB + n0 + 2 * t4 + 1] = ca[1];
       }
       if (lane == 0) {
-        atomicMax(reinterpret_cast<int*>(&s_err), __float_as_int(er));
-        atomicAdd(&s_fro, fr);
+        errpart[tile] = er;
+        fropart[tile] = fr;
       }
     }
     __syncthreads();
     if (tid == 0) {
-      float m = 0.f;
-      for (int jb = 0; jb < NB; ++jb) m = fmaxf(m, colabs[jb]);
+      float m = 0.f, e = 0.f, f = 0.f;
+      for (int jb = 0; jb < NB; ++jb) {
+        float cs = 0.f;
+        for (int mt = 0; mt < S::MT; ++mt) cs += colpart[mt * NB + jb];
+        m = fmaxf(m, cs);
+      }
+      for (int t = 0; t < S::TILES; ++t) {
+        e = fmaxf(e, errpart[t]);
+        f += fropart[t];
+      }
       s_abs = m;
+      s_err = e;
+      s_fro = f;
     }
     __syncthreads();
   };
@@ -590,6 +597,20 @@ __global__ void __launch_bounds__(512, 1) stpm_step_kernel(StpmUpdateArgs a) {
   if (timed_out) __nanosleep(100000);  // let copies a stalled exchange left in flight land
 }
 
+template <int KP, int CL>
+__global__ void __launch_bounds__(512, 1) stpm_step_kernel(StpmUpdateArgs a) {
+  step_body<KP, CL>(a);
+}
+
+// one cluster per graph: blockIdx.y selects the graph's arguments; graphs
+// with no update in this round (active == 0) leave at once
+template <int KP, int CL>
+__global__ void __launch_bounds__(512, 1) stpm_step_batched(const StpmUpdateArgs* __restrict__ args) {
+  const StpmUpdateArgs a = args[blockIdx.y];
+  if (!a.active) return;
+  step_body<KP, CL>(a);
+}
+
 // ---- partial contractions on the tensor cores -----------------------------------
 //
 // Per tile of TM nodes, with Phi resident in shared memory:
@@ -653,7 +674,7 @@ __device__ __forceinline__ void split_tf32(float v, uint32_t& hi, uint32_t& lo) 
 }
 
 template <int KP, int MODE, bool BF>
-__global__ void __launch_bounds__(256) stpm_contract_kernel(StpmPartialArgs a) {
+__device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblocks) {
   using Cfg = Contract<KP, MODE, BF>;
   using T = typename Cfg::T;
   constexpr int TM = Cfg::TM, NZ = Cfg::NZ, NC = Cfg::NC, PLD = Cfg::PLD, LDY = Cfg::LDY,
@@ -717,7 +738,7 @@ __global__ void __launch_bounds__(256) stpm_contract_kernel(StpmPartialArgs a) {
   const float cc0 = a.c0, cc2 = a.c2;
 
   const int64_t ntiles = ceil_div_dev(a.count, TM);
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += nblocks) {
     const int64_t x0 = a.begin + tile * TM;
     const int64_t left = a.begin + a.count - x0;
     const int nvalid = left < TM ? (int)left : TM;
@@ -959,6 +980,20 @@ __global__ void __launch_bounds__(256) stpm_contract_kernel(StpmPartialArgs a) {
   cluster.sync();  // keep shared memory alive until every remote read is done
 }
 
+template <int KP, int MODE, bool BF>
+__global__ void __launch_bounds__(256) stpm_contract_kernel(StpmPartialArgs a) {
+  contract_body<KP, MODE, BF>(a, gridDim.x);
+}
+
+// blockIdx.y selects the graph; its first a.nblocks CTAs (a multiple of the
+// cluster size) work, the rest and graphs without nodes this round leave
+template <int KP, int MODE, bool BF>
+__global__ void __launch_bounds__(256) stpm_contract_batched(const StpmPartialArgs* __restrict__ args) {
+  const StpmPartialArgs a = args[blockIdx.y];
+  if ((int)blockIdx.x >= a.nblocks || a.count <= 0) return;
+  contract_body<KP, MODE, BF>(a, a.nblocks);
+}
+
 // batch power: Phi_new = G (already includes the shift terms), lambda = ||col||^3,
 // column normalisation, error = ||Phi_new - Phi_old||_F
 __global__ void __launch_bounds__(1024) batch_update_kernel(int k, float* __restrict__ phi,
@@ -1055,6 +1090,48 @@ cudaError_t launch_partial_p(int mode, int KP, const StpmPartialArgs& a, int gri
   }
 }
 
+template <int KP, int MODE, bool BF>
+cudaError_t launch_partial_batched_t(const StpmPartialArgs* args, int graphs, int grid,
+                                     cudaStream_t s) {
+  const size_t smem = Contract<KP, MODE, BF>::smem;
+  static bool set = false;
+  if (!set) {
+    MMSB_CUDA_TRY(cudaFuncSetAttribute(stpm_contract_batched<KP, MODE, BF>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    set = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid, (unsigned)graphs, 1);
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kPartialCluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MMSB_CUDA_TRY(cudaLaunchKernelEx(&cfg, stpm_contract_batched<KP, MODE, BF>, args));
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+template <int MODE, bool BF>
+cudaError_t launch_partial_batched_m(int KP, const StpmPartialArgs* args, int graphs, int grid,
+                                     cudaStream_t s) {
+  switch (KP) {
+    case 32: return launch_partial_batched_t<32, MODE, BF>(args, graphs, grid, s);
+    case 48: return launch_partial_batched_t<48, MODE, BF>(args, graphs, grid, s);
+    case 64: return launch_partial_batched_t<64, MODE, BF>(args, graphs, grid, s);
+    case 80: return launch_partial_batched_t<80, MODE, BF>(args, graphs, grid, s);
+    case 96: return launch_partial_batched_t<96, MODE, BF>(args, graphs, grid, s);
+    case 112: return launch_partial_batched_t<112, MODE, BF>(args, graphs, grid, s);
+    case 128: return launch_partial_batched_t<128, MODE, BF>(args, graphs, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 template <int KP, int CL>
 cudaError_t launch_step_t(const StpmUpdateArgs& a, cudaStream_t s) {
   const size_t smem = sizeof(float) * StepSmem<KP, CL>::floats;
@@ -1102,6 +1179,51 @@ cudaError_t launch_step_k(const StpmUpdateArgs& a, cudaStream_t s) {
   return launch_step_t<KP, KP / 16>(a, s);
 }
 
+template <int KP, int CL>
+cudaError_t launch_step_batched_t(const StpmUpdateArgs* args, int graphs, cudaStream_t s) {
+  const size_t smem = sizeof(float) * StepSmem<KP, CL>::floats;
+  static bool set = false;
+  if (!set) {
+    MMSB_CUDA_TRY(cudaFuncSetAttribute(stpm_step_batched<KP, CL>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (CL > 8)
+      MMSB_CUDA_TRY(cudaFuncSetAttribute(stpm_step_batched<KP, CL>,
+                                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    set = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CL, (unsigned)graphs, 1);
+  cfg.blockDim = dim3(512, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MMSB_CUDA_TRY(cudaLaunchKernelEx(&cfg, stpm_step_batched<KP, CL>, args));
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+template <int KP>
+cudaError_t launch_step_batched_k(const StpmUpdateArgs* args, int graphs, cudaStream_t s) {
+  static int wide = -1;
+  if (wide != 0) {
+    cudaError_t e = launch_step_batched_t<KP, KP / 8>(args, graphs, s);
+    if (e == cudaSuccess) {
+      wide = 1;
+      return e;
+    }
+    if (wide == 1) return e;
+    cudaGetLastError();
+    wide = 0;
+  }
+  return launch_step_batched_t<KP, KP / 16>(args, graphs, s);
+}
+
 }  // namespace
 
 int stpm_partial_cluster() { return kPartialCluster; }
@@ -1145,6 +1267,35 @@ cudaError_t stpm_update(const StpmUpdateArgs& a, cudaStream_t s) {
 }
 
 int stpm_step_kp(int k) { return k <= 32 ? 32 : (int)round_up(k, 16); }
+
+cudaError_t stpm_partial_batched(int mode, int KP, const StpmPartialArgs* args, int graphs,
+                                 int grid, bool bf16, cudaStream_t s) {
+  if (KP > 128 || grid % kPartialCluster != 0 || graphs < 1 || graphs > 65535)
+    return cudaErrorInvalidValue;
+  switch (mode) {
+    case kModePlain:
+      return bf16 ? launch_partial_batched_m<kModePlain, true>(KP, args, graphs, grid, s)
+                  : launch_partial_batched_m<kModePlain, false>(KP, args, graphs, grid, s);
+    case kModeAdjoint:
+      return bf16 ? launch_partial_batched_m<kModeAdjoint, true>(KP, args, graphs, grid, s)
+                  : launch_partial_batched_m<kModeAdjoint, false>(KP, args, graphs, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t stpm_update_batched(int KP, const StpmUpdateArgs* args, int graphs, cudaStream_t s) {
+  if (graphs < 1 || graphs > 65535) return cudaErrorInvalidValue;
+  switch (KP) {
+    case 32: return launch_step_batched_k<32>(args, graphs, s);
+    case 48: return launch_step_batched_k<48>(args, graphs, s);
+    case 64: return launch_step_batched_k<64>(args, graphs, s);
+    case 80: return launch_step_batched_k<80>(args, graphs, s);
+    case 96: return launch_step_batched_k<96>(args, graphs, s);
+    case 112: return launch_step_batched_k<112>(args, graphs, s);
+    case 128: return launch_step_batched_k<128>(args, graphs, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
 
 cudaError_t stpm_batch_update(int k, float* phi, const float* G, double* lambda, double* err,
                               cudaStream_t s) {

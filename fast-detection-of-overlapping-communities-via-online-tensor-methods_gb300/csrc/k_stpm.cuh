@@ -34,6 +34,7 @@ struct StpmPartialArgs {
   float c0, c2;          // plain: C = c0 Z1Z2 + c2(Z1 m2 + m1 Z2); adjoint/loss: p0, p2
   float* gpart;          // [grid][part_stride]: k*k partial G, then 3k d-sums (+1 loss)
   int64_t part_stride;
+  int nblocks;           // batched launches: CTAs of this graph (multiple of the cluster size)
 };
 
 struct StpmReduceArgs {
@@ -75,6 +76,7 @@ struct StpmUpdateArgs {
   float ns_tol;
   unsigned* flags;
   int* ns_iters;         // accumulates Newton-Schulz iterations
+  int active;            // batched launches: 0 = no update for this graph in this round
 };
 
 int stpm_kp(int k);
@@ -87,6 +89,13 @@ int stpm_partial_cluster();
 // otherwise FP32 operands through the 3xTF32 split
 cudaError_t stpm_partial(int mode, const StpmPartialArgs& a, int grid, bool bf16, cudaStream_t s);
 cudaError_t stpm_reduce(const StpmReduceArgs& a, cudaStream_t s);
+// batched forms over `graphs` graphs of one padded size KP: args are device
+// arrays indexed by graph; the contraction runs `grid` CTAs per graph (a
+// multiple of stpm_partial_cluster(); each graph uses its args.nblocks of
+// them), the step one cluster per graph (args.active == 0 skips a graph)
+cudaError_t stpm_partial_batched(int mode, int KP, const StpmPartialArgs* args, int graphs,
+                                 int grid, bool bf16, cudaStream_t s);
+cudaError_t stpm_update_batched(int KP, const StpmUpdateArgs* args, int graphs, cudaStream_t s);
 cudaError_t stpm_update(const StpmUpdateArgs& a, cudaStream_t s);
 cudaError_t stpm_batch_update(int k, float* phi, const float* G, double* lambda, double* err,
                               cudaStream_t s);

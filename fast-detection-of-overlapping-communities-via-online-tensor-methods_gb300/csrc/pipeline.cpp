@@ -158,7 +158,7 @@ void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A
     ck(dgemm_small(false, false, n, n, n, 1.0, X, n, E, n, 1.0, X2, n, s), "X + X E");
     std::swap(X, X2);
   }
-  ck(sort_eigen(n, lam, X, evals, V, s), "sort");
+  ck(sort_eigen(n, lam, X, evals, V, c->flags, s), "sort");
 }
 
 namespace {
@@ -261,6 +261,13 @@ void pipeline_upload(mmsb_ctx* c, const mmsb_csr* blocks) {
     }
     if (m.n_rows > 0 && (m.row_ptr[0] != 0 || m.row_ptr[m.n_rows] != m.nnz))
       throw MmsbError(MMSB_ERR_INVALID_ARG, "block " + std::to_string(b) + ": row_ptr/nnz mismatch");
+    // the device transposes and SpMMs index with these: reject bad input here
+    for (int64_t r = 0; r < m.n_rows; ++r)
+      if (m.row_ptr[r + 1] < m.row_ptr[r])
+        throw MmsbError(MMSB_ERR_INVALID_ARG, "block " + std::to_string(b) + ": decreasing row_ptr");
+    for (int64_t j = 0; j < m.nnz; ++j)
+      if (m.col_idx[j] < 0 || m.col_idx[j] >= m.n_cols)
+        throw MmsbError(MMSB_ERR_INVALID_ARG, "block " + std::to_string(b) + ": column index out of range");
     if (m.n_cols > INT32_MAX) throw MmsbError(MMSB_ERR_INVALID_ARG, "too many columns");
   }
   c->free_graph();
@@ -356,7 +363,7 @@ void collect_spmm_time(mmsb_ctx* c) {
   c->spmm_events.clear();
 }
 
-void pipeline_whiten(mmsb_ctx* c, const double* const* sketches) {
+void pipeline_whiten(mmsb_ctx* c, const double* const* sketches, bool finish) {
   if (!c->have_graph) throw MmsbError(MMSB_ERR_STATE, "whiten before upload_graph");
   c->spmm_events.clear();
   const int k = c->k, p = c->p, ldp = c->ldp, ldk = c->ldk;
@@ -481,6 +488,10 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches) {
   ck(panel_scale_cols(c->W, ldk, c->nA, k, Linv_sqrt, s), "W scale");
   c->have_white = true;
   pipeline_ydata(c);
+  if (finish) pipeline_whiten_finish(c);
+}
+
+void pipeline_whiten_finish(mmsb_ctx* c) {
   check_flags(c, "whitening");
   collect_spmm_time(c);
 }
@@ -527,13 +538,10 @@ static void collect_kernel_times(mmsb_ctx* c) {
   }
 }
 
-// per-CTA partial contractions over nodes [begin, begin+count)
-static PartialOut stpm_partials(mmsb_ctx* c, int mode, int q1, int q2, int q3, int64_t begin,
-                                int64_t count, double c0, double c2, bool bf16 = false) {
+StpmPartialArgs stpm_partial_args(mmsb_ctx* c, int q1, int q2, int q3, int64_t begin,
+                                  int64_t count, double c0, double c2, bool bf16, float* gpart,
+                                  int64_t stride, int nblocks) {
   const int k = c->k;
-  const int grid = stpm_partial_grid(count, bf16);
-  const int64_t stride = (int64_t)k * k + 3 * k + 4;
-  float* gpart = c->tbuf<float>("gpart", (size_t)grid * stride);
   StpmPartialArgs a{};
   a.y1 = c->y[q1];
   a.y2 = c->y[q2];
@@ -556,6 +564,18 @@ static PartialOut stpm_partials(mmsb_ctx* c, int mode, int q1, int q2, int q3, i
   a.c2 = (float)c2;
   a.gpart = gpart;
   a.part_stride = stride;
+  a.nblocks = nblocks;
+  return a;
+}
+
+// per-CTA partial contractions over nodes [begin, begin+count)
+static PartialOut stpm_partials(mmsb_ctx* c, int mode, int q1, int q2, int q3, int64_t begin,
+                                int64_t count, double c0, double c2, bool bf16 = false) {
+  const int k = c->k;
+  const int grid = stpm_partial_grid(count, bf16);
+  const int64_t stride = (int64_t)k * k + 3 * k + 4;
+  float* gpart = c->tbuf<float>("gpart", (size_t)grid * stride);
+  StpmPartialArgs a = stpm_partial_args(c, q1, q2, q3, begin, count, c0, c2, bf16, gpart, stride, grid);
   timed_launch(c, 0, [&]() { ck(stpm_partial(mode, a, grid, bf16, c->s), "stpm_partial"); });
   const int products = mode == kModePlain ? 3 : mode == kModeAdjoint ? 6 : 3;
   c->stats.contract_flops += 2.0 * k * k * (double)count * products;
@@ -596,6 +616,7 @@ static StpmUpdateArgs step_args(mmsb_ctx* c, int step_mode, int* ns_iters) {
   u.ns_tol = 2e-6f;  // early exit; the 1e-3 + one-iteration rule ends typical steps
   u.flags = c->flags;
   u.ns_iters = ns_iters;
+  u.active = 1;
   return u;
 }
 
@@ -604,38 +625,82 @@ static void polar_only(mmsb_ctx* c, int* ns_iters) {
   ck(stpm_update(u, c->s), "stpm_polar");
 }
 
-// one minibatch update: partial contractions, then the fused reduction +
-// Phi - beta (3 theta O - gscale G) + polar orthonormalisation on one cluster
-static void stpm_step(mmsb_ctx* c, int mode, int64_t x0, int64_t cnt, double c0, double c1,
-                      double c2, double scale, double beta, double gscale, int* ns_iters,
-                      bool bf16) {
+StpmUpdateArgs stpm_online_update_args(mmsb_ctx* c, const OnlineRound& rd, float* gpart,
+                                       int64_t stride, int nparts) {
   const int k = c->k;
-  PartialOut po = stpm_partials(c, mode, 0, 1, 2, x0, cnt, c0, c2, bf16);
-  StpmUpdateArgs u = step_args(c, kStepOnline, ns_iters);
-  u.mode = mode;
-  u.gpart = po.gpart;
-  u.part_stride = po.stride;
-  u.nparts = po.grid;
+  StpmUpdateArgs u = step_args(c, kStepOnline, c->tbuf<int>("ns_iters", 4));
+  u.mode = rd.mode;
+  u.gpart = gpart;
+  u.part_stride = stride;
+  u.nparts = nparts;
   u.mu1 = c->ymu;
   u.mu2 = c->ymu + k;
   u.mu3 = c->ymu + 2 * k;
-  u.c1 = c1;
-  u.c2 = c2;
-  u.scale = scale;
-  u.count = (double)cnt;
-  u.beta = (float)beta;
-  u.gscale = (float)gscale;
+  u.c1 = rd.c1;
+  u.c2 = rd.c2;
+  u.scale = rd.scale;
+  u.count = (double)rd.cnt;
+  u.beta = (float)rd.beta;
+  u.gscale = (float)rd.gscale;
+  return u;
+}
+
+// minibatch schedule of the online / adjoint methods: update r of
+// sweeps x ceil(n_X / b) covers nodes [x0, x0 + cnt) of sweep r / steps with
+// beta_r = lr0 / (1 + r); the BF16 form's last sweep is FP32
+bool stpm_online_round(const mmsb_ctx* c, int64_t r, OnlineRound* out) {
+  const int64_t nx = c->nX;
+  const int64_t b = std::max<int64_t>(1, std::min<int64_t>(c->cfg.minibatch, nx));
+  const int64_t per = (nx + b - 1) / b;
+  if (r < 0 || r >= per * c->cfg.sweeps) return false;
+  const double a0 = c->cfg.alpha0;
+  const double p0 = (a0 + 1.0) * (a0 + 2.0) / 2.0, p1 = a0 * a0, p2 = -a0 * (a0 + 1.0) / 2.0;
+  const int64_t sw = r / per;
+  out->x0 = (r % per) * b;
+  out->cnt = std::min<int64_t>(b, nx - out->x0);
+  out->beta = c->cfg.lr0 / (1.0 + (double)r);
+  out->bf16 = c->cfg.precision == MMSB_PREC_BF16 && sw + 1 < c->cfg.sweeps;
+  if (c->cfg.stpm_method == MMSB_STPM_ADJOINT) {
+    // dT (column i = d That_i / d phi_i); step = 3 theta O - dT
+    out->mode = kModeAdjoint;
+    out->c0 = p0;
+    out->c1 = p1;
+    out->c2 = p2;
+    out->scale = 1.0 / (double)out->cnt;
+    out->gscale = 1.0;
+  } else {
+    // G = mean of The_second_term; step = 3 theta O - 3 G
+    out->mode = kModePlain;
+    out->c0 = p0 / (double)out->cnt;
+    out->c1 = p1;
+    out->c2 = p2 / (double)out->cnt;
+    out->scale = 1.0;
+    out->gscale = 3.0;
+  }
+  return true;
+}
+
+int64_t stpm_online_rounds(const mmsb_ctx* c) {
+  const int64_t nx = c->nX;
+  const int64_t b = std::max<int64_t>(1, std::min<int64_t>(c->cfg.minibatch, nx));
+  return ((nx + b - 1) / b) * c->cfg.sweeps;
+}
+
+// one minibatch update: partial contractions, then the fused reduction +
+// Phi - beta (3 theta O - gscale G) + polar orthonormalisation on one cluster
+static void stpm_step(mmsb_ctx* c, const OnlineRound& rd) {
+  PartialOut po = stpm_partials(c, rd.mode, 0, 1, 2, rd.x0, rd.cnt, rd.c0, rd.c2, rd.bf16);
+  StpmUpdateArgs u = stpm_online_update_args(c, rd, po.gpart, po.stride, po.grid);
   timed_launch(c, 1, [&]() { ck(stpm_update(u, c->s), "stpm_step"); });
 }
 
-void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
+// Phi0 (host FP64, or the polar factor of a seeded Gaussian matrix), counters
+// and, for the BF16 form, the BF16 copies of y
+void stpm_prepare(mmsb_ctx* c, const double* phi0) {
   if (!c->have_y) throw MmsbError(MMSB_ERR_STATE, "stpm before whitening");
   const int k = c->k;
   if (k > 128) throw MmsbError(MMSB_ERR_UNSUPPORTED, "STPM kernels support k <= 128");
   cudaStream_t s = c->s;
-  const double a0 = c->cfg.alpha0;
-  const double p0 = (a0 + 1.0) * (a0 + 2.0) / 2.0, p1 = a0 * a0, p2 = -a0 * (a0 + 1.0) / 2.0;
-  float* G = c->tbuf<float>("G", (size_t)k * k);
   int* ns_it = c->tbuf<int>("ns_iters", 4);
   ck(cudaMemsetAsync(ns_it, 0, sizeof(int), s), "ns counter");
   if (phi0) {
@@ -647,15 +712,66 @@ void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
     ck(gaussian_panel(c->phi, k, k, k, c->cfg.seed, 7, s), "phi0");
     polar_only(c, nullptr);  // (not counted: the statistics cover the minibatch steps)
   }
-  const int64_t nx = c->nX;
   c->stats.stpm_steps = 0;
   c->stats.contract_ms = c->stats.step_ms = c->stats.contract_flops = c->stats.step_flops = 0.0;
   c->stats.contract_launches = c->stats.step_launches = 0;
   c->kused[0] = c->kused[1] = 0;
+  if (c->cfg.stpm_method != MMSB_STPM_BATCH_POWER && c->cfg.precision == MMSB_PREC_BF16) {
+    const int64_t nx = c->nX;
+    c->ldkh = (int)round_up(k, 8);
+    for (int q = 0; q < 3; ++q) {
+      c->yh[q] = c->buf("yh" + std::to_string(q), sizeof(uint16_t) * (size_t)nx * c->ldkh);
+      ck(panel_to_bf16(c->y[q], c->ldk, nx, k, c->yh[q], c->ldkh, s), "y bf16");
+    }
+  }
+}
+
+// lambda_i = That(phi_i, phi_i, phi_i) over all of X, sign fixed so lambda > 0
+// (queued on the context's stream)
+void stpm_lambda_pass(mmsb_ctx* c) {
+  const int k = c->k;
+  const int64_t nx = c->nX;
+  const double a0 = c->cfg.alpha0;
+  const double p0 = (a0 + 1.0) * (a0 + 2.0) / 2.0, p1 = a0 * a0, p2 = -a0 * (a0 + 1.0) / 2.0;
+  float* G = c->tbuf<float>("G", (size_t)k * k);
+  stpm_pass(c, kModePlain, 0, 1, 2, 0, nx, p0 / nx, p1, p2 / nx, 1.0, G, nullptr);
+  ck(stpm_tensor_values(k, c->phi, G, c->lambda, c->s), "lambda");
+}
+
+// statistics and device flags of an online / adjoint run (waits for the stream)
+void stpm_online_stats(mmsb_ctx* c, int64_t steps) {
+  const int k = c->k;
+  c->stats.stpm_steps = steps;
+  c->stats.node_updates = c->nX * c->cfg.sweeps;
+  int nsit = 0;
+  ck(cudaMemcpyAsync(&nsit, c->tbuf<int>("ns_iters", 4), sizeof(int), cudaMemcpyDeviceToHost,
+                     c->s), "ns counter");
+  ck(cudaStreamSynchronize(c->s), "sync");
+  c->stats.polar_iterations = nsit;
+  // gram + product of every Newton-Schulz iteration and of every online update
+  c->stats.step_flops = 4.0 * (double)k * k * k * (double)(nsit + steps);
+  check_flags(c, "stpm");
+  collect_kernel_times(c);
+  c->have_phi = true;
+}
+
+void stpm_finish_online(mmsb_ctx* c, int64_t steps) {
+  stpm_lambda_pass(c);
+  stpm_online_stats(c, steps);
+}
+
+void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
+  stpm_prepare(c, phi0);
+  const int k = c->k;
+  cudaStream_t s = c->s;
+  const int64_t nx = c->nX;
   if (c->cfg.stpm_method == MMSB_STPM_BATCH_POWER) {
     // tensorDecom_alpha0 (Util.cpp:131-184)
+    const double a0 = c->cfg.alpha0;
+    const double p0 = (a0 + 1.0) * (a0 + 2.0) / 2.0, p1 = a0 * a0, p2 = -a0 * (a0 + 1.0) / 2.0;
     const double inv_x = 1.0 / (double)nx;
     const double p_main = p0 * inv_x, p_s1 = p2 * inv_x, p_s0 = p1;
+    float* G = c->tbuf<float>("G", (size_t)k * k);
     double err = 0.0;
     for (int64_t it = 1;; ++it) {
       if (c->stop.load()) throw MmsbError(MMSB_ERR_STOPPED, "stop requested");
@@ -670,48 +786,19 @@ void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
     }
     c->stats.stpm_last_error = err;
     c->stats.node_updates = nx * c->stats.stpm_steps;
-  } else {
-    const bool adj = c->cfg.stpm_method == MMSB_STPM_ADJOINT;
-    const int64_t b = std::max<int64_t>(1, std::min<int64_t>(c->cfg.minibatch, nx));
-    // BF16 form: y and Phi enter the contraction in BF16 (FP32 accumulation)
-    // for every sweep but the last, which refines in FP32
-    const bool bf16_form = c->cfg.precision == MMSB_PREC_BF16;
-    if (bf16_form) {
-      c->ldkh = (int)round_up(k, 8);
-      for (int q = 0; q < 3; ++q) {
-        c->yh[q] = c->buf("yh" + std::to_string(q), sizeof(uint16_t) * (size_t)nx * c->ldkh);
-        ck(panel_to_bf16(c->y[q], c->ldk, nx, k, c->yh[q], c->ldkh, s), "y bf16");
-      }
-    }
-    int64_t t = 0;
-    for (int sw = 0; sw < c->cfg.sweeps; ++sw) {
-      const bool bf = bf16_form && sw + 1 < c->cfg.sweeps;
-      for (int64_t x0 = 0; x0 < nx; x0 += b) {
-        if (c->stop.load()) throw MmsbError(MMSB_ERR_STOPPED, "stop requested");
-        const int64_t cnt = std::min<int64_t>(b, nx - x0);
-        const double beta = c->cfg.lr0 / (1.0 + (double)t);
-        if (adj)  // dT (column i = d That_i / d phi_i); step = 3 theta O - dT
-          stpm_step(c, kModeAdjoint, x0, cnt, p0, p1, p2, 1.0 / cnt, beta, 1.0, ns_it, bf);
-        else  // G = mean of The_second_term; step = 3 theta O - 3 G
-          stpm_step(c, kModePlain, x0, cnt, p0 / cnt, p1, p2 / cnt, 1.0, beta, 3.0, ns_it, bf);
-        ++t;
-      }
-    }
-    c->stats.stpm_steps = t;
-    c->stats.node_updates = nx * c->cfg.sweeps;
-    int nsit = 0;
-    ck(cudaMemcpyAsync(&nsit, ns_it, sizeof(int), cudaMemcpyDeviceToHost, s), "ns counter");
-    ck(cudaStreamSynchronize(s), "sync");
-    c->stats.polar_iterations = nsit;
-    // gram + product of every Newton-Schulz iteration and of every online update
-    c->stats.step_flops = 4.0 * (double)k * k * k * (double)(nsit + t);
-    // lambda_i = That(phi_i, phi_i, phi_i) over all of X; sign fixed so lambda > 0
-    stpm_pass(c, kModePlain, 0, 1, 2, 0, nx, p0 / nx, p1, p2 / nx, 1.0, G, nullptr);
-    ck(stpm_tensor_values(k, c->phi, G, c->lambda, s), "lambda");
+    check_flags(c, "stpm");
+    collect_kernel_times(c);
+    c->have_phi = true;
+    return;
   }
-  check_flags(c, "stpm");
-  collect_kernel_times(c);
-  c->have_phi = true;
+  const int64_t rounds = stpm_online_rounds(c);
+  OnlineRound rd;
+  for (int64_t r = 0; r < rounds; ++r) {
+    if (c->stop.load()) throw MmsbError(MMSB_ERR_STOPPED, "stop requested");
+    stpm_online_round(c, r, &rd);
+    stpm_step(c, rd);
+  }
+  stpm_finish_online(c, rounds);
 }
 
 void pipeline_post(mmsb_ctx* c) {

@@ -305,6 +305,56 @@ mmsb_status mmsb_write_triplets_f32(const char* path, const float* m, int64_t ro
 mmsb_status mmsb_write_triplets_f64(const char* path, const double* m, int64_t rows,
                                     int64_t cols);
 
+/* ---- batched solver (many independent graphs) ----------------------------
+ * No counterpart in the reference, which solves one graph per process.  Each
+ * graph has its own context (k, alpha0 and seed base->seed + index; every
+ * other field from base, online or adjoint method, minibatch optionally per
+ * graph); the whitening chains of
+ * all graphs are queued concurrently, and the STPM minibatch updates of all
+ * graphs advance together: per round one contraction launch and one step
+ * launch per group of graphs with the same padded k, the whole round loop
+ * captured in a CUDA graph on the first run and replayed afterwards.  The
+ * contraction's CTAs per graph are chosen per group by timing candidates on
+ * the first run.  Results of graph i: the mmsb_get_* functions on
+ * mmsb_batch_graph(b, i). */
+typedef struct mmsb_batch mmsb_batch;
+
+typedef struct mmsb_batch_stats {
+  double total_ms;        /* last run: start to the last graph's results (device events) */
+  double stpm_end_ms;     /* batched run: start to the end of the STPM rounds */
+  double wall_ms;         /* host wall clock of the last run */
+  double latency_p50_ms;  /* per-graph latency: start to the graph's results */
+  double latency_p99_ms;
+  double latency_max_ms;
+  int64_t rounds;           /* batched minibatch rounds (the longest schedule) */
+  int64_t batched_launches; /* kernel launches of the STPM round loop */
+  int32_t graph_replayed;   /* 1: the round loop ran as a CUDA graph replay */
+  int32_t buckets;          /* groups of graphs with the same padded k */
+  int32_t bucket_kp[8];
+  int32_t bucket_ctas[8];   /* tuned contraction CTAs per graph */
+  int32_t bucket_graphs[8];
+} mmsb_batch_stats;
+
+/* k[count] required; alpha0[count] and minibatch[count] optional (NULL: base's) */
+mmsb_status mmsb_batch_create(const mmsb_config* base, int32_t count, const int32_t* k,
+                              const double* alpha0, const int32_t* minibatch, mmsb_batch** out);
+void mmsb_batch_destroy(mmsb_batch* b);
+/* upload graph `graph` (all before the first run) */
+mmsb_status mmsb_batch_upload(mmsb_batch* b, int32_t graph, const mmsb_csr blocks[MMSB_NUM_BLOCKS]);
+/* whitening, STPM and post-processing of every graph, batched */
+mmsb_status mmsb_batch_run(mmsb_batch* b);
+/* the same work graph by graph, each through the single-graph pipeline */
+mmsb_status mmsb_batch_run_sequential(mmsb_batch* b);
+int32_t mmsb_batch_count(const mmsb_batch* b);
+/* contraction CTAs per graph: 0 (default) lets the first run choose by
+ * timing; a positive multiple of 8 fixes it (before the first run) */
+mmsb_status mmsb_batch_set_contract_ctas(mmsb_batch* b, int32_t ctas);
+mmsb_ctx* mmsb_batch_graph(mmsb_batch* b, int32_t graph);
+/* per-graph latency (ms) of the last run, count values */
+mmsb_status mmsb_batch_latencies(const mmsb_batch* b, double* ms);
+mmsb_status mmsb_batch_get_stats(const mmsb_batch* b, mmsb_batch_stats* out);
+const char* mmsb_batch_last_error(const mmsb_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -266,3 +266,26 @@ def test_errors_are_status_codes(mm, golden_cfg1):
         with pytest.raises(mm.MmsbError) as e:
             p.upload(bad)
         assert e.value.status == 1
+
+
+def test_rank_deficient_graph(mm, oracle):
+    """A graph too sparse for its k (124 X->A edges, pair operators of rank
+    ~101 < 2k = 120): the eigen-solver meets exactly zero directions.  The
+    pipeline must stay finite and agree with the FP64 oracle on the whitening
+    subspace (W W^T, which is invariant under the free rotations)."""
+    n, k, a0 = 2000, 60, 0.3
+    g = mm.generate(n, k, a0, 0.02, 2e-4, seed=5)
+    Gxa, Gxb, Gxc, _, _ = g.scipy_blocks()
+    rng = np.random.default_rng(3)
+    nX, nA, nB, nC = g.parts
+    sk = (rng.standard_normal((nB, 2 * k)), rng.standard_normal((nC, 2 * k)),
+          rng.standard_normal((nA, 2 * k)))
+    wh = oracle.second_whiten(Gxa, Gxb, Gxc, k, a0, sk)
+    with mm.Pipeline(k=k, alpha0=a0, stpm_method=mm.STPM_ONLINE, sweeps=2, minibatch=128) as p:
+        p.upload(g).whiten(sk)
+        W = p.whitening()["W"]
+        assert np.isfinite(W).all()
+        P, Po = W @ W.T, wh["W"] @ wh["W"].T
+        assert np.linalg.norm(P - Po) / np.linalg.norm(Po) < 1e-2
+        p.stpm().postproc()
+        assert np.isfinite(p.lam()).all() and np.isfinite(p.pi()).all()
