@@ -2,8 +2,8 @@
 //
 // Some callers must not call cudaMalloc: code running inside another
 // framework's memory pool (which owns every device allocation and would be
-// bypassed or fragmented by a raw cudaMalloc), or code executing while a
-// stream is being captured, where allocation calls are not allowed.  Such a
+// bypassed or fragmented by a raw cudaMalloc), or latency-critical code that
+// must not wait on cudaMalloc, which can synchronize the device.  Such a
 // caller already owns its input and output device buffers; the only extra
 // memory this operation needs -- the transposed copy of the CSR block -- lives
 // here in a fixed, file-scope device array instead.
@@ -12,7 +12,9 @@
 // that loads this library until the process exits.  All calls share it: two
 // calls that overlap on the GPU (different streams, or different host threads)
 // race on it and must be serialised by the caller.  Each call clears the part
-// that must start at zero (the per-column counters) itself.
+// that must start at zero (the per-column counters) itself.  The first call
+// on a device looks the array's device address up once (see below); make that
+// first call before any stream capture.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -247,7 +247,9 @@ mmsb_status mmsb_op_symeig(const double* A, int32_t n, double* evals, double* ev
 
 /* No counterpart in the reference.  Y = alpha * G^T * P for callers that
  * cannot allocate device memory (code inside another framework's memory pool,
- * or running while a stream is captured): same result as mmsb_op_spmm with
+ * which owns every device allocation, or latency-critical code that must not
+ * wait on cudaMalloc, which can synchronize the device): same result as
+ * mmsb_op_spmm with
  * transpose != 0, but every pointer is a DEVICE pointer the caller owns and
  * the call allocates nothing.  G: n_rows x n_cols CSR (d_val NULL = binary);
  * P: n_rows x p row-major, Y: n_cols x p row-major, p a multiple of 4, 16-byte

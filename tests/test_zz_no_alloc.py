@@ -1,6 +1,6 @@
 """mmsb_op_spmm_t_noalloc: the transposed SpMM for callers that cannot
 allocate device memory (code inside another framework's memory pool, or
-running while a stream is captured).  Its result must equal the allocating
+latency-critical code that must not wait on cudaMalloc).  Its result must equal the allocating
 entry point mmsb_op_spmm(transpose=1) on the same inputs, call after call,
 because every call reuses the same fixed device array.
 
