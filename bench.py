@@ -33,6 +33,11 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 
+# independent graphs' streams (batched solver) run concurrently only on
+# separate hardware work queues; the runtime default is 8 (read when the
+# CUDA context is created, so this must precede the first CUDA call)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 WORKLOAD = dict(name="mmsb-n200k-k100-fp32-online", n=200_000, k=100, alpha0=0.1, p_in=0.05,
                 p_out=5e-4, sweeps=20, minibatch=4096, seed=0)
 
