@@ -79,7 +79,8 @@ __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
   }
   if (a.mode == kModeLoss && blockIdx.x == 0 && threadIdx.x == 0) {
     double t = 0.0;
-    for (int p = 0; p < a.nparts; ++p) t += (double)a.gpart[(int64_t)p * a.part_stride + kk + 3 * k];
+    for (int p = 0; p < a.nparts; ++p)  // one loss slot per contraction column block
+      for (int sl = 0; sl < 4; ++sl) t += (double)a.gpart[(int64_t)p * a.part_stride + kk + 3 * k + sl];
     double that = t / a.count;
     for (int i = 0; i < k; ++i) that += a.c1 * m[i] * m[k + i] * m[2 * k + i];
     a.loss_out[0] = that;  // sum_i That(phi_i, phi_i, phi_i)
@@ -114,15 +115,20 @@ __device__ __forceinline__ float ns_poly(float y) { return y * (1.5f - 0.5f * y 
 // multiple of 16) makes the fragment loads of the Gram product conflict-free
 __host__ __device__ constexpr int step_xld(int KP) { return KP + 4; }
 
-// NB = 8 (one n-tile) when the cluster has KP / 8 CTAs, else 16
+// NB = 8 (one n-tile) when the cluster has KP / 8 CTAs, else 16.  Above
+// KP = 128 two FP32 copies of Phi no longer fit one SM (SB: a single buffer,
+// refilled in place after a cluster barrier, and the G block kept in the
+// second staging tile, which the online update leaves unused).
 template <int KP, int CL>
 struct StepSmem {
   static constexpr int NB = KP / CL, XLD = step_xld(KP), MT = KP / 16, NT = NB / 8;
   static constexpr int TILES = MT * NT, KS = TILES <= 8 ? 2 : 1;  // K split over warps
-  static constexpr size_t floats = (size_t)2 * KP * XLD    // X, next X
-                                   + (size_t)4 * NB * XLD  // B (Ab), G block, 2 output tiles
-                                   + (size_t)TILES * 128   // K-split partial tiles
+  static constexpr bool SB = KP > 128;
+  static constexpr size_t floats = (size_t)(SB ? 1 : 2) * KP * XLD    // X (and next X)
+                                   + (size_t)(SB ? 3 : 4) * NB * XLD  // B, 2 output tiles (+ G block)
+                                   + (size_t)(KS == 2 ? TILES * 128 : 0)  // K-split partial tiles
                                    + 4 * KP + 3 * CL + 3 * NB + 2 * NB + 8;
+  static_assert(floats * sizeof(float) <= 227 * 1024 - 2048, "step kernel shared memory");
 };
 
 __device__ __forceinline__ uint32_t tf32_round(float x) {
@@ -228,35 +234,42 @@ __device__ __forceinline__ void warp_tile_3xtf32(const float* __restrict__ pa,
 // kProdTimes: P_blk = X B_blk                 (A(m=r, k=i) = X[i XLD + r])
 enum StepProd : int { kProdGram = 0, kProdTimes = 1 };
 
-template <int KP, int CL, int PROD>
-__device__ __forceinline__ bool step_product(const float* __restrict__ X, const float* __restrict__ Bm,
-                                             int c0, float* __restrict__ part, float (&acc)[4],
-                                             int& m0, int& n0) {
+template <int KP, int CL, int PROD, typename Epi>
+__device__ __forceinline__ void step_tiles(const float* __restrict__ X, const float* __restrict__ Bm,
+                                           int c0, float* __restrict__ part, Epi&& epi) {
   using S = StepSmem<KP, CL>;
   constexpr int XLD = S::XLD;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tile = warp % S::TILES, ks = warp / S::TILES;
-  const bool active = warp < S::TILES * S::KS;
-  m0 = (tile % S::MT) * 16;
-  n0 = (tile / S::MT) * 8;
-  const int kb = ks * (KP / S::KS), ke = kb + KP / S::KS;
-  if (active) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  auto product = [&](int tile, int kb, int ke, float (&acc)[4]) {
+    const int m0 = (tile % S::MT) * 16, n0 = (tile / S::MT) * 8;
     if (PROD == kProdGram)
       warp_tile_3xtf32<XLD, 1, 1, XLD>(X + m0 * XLD, X + (c0 + n0) * XLD, kb, ke, acc);
     else
       warp_tile_3xtf32<1, XLD, 1, XLD>(X + m0, Bm + n0 * XLD, kb, ke, acc);
-    if (S::KS == 2 && ks == 1) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) part[tile * 128 + q * 32 + lane] = acc[q];
-    }
-  }
-  __syncthreads();
-  if (!active || ks != 0) return false;
+  };
   if (S::KS == 2) {
+    const int tile = warp % S::TILES, ks = warp / S::TILES;
+    const bool active = warp < S::TILES * S::KS;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    if (active) {
+      product(tile, ks * (KP / 2), ks * (KP / 2) + KP / 2, acc);
+      if (ks == 1) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) part[tile * 128 + q * 32 + lane] = acc[q];
+      }
+    }
+    __syncthreads();
+    if (!active || ks != 0) return;
 #pragma unroll
     for (int q = 0; q < 4; ++q) acc[q] += part[tile * 128 + q * 32 + lane];
+    epi(acc, (tile % S::MT) * 16, (tile / S::MT) * 8, tile);
+  } else {
+    for (int tile = warp; tile < S::TILES; tile += nw) {
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      product(tile, 0, KP, acc);
+      epi(acc, (tile % S::MT) * 16, (tile / S::MT) * 8, tile);
+    }
   }
-  return true;
 }
 
 template <int KP, int CL>
@@ -268,12 +281,12 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   const int rank = (int)cluster.block_rank();
   extern __shared__ __align__(16) float sm[];
   float* Xa = sm;
-  float* Xb = Xa + KP * XLD;
-  float* Ab = Xb + KP * XLD;      // B (or A) block, column jb at Ab + jb * XLD
-  float* Gb = Ab + NB * XLD;      // G block (online step)
-  float* Ot = Gb + NB * XLD;      // 2 staging tiles of the cluster broadcast
-  float* part = Ot + 2 * NB * XLD;    // K-split partial tiles
-  float* mv = part + S::TILES * 128;  // m1, m2, m3 (+ pad) for this block
+  float* Xb = S::SB ? Xa : Xa + KP * XLD;         // SB: one buffer, refilled in place
+  float* Ab = Xa + (S::SB ? 1 : 2) * KP * XLD;    // B (or A) block, column jb at Ab + jb * XLD
+  float* Ot = Ab + NB * XLD;                      // 2 staging tiles of the cluster broadcast
+  float* Gb = Ot + (S::SB ? 1 : 2) * NB * XLD;    // G block (online step; SB: staging tile 2)
+  float* part = Ot + (S::SB ? 2 : 3) * NB * XLD;  // K-split partial tiles
+  float* mv = part + (S::KS == 2 ? S::TILES * 128 : 0);  // m1, m2, m3 (+ pad) for this block
   float* red = mv + 4 * KP;       // initial statistics of the CL ranks (3 x CL)
   float* dcol = red + 3 * CL;     // 3 * NB d-sums (online step)
   __shared__ float s_abs, s_err, s_fro;
@@ -295,7 +308,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       for (int u = 0; u < B; ++u)
         if (e0 + 512 * u < N) {
           Xa[e0 + 512 * u] = v[u];
-          Xb[e0 + 512 * u] = 0.f;
+          if (!S::SB) Xb[e0 + 512 * u] = 0.f;
         }
     }
   }
@@ -325,9 +338,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   auto times_and_broadcast = [&](float alpha, float beta_self, const float* Gsrc, float gamma) {
     float* Otc = Ot + (nbcast & 1) * NB * XLD;
     ++nbcast;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    int m0, n0;
-    if (step_product<KP, CL, kProdTimes>(X, Ab, c0, part, acc, m0, n0)) {
+    step_tiles<KP, CL, kProdTimes>(X, Ab, c0, part, [&](const float (&acc)[4], int m0, int n0, int) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int r = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
@@ -335,7 +346,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
         if (Gsrc) v += gamma * Gsrc[jb * XLD + r];
         Otc[jb * XLD + r] = (r < k && col < k) ? v : 0.f;
       }
-    }
+    });
     if (tid == 0) {
       Otc[KP] = s_abs;
       Otc[KP + 1] = s_err;
@@ -343,6 +354,9 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // staging -> async proxy
     __syncthreads();
+    // single buffer: every CTA has finished reading the current iterate
+    // before any copy overwrites it
+    if (S::SB) cluster.sync();
     const int bi = dn == Xa ? 0 : 1;
     if (tid < CL)
       bulk_copy_to_rank(dn + c0 * XLD, Otc, (uint32_t)(sizeof(float) * NB * XLD), &s_full[bi],
@@ -411,18 +425,14 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       Gb[jb * XLD + j] = gval;
     }
     // Phi' = Phi - beta (3 theta Phi (Phi^T Phi)^.2 - gscale G)   (Util.cpp:259-272)
-    {
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
-      int m0, n0;
-      if (step_product<KP, CL, kProdGram>(X, nullptr, c0, part, acc, m0, n0)) {
+    step_tiles<KP, CL, kProdGram>(X, nullptr, c0, part, [&](const float (&acc)[4], int m0, int n0, int) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int i = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1);
-          Ab[jb * XLD + i] = acc[q] * acc[q];
-        }
+      for (int q = 0; q < 4; ++q) {
+        const int i = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1);
+        Ab[jb * XLD + i] = acc[q] * acc[q];
       }
-      __syncthreads();
-    }
+    });
+    __syncthreads();
     if (!times_and_broadcast(-a.beta * a.theta3, 1.f, Gb, a.beta * a.gscale)) timed_out = true;
     swap_buffers();
   }
@@ -449,10 +459,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   // so the result does not depend on warp timing)
   __shared__ float colpart[S::MT * NB], errpart[S::TILES], fropart[S::TILES];
   auto gram_stats = [&](float d0, float d1) {
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    int m0, n0;
-    const bool own = step_product<KP, CL, kProdGram>(X, nullptr, c0, part, acc, m0, n0);
-    if (own) {
+    step_tiles<KP, CL, kProdGram>(X, nullptr, c0, part, [&](const float (&acc)[4], int m0, int n0, int tile) {
       float er = 0.f, fr = 0.f, ca[2] = {0.f, 0.f};
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
@@ -477,7 +484,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
         er = fmaxf(er, __shfl_xor_sync(0xffffffffu, er, off));
         fr += __shfl_xor_sync(0xffffffffu, fr, off);
       }
-      const int mt = m0 / 16, tile = (tid >> 5) % S::TILES;
+      const int mt = m0 / 16;
       if (g == 0) {
         colpart[mt * NB + n0 + 2 * t4] = ca[0];
         colpart[mt * NB + n0 + 2 * t4 + 1] = ca[1];
@@ -486,7 +493,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
         errpart[tile] = er;
         fropart[tile] = fr;
       }
-    }
+    });
     __syncthreads();
     if (tid == 0) {
       float m = 0.f, e = 0.f, f = 0.f;
@@ -630,16 +637,24 @@ struct Contract {
   static constexpr int TM = BF ? 64 : 32;  // nodes per tile
   static constexpr int NZ = MODE == kModePlain ? 2 : 3;
   static constexpr int NC = MODE == kModePlain ? 1 : MODE == kModeAdjoint ? 3 : 0;
+  // columns i of Phi handled by one CTA: all of them up to KP = 128, above
+  // that blocks of 64 (blockIdx.y), so that Phi's block, the G accumulators
+  // and the staged partial fit one SM; Z, C, G and the d-sums are separable
+  // by column
+  static constexpr int IB = KP <= 128 ? KP : 64;
+  static constexpr int NBC = (KP + IB - 1) / IB;  // column blocks (<= 4: one loss slot each)
   static constexpr int PAD = BF ? 8 : 4;   // row strides == 4 words mod 8: conflict-free fragments
   static constexpr int PLD = KP + PAD, LDY = KP + PAD, LDC = TM + PAD;
-  static constexpr int MTI = KP / 16, NTX = TM / 8, NTI = KP / 8;
-  static constexpr int GT = MTI * NTI, GPW = (GT + 7) / 8;  // G tiles (16 x 8), per warp
+  static constexpr int MTI = IB / 16, NTX = TM / 8;        // Z^T tiles: i (16) x nodes (8)
+  static constexpr int MTJ = KP / 16, NTI = IB / 8;        // G tiles: j (16) x i (8)
+  static constexpr int GT = MTJ * NTI, GPW = (GT + 7) / 8;  // G tiles, per warp
   static constexpr int KSTEP = BF ? 16 : 8;
   static constexpr size_t tile_bytes =
-      sizeof(T) * ((size_t)KP * PLD + (size_t)3 * TM * LDY + (size_t)NC * KP * LDC);
-  static constexpr size_t stage_bytes = sizeof(float) * ((size_t)KP * KP + 3 * KP + 4);
+      sizeof(T) * ((size_t)IB * PLD + (size_t)3 * TM * LDY + (size_t)NC * IB * LDC);
+  static constexpr size_t stage_bytes = sizeof(float) * ((size_t)KP * IB + 3 * IB + 4);
   static constexpr size_t region = ((tile_bytes > stage_bytes ? tile_bytes : stage_bytes) + 15) / 16 * 16;
-  static constexpr size_t smem = region + sizeof(float) * (3 * KP + 8 + 8 * 3 * KP);
+  static constexpr size_t smem = region + sizeof(float) * (3 * IB + 8 + 8 * 3 * IB);
+  static_assert(NBC <= 4, "one loss slot per column block");
 };
 
 template <typename T>
@@ -679,25 +694,28 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
   using T = typename Cfg::T;
   constexpr int TM = Cfg::TM, NZ = Cfg::NZ, NC = Cfg::NC, PLD = Cfg::PLD, LDY = Cfg::LDY,
                 LDC = Cfg::LDC;
-  static_assert(KP % 16 == 0 && KP <= 128, "KP");
+  constexpr int IB = Cfg::IB;
+  static_assert(KP % 16 == 0 && KP <= 256, "KP");
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* Phis = reinterpret_cast<T*>(smraw);  // Phis[i PLD + j] = Phi_ji (column i of Phi)
-  T* Ys = Phis + KP * PLD;                // 3 node-major tiles: Ys[q TM LDY + x LDY + j]
-  T* CT = Ys + 3 * TM * LDY;              // NC coefficient tiles, i-major: CT[c KP LDC + i LDC + x]
-  float* mv = reinterpret_cast<float*>(smraw + Cfg::region);  // m1 | m2 | m3
-  float* tred = mv + 3 * KP;                                  // 8 loss partials
-  float* dw = tred + 8;  // per-warp d-sums (3 KP each), summed in a fixed order at the end
+  // this CTA's columns of Phi: i0 + ii, ii < IB (i local below)
+  const int cb = (Cfg::NBC > 1) ? (int)blockIdx.y : 0, i0 = cb * IB;
+  T* Phis = reinterpret_cast<T*>(smraw);  // Phis[ii PLD + j] = Phi_j,i0+ii (column i0+ii of Phi)
+  T* Ys = Phis + IB * PLD;                // 3 node-major tiles: Ys[q TM LDY + x LDY + j]
+  T* CT = Ys + 3 * TM * LDY;              // NC coefficient tiles, i-major: CT[c IB LDC + ii LDC + x]
+  float* mv = reinterpret_cast<float*>(smraw + Cfg::region);  // m1 | m2 | m3 (IB each)
+  float* tred = mv + 3 * IB;                                  // 8 loss partials
+  float* dw = tred + 8;  // per-warp d-sums (3 IB each), summed in a fixed order at the end
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, g = lane >> 2, t4 = lane & 3;
   const int k = a.k;
 
   // Phi: loads issued in batches of 8 per thread so that their latencies overlap
   {
-    constexpr int N = KP * PLD, B = 8;
+    constexpr int N = IB * PLD, B = 8;
     for (int e0 = tid; e0 < N; e0 += 256 * B) {
       float v[B];
 #pragma unroll
       for (int u = 0; u < B; ++u) {
-        const int e = e0 + 256 * u, i = e / PLD, j = e % PLD;
+        const int e = e0 + 256 * u, i = i0 + e / PLD, j = e % PLD;
         v[u] = (e < N && i < k && j < k) ? __ldg(a.phi + (int64_t)i * k + j) : 0.f;
       }
 #pragma unroll
@@ -713,9 +731,9 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
     dw[e] = (mu && j < k) ? mu[j] : 0.f;
   }
   __syncthreads();
-  for (int e = tid; e < 3 * KP; e += 256) {
-    const float* mu = dw + (e / KP) * KP;
-    const T* ph = Phis + (e % KP) * PLD;
+  for (int e = tid; e < 3 * IB; e += 256) {
+    const float* mu = dw + (e / IB) * KP;
+    const T* ph = Phis + (e % IB) * PLD;
     float s0 = 0.f, s1 = 0.f;
 #pragma unroll 4
     for (int j = 0; j < KP; j += 2) {
@@ -725,7 +743,7 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
     mv[e] = s0 + s1;
   }
   __syncthreads();
-  for (int e = tid; e < 8 * 3 * KP; e += 256) dw[e] = 0.f;
+  for (int e = tid; e < 8 * 3 * IB; e += 256) dw[e] = 0.f;
   if (tid < 8) tred[tid] = 0.f;
   __syncthreads();
 
@@ -833,14 +851,14 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const int i = m0 + g + 8 * (r >> 1), x = n0 + 2 * t4 + (r & 1);
-        const bool valid = x < nvalid && i < k;
-        const float m1 = mv[i], m2 = mv[KP + i];
+        const bool valid = x < nvalid && i0 + i < k;
+        const float m1 = mv[i], m2 = mv[IB + i];
         const float z1 = z[0][r], z2 = z[1][r];
         if (MODE == kModePlain) {
           cv[0][r] = valid ? cc0 * z1 * z2 + cc2 * (z1 * m2 + m1 * z2) : 0.f;
           if (valid) dl[0][r >> 1] = fmaf(z1, z2, dl[0][r >> 1]);
         } else {
-          const float m3 = mv[2 * KP + i], z3 = z[NZ - 1][r];
+          const float m3 = mv[2 * IB + i], z3 = z[NZ - 1][r];
           if (MODE == kModeAdjoint) {
             cv[0][r] = valid ? cc0 * z2 * z3 + cc2 * (z2 * m3 + m2 * z3) : 0.f;
             cv[1][r] = valid ? cc0 * z1 * z3 + cc2 * (z1 * m3 + m1 * z3) : 0.f;
@@ -859,7 +877,7 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
       for (int c = 0; c < NC; ++c)
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          T* dst = CT + c * KP * LDC + (m0 + g + 8 * h) * LDC + n0 + 2 * t4;
+          T* dst = CT + c * IB * LDC + (m0 + g + 8 * h) * LDC + n0 + 2 * t4;
           if (BF) {
             *reinterpret_cast<__nv_bfloat162*>(dst) = __floats2bfloat162_rn(cv[c][2 * h], cv[c][2 * h + 1]);
           } else {
@@ -874,7 +892,7 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
           float v = dl[qd][h];
           v += __shfl_xor_sync(0xffffffffu, v, 1);
           v += __shfl_xor_sync(0xffffffffu, v, 2);
-          if (t4 == 0) dw[warp * 3 * KP + qd * KP + m0 + g + 8 * h] += v;
+          if (t4 == 0) dw[warp * 3 * IB + qd * IB + m0 + g + 8 * h] += v;
         }
       }
     }
@@ -888,11 +906,11 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
         for (int u = 0; u < Cfg::GPW; ++u) {
           const int tt = warp + 8 * u;
           if (tt >= Cfg::GT) continue;
-          const int m0 = (tt % Cfg::MTI) * 16, n0 = (tt / Cfg::MTI) * 8;
+          const int m0 = (tt % Cfg::MTJ) * 16, n0 = (tt / Cfg::MTJ) * 8;
 #pragma unroll
           for (int c = 0; c < NC; ++c) {
             const T* Yo = Ys + (MODE == kModePlain ? 2 : c) * TM * LDY;
-            const T* Cc = CT + c * KP * LDC;
+            const T* Cc = CT + c * IB * LDC;
             if (BF) {
               uint32_t af[4];
               const int q = lane >> 3, rr = lane & 7;
@@ -926,16 +944,18 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
     for (int off = 16; off; off >>= 1) tsum += __shfl_xor_sync(0xffffffffu, tsum, off);
     if (lane == 0) tred[warp] = tsum;
   }
-  // cluster reduction: every CTA stages its partial (k x k column-major
-  // contraction, 3 d-sums, loss) in shared memory; CTA r of the cluster sums a
-  // 1/CLP slice over the cluster's CTAs through DSMEM and writes it out.
+  // cluster reduction: every CTA stages its partial (this column block of
+  // the k x k column-major contraction, its 3 d-sums, loss) in shared memory;
+  // CTA r of the cluster sums a 1/CLP slice over the cluster's CTAs through
+  // DSMEM and writes it out.  Column block cb writes loss slot cb of the 4
+  // spare floats of the partial row (block 0 also clears the unused slots).
   float* stage = reinterpret_cast<float*>(smraw);  // tiles are dead from here on
   if (NC > 0) {
 #pragma unroll
     for (int u = 0; u < Cfg::GPW; ++u) {
       const int tt = warp + 8 * u;
       if (tt >= Cfg::GT) continue;
-      const int m0 = (tt % Cfg::MTI) * 16, n0 = (tt / Cfg::MTI) * 8;
+      const int m0 = (tt % Cfg::MTJ) * 16, n0 = (tt / Cfg::MTJ) * 8;
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         const int j = m0 + g + 8 * (r >> 1), i = n0 + 2 * t4 + (r & 1);
@@ -944,22 +964,22 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
     }
   }
   __syncthreads();
-  for (int e = tid; e < 3 * KP; e += 256) {
+  for (int e = tid; e < 3 * IB; e += 256) {
     float v = 0.f;
 #pragma unroll
-    for (int w = 0; w < 8; ++w) v += dw[w * 3 * KP + e];
-    stage[KP * KP + e] = v;
+    for (int w = 0; w < 8; ++w) v += dw[w * 3 * IB + e];
+    stage[KP * IB + e] = v;
   }
   if (tid == 0) {
     float t = 0.f;
     if (MODE == kModeLoss)
       for (int w = 0; w < 8; ++w) t += tred[w];
-    stage[KP * KP + 3 * KP] = t;
+    stage[KP * IB + 3 * IB] = t;
   }
   cg::cluster_group cluster = cg::this_cluster();
   const int crank = (int)cluster.block_rank();
   constexpr int CLP = kPartialCluster;
-  constexpr int STAGE = KP * KP + 3 * KP + 4;
+  constexpr int STAGE = KP * IB + 3 * IB + 1;
   cluster.sync();
   float* gp = a.gpart + (int64_t)(blockIdx.x / CLP) * a.part_stride;
   const int slice = (STAGE + CLP - 1) / CLP;
@@ -967,16 +987,17 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
     float v = 0.f;
 #pragma unroll
     for (int q = 0; q < CLP; ++q) v += cluster.map_shared_rank(stage, q)[e];
-    if (e < KP * KP) {
-      const int i = e / KP, j = e % KP;
+    if (e < KP * IB) {
+      const int i = i0 + e / KP, j = e % KP;
       if (i < k && j < k && MODE != kModeLoss) gp[(int64_t)i * k + j] = v;
-    } else if (e < KP * KP + 3 * KP) {
-      const int q = (e - KP * KP) / KP, i = (e - KP * KP) % KP;
+    } else if (e < KP * IB + 3 * IB) {
+      const int q = (e - KP * IB) / IB, i = i0 + (e - KP * IB) % IB;
       if (i < k) gp[(int64_t)k * k + q * k + i] = v;
-    } else if (e == KP * KP + 3 * KP) {
-      gp[(int64_t)k * k + 3 * k] = v;
+    } else {
+      gp[(int64_t)k * k + 3 * k + cb] = v;
     }
   }
+  if (cb == 0 && crank == 0 && tid < 4 && tid >= Cfg::NBC) gp[(int64_t)k * k + 3 * k + tid] = 0.f;
   cluster.sync();  // keep shared memory alive until every remote read is done
 }
 
@@ -1050,7 +1071,7 @@ cudaError_t launch_partial_t(const StpmPartialArgs& a, int grid, cudaStream_t s)
     set = true;
   }
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid, 1, 1);
+  cfg.gridDim = dim3((unsigned)grid, (unsigned)Contract<KP, MODE, BF>::NBC, 1);
   cfg.blockDim = dim3(256, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
@@ -1076,6 +1097,8 @@ cudaError_t launch_partial_m(int KP, const StpmPartialArgs& a, int grid, cudaStr
     case 96: return launch_partial_t<96, MODE, BF>(a, grid, s);
     case 112: return launch_partial_t<112, MODE, BF>(a, grid, s);
     case 128: return launch_partial_t<128, MODE, BF>(a, grid, s);
+    case 160: return launch_partial_t<160, MODE, BF>(a, grid, s);
+    case 208: return launch_partial_t<208, MODE, BF>(a, grid, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -1164,19 +1187,24 @@ cudaError_t launch_step_t(const StpmUpdateArgs& a, cudaStream_t s) {
 template <int KP>
 cudaError_t launch_step_k(const StpmUpdateArgs& a, cudaStream_t s) {
   // KP / 8 CTAs (8 columns each; up to 16, a non-portable cluster size) where
-  // the device can co-schedule them, else KP / 16 CTAs of 16 columns
-  static int wide = -1;
-  if (wide != 0) {
-    cudaError_t e = launch_step_t<KP, KP / 8>(a, s);
-    if (e == cudaSuccess) {
-      wide = 1;
-      return e;
+  // the device can co-schedule them, else KP / 16 CTAs of 16 columns; above
+  // KP = 128 always KP / 16 (a cluster holds at most 16 CTAs)
+  if constexpr (KP > 128) {
+    return launch_step_t<KP, KP / 16>(a, s);
+  } else {
+    static int wide = -1;
+    if (wide != 0) {
+      cudaError_t e = launch_step_t<KP, KP / 8>(a, s);
+      if (e == cudaSuccess) {
+        wide = 1;
+        return e;
+      }
+      if (wide == 1) return e;
+      cudaGetLastError();
+      wide = 0;
     }
-    if (wide == 1) return e;
-    cudaGetLastError();
-    wide = 0;
+    return launch_step_t<KP, KP / 16>(a, s);
   }
-  return launch_step_t<KP, KP / 16>(a, s);
 }
 
 template <int KP, int CL>
@@ -1228,7 +1256,16 @@ cudaError_t launch_step_batched_k(const StpmUpdateArgs* args, int graphs, cudaSt
 
 int stpm_partial_cluster() { return kPartialCluster; }
 
-int stpm_kp(int k) { return (int)round_up(k, 16) < 32 ? 32 : (int)round_up(k, 16); }
+// padded k of the STPM kernels: multiples of 16 from 32 to 128, then 160 and
+// 208 (k <= 208); -1 beyond
+int stpm_kp(int k) {
+  const int r = (int)round_up(k, 16);
+  if (r <= 32) return 32;
+  if (r <= 128) return r;
+  if (r <= 160) return 160;
+  if (r <= 208) return 208;
+  return -1;
+}
 
 int stpm_partial_grid(int64_t count, bool bf16) {
   const int64_t tiles = ceil_div(count, bf16 ? 64 : 32);
@@ -1238,7 +1275,7 @@ int stpm_partial_grid(int64_t count, bool bf16) {
 
 cudaError_t stpm_partial(int mode, const StpmPartialArgs& a, int grid, bool bf16, cudaStream_t s) {
   const int KP = stpm_kp(a.k);
-  if (KP > 128) return cudaErrorInvalidValue;
+  if (KP < 0) return cudaErrorInvalidValue;
   if (bf16 && (!a.yh1 || !a.yh2 || !a.yh3 || a.ldyh % 8 != 0)) return cudaErrorInvalidValue;
   if (!bf16 && a.ldy % 4 != 0) return cudaErrorInvalidValue;
   return bf16 ? launch_partial_p<true>(mode, KP, a, grid, s)
@@ -1262,11 +1299,13 @@ cudaError_t stpm_update(const StpmUpdateArgs& a, cudaStream_t s) {
     case 96: return launch_step_k<96>(a, s);
     case 112: return launch_step_k<112>(a, s);
     case 128: return launch_step_k<128>(a, s);
+    case 160: return launch_step_k<160>(a, s);
+    case 208: return launch_step_k<208>(a, s);
     default: return cudaErrorInvalidValue;
   }
 }
 
-int stpm_step_kp(int k) { return k <= 32 ? 32 : (int)round_up(k, 16); }
+int stpm_step_kp(int k) { return stpm_kp(k); }
 
 cudaError_t stpm_partial_batched(int mode, int KP, const StpmPartialArgs* args, int graphs,
                                  int grid, bool bf16, cudaStream_t s) {

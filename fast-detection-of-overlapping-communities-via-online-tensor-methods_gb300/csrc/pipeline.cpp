@@ -699,7 +699,7 @@ static void stpm_step(mmsb_ctx* c, const OnlineRound& rd) {
 void stpm_prepare(mmsb_ctx* c, const double* phi0) {
   if (!c->have_y) throw MmsbError(MMSB_ERR_STATE, "stpm before whitening");
   const int k = c->k;
-  if (k > 128) throw MmsbError(MMSB_ERR_UNSUPPORTED, "STPM kernels support k <= 128");
+  if (stpm_kp(k) < 0) throw MmsbError(MMSB_ERR_UNSUPPORTED, "STPM kernels support k <= 208");
   cudaStream_t s = c->s;
   int* ns_it = c->tbuf<int>("ns_iters", 4);
   ck(cudaMemsetAsync(ns_it, 0, sizeof(int), s), "ns counter");
@@ -851,7 +851,7 @@ struct PhiSwap {
 
 void check_range(mmsb_ctx* c, int64_t& begin, int64_t& count) {
   if (!c->have_y) throw MmsbError(MMSB_ERR_STATE, "loss needs whitened data");
-  if (c->k > 128) throw MmsbError(MMSB_ERR_UNSUPPORTED, "STPM kernels support k <= 128");
+  if (stpm_kp(c->k) < 0) throw MmsbError(MMSB_ERR_UNSUPPORTED, "STPM kernels support k <= 208");
   if (count <= 0) {
     begin = 0;
     count = c->nX;
