@@ -48,6 +48,12 @@ BATCH = dict(name="mmsb-batch256-n2k-200k-k5-64-online", graphs=256, n_lo=2_000,
              steps_per_sweep=8, degree_cap=30, seed=0)
 
 
+# the precision configuration: the BF16 form beside the FP32 form, errors of
+# both against an FP64 STPM and post-processing
+PRECISION = dict(name="mmsb-n2m-k200-bf16-online", n=2_000_000, k=200, alpha0=0.5, p_in=0.02,
+                 p_out=1e-5, sweeps=5, minibatch=65536, seed=0)
+
+
 def load_pkg():
     sys.path.insert(0, str(ROOT))
     import __graft_entry__ as ge
@@ -486,6 +492,128 @@ def run_batch(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def _match(A, B):
+    """Permutation and signs of B's columns best matching A's (greedy on |cos|)."""
+    An = A / np.maximum(np.linalg.norm(A, axis=0), 1e-300)
+    Bn = B / np.maximum(np.linalg.norm(B, axis=0), 1e-300)
+    C = np.abs(An.T @ Bn)
+    perm = -np.ones(A.shape[1], dtype=int)
+    used = set()
+    for i in np.argsort(-C.max(axis=1)):
+        for j in np.argsort(-C[i]):
+            if j not in used:
+                perm[i] = j
+                used.add(j)
+                break
+    sign = np.sign(np.sum(A * B[:, perm], axis=0))
+    sign[sign == 0] = 1
+    return perm, sign
+
+
+def run_precision(args, ws, rank, local):
+    """The BF16 form (y in BF16, Phi as a BF16 hi/lo pair, FP32 accumulation,
+    all sweeps but the last; the last sweep refines in FP32) beside the FP32
+    form on the precision configuration, with the error of lambda, Phi and Pi
+    of both against the FP64 oracle's STPM and post-processing run from the
+    same Phi0 on the device's whitening (an FP64 whitening of the 100M-edge
+    graph is beyond the oracle's single-threaded sparse products)."""
+    if rank != 0:
+        return
+    mm = load_pkg()
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import mmsb_oracle as O
+    wl = dict(PRECISION)
+    t0 = time.perf_counter()
+    graph = make_graph(mm, wl)
+    t_gen = time.perf_counter() - t0
+    k, a0, nX = wl["k"], wl["alpha0"], graph.parts[0]
+    rng = np.random.default_rng(wl["seed"])
+    phi0 = O.polar(rng.standard_normal((k, k)))
+    forms, res = {}, {}
+    y64 = wh = None
+    for name, prec in (("fp32", mm.PREC_FP32), ("bf16", mm.PREC_BF16)):
+        cfg = mm.default_config(k=k, alpha0=a0, stpm_method=mm.STPM_ONLINE, sweeps=wl["sweeps"],
+                                minibatch=wl["minibatch"], seed=wl["seed"], device=local, tau=0.1,
+                                precision=prec)
+        with mm.Pipeline(cfg) as p:
+            p.upload(graph)
+            runs = []
+            for rep in range(1 + max(1, args.steps)):
+                p.flush_l2()
+                p.synchronize()
+                p.whiten()
+                w_ms = p.stats()["whiten_ms"]
+                p.stpm(phi0)
+                s_ms = p.stats()["stpm_ms"]
+                p.postproc()
+                st = p.stats()
+                if rep > 0:
+                    runs.append((w_ms, s_ms, st["post_ms"]))
+            step = statistics.median(sum(r) for r in runs)
+            forms[name] = {"value": nX * wl["sweeps"] / (step / 1e3), "unit": "node-updates/s",
+                           "ms_per_step": step,
+                           "stages_ms": {"whiten_ms": statistics.median(r[0] for r in runs),
+                                         "stpm_ms": statistics.median(r[1] for r in runs),
+                                         "post_ms": statistics.median(r[2] for r in runs)}}
+            res[name] = (np.asarray(p.lam(), np.float64), np.asarray(p.phi(), np.float64), p.pi())
+            if y64 is None:
+                y64 = {n_: np.asarray(v, dtype=np.float64) for n_, v in p.whitened().items()}
+                wh = p.whitening()
+    t1 = time.perf_counter()
+    Gxa, _, _, Gba, Gca = graph.scipy_blocks()
+    lam_o, phi_o, _ = O.stpm_online(y64, a0, phi0, sweeps=wl["sweeps"], minibatch=wl["minibatch"])
+    _, pi_o = O.postprocess(Gxa, Gba, Gca, wh, lam_o, phi_o)
+    # the oracle's own response to a 1e-6 relative perturbation of y: how far
+    # Phi and Pi are determined by the data at this size (near-degenerate
+    # eigenvalues let Phi rotate inside their pairs)
+    yp = {n_: (v * (1 + 1e-6 * rng.standard_normal(v.shape)) if n_ in ("Da", "Db", "Dc") else v)
+          for n_, v in y64.items()}
+    lam_p, phi_p, _ = O.stpm_online(yp, a0, phi0, sweeps=wl["sweeps"], minibatch=wl["minibatch"])
+    del yp
+    _, pi_p = O.postprocess(Gxa, Gba, Gca, wh, lam_p, phi_p)
+    t_oracle = time.perf_counter() - t1
+    lam_sorted = np.sort(lam_o)
+
+    def residual(lam, phi):
+        """max_i |T(I, phi_i, phi_i) - lambda_i phi_i| / max_j lambda_j in FP64 over all of X."""
+        G = O.online_grad_terms(phi, y64, np.arange(nX), a0)
+        return float(np.linalg.norm(G - phi * lam, axis=0).max() / np.abs(lam).max())
+
+    def compare(lam, phi, pi):
+        perm, sign = _match(phi_o, phi)
+        e_pi = 0.0
+        for c0 in range(0, pi_o.shape[1], 1 << 20):
+            sl = slice(c0, c0 + (1 << 20))
+            e_pi = max(e_pi, float(np.abs(pi[perm, sl].astype(np.float64) - pi_o[:, sl]).max()))
+        return {"lambda_rel": float(np.linalg.norm(lam[perm] - lam_o) / np.linalg.norm(lam_o)),
+                "lambda_rel_sorted": float(np.linalg.norm(np.sort(lam) - lam_sorted)
+                                           / np.linalg.norm(lam_o)),
+                "phi_max": float(np.abs(phi[:, perm] * sign - phi_o).max()),
+                "pi_max": e_pi}
+
+    errors = {}
+    for name, r in res.items():
+        errors[name] = compare(*r)
+        errors[name]["eigen_residual"] = residual(r[0], r[1])
+    line = {
+        "metric": "stpm_node_updates_per_s", "value": forms["bf16"]["value"],
+        "unit": "node-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": 1,
+        "ms_per_step": forms["bf16"]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": wl["name"], **{k_: v for k_, v in wl.items() if k_ != "name"},
+                   "nnz_directed": int(sum(b.nnz for b in graph.blocks[:3]) * 2),
+                   "generation_s": t_gen},
+        "forms": forms, "bf16_over_fp32": forms["bf16"]["value"] / forms["fp32"]["value"],
+        "errors_vs_fp64": errors,
+        "oracle": {"seconds": t_oracle, "eigen_residual": residual(lam_o, phi_o),
+                   "sensitivity_to_1e-6_input_noise": compare(lam_p, phi_p, pi_p),
+                   "note": "FP64 STPM + post-processing on the device's whitening from the same "
+                           "Phi0; eigen_residual = max_i |T(I,phi_i,phi_i) - lambda_i phi_i| / "
+                           "max_j lambda_j over all of X"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -496,6 +624,8 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="override node count (testing)")
     ap.add_argument("--batch", action="store_true",
                     help="the batching configuration (256 graphs) instead of the default")
+    ap.add_argument("--precision", action="store_true",
+                    help="the precision configuration (n = 2M, k = 200, BF16 form vs FP32 vs FP64)")
     args = ap.parse_args()
     wl = dict(WORKLOAD)
     if args.n:
@@ -504,6 +634,9 @@ def main():
     ws, rank, local = dist_env()
     if args.batch and args.impl != "reference":
         run_batch(args, ws, rank, local)
+        return
+    if args.precision and args.impl != "reference":
+        run_precision(args, ws, rank, local)
         return
     if args.impl == "reference":
         run_reference(args, wl, ws, rank)

@@ -630,7 +630,8 @@ __global__ void __launch_bounds__(512, 1) stpm_step_batched(const StpmUpdateArgs
 //                                  ldmatrix.trans in BF16)
 //   d_i += sum_x Z1 Z2            (per column i)
 // The FP32 form keeps FP32 accuracy through the 3xTF32 split; the BF16 form
-// reads y and Phi rounded to BF16 and accumulates in FP32.
+// reads y rounded to BF16, Phi as a BF16 pair (hi + lo: Z = hi^T y + lo^T y,
+// two MMAs), the coefficients C rounded to BF16, and accumulates in FP32.
 template <int KP, int MODE, bool BF>
 struct Contract {
   using T = typename std::conditional<BF, __nv_bfloat16, float>::type;
@@ -649,8 +650,11 @@ struct Contract {
   static constexpr int MTJ = KP / 16, NTI = IB / 8;        // G tiles: j (16) x i (8)
   static constexpr int GT = MTJ * NTI, GPW = (GT + 7) / 8;  // G tiles, per warp
   static constexpr int KSTEP = BF ? 16 : 8;
+  // the BF16 form keeps Phi as a pair of BF16 arrays (hi + lo): rounding Phi
+  // itself to BF16 would bias every product Phi^T y of a step the same way
+  static constexpr int NPHI = BF ? 2 : 1;
   static constexpr size_t tile_bytes =
-      sizeof(T) * ((size_t)IB * PLD + (size_t)3 * TM * LDY + (size_t)NC * IB * LDC);
+      sizeof(T) * ((size_t)NPHI * IB * PLD + (size_t)3 * TM * LDY + (size_t)NC * IB * LDC);
   static constexpr size_t stage_bytes = sizeof(float) * ((size_t)KP * IB + 3 * IB + 4);
   static constexpr size_t region = ((tile_bytes > stage_bytes ? tile_bytes : stage_bytes) + 15) / 16 * 16;
   static constexpr size_t smem = region + sizeof(float) * (3 * IB + 8 + 8 * 3 * IB);
@@ -702,6 +706,7 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
   T* Phis = reinterpret_cast<T*>(smraw);  // Phis[ii PLD + j] = Phi_j,i0+ii (column i0+ii of Phi)
   T* Ys = Phis + IB * PLD;                // 3 node-major tiles: Ys[q TM LDY + x LDY + j]
   T* CT = Ys + 3 * TM * LDY;              // NC coefficient tiles, i-major: CT[c IB LDC + ii LDC + x]
+  T* PhiLo = CT + NC * IB * LDC;          // BF16 form: Phi - hi(Phi), same layout as Phis
   float* mv = reinterpret_cast<float*>(smraw + Cfg::region);  // m1 | m2 | m3 (IB each)
   float* tred = mv + 3 * IB;                                  // 8 loss partials
   float* dw = tred + 8;  // per-warp d-sums (3 IB each), summed in a fixed order at the end
@@ -720,7 +725,11 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
       }
 #pragma unroll
       for (int u = 0; u < B; ++u)
-        if (e0 + 256 * u < N) Phis[e0 + 256 * u] = to_elem<T>(v[u]);
+        if (e0 + 256 * u < N) {
+          const T hi = to_elem<T>(v[u]);
+          Phis[e0 + 256 * u] = hi;
+          if (BF) PhiLo[e0 + 256 * u] = to_elem<T>(v[u] - to_f32(hi));
+        }
     }
   }
   // m_P = Phi^T mu_P with Phi as staged (mu_1..3 staged in dw, which is
@@ -734,11 +743,17 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
   for (int e = tid; e < 3 * IB; e += 256) {
     const float* mu = dw + (e / IB) * KP;
     const T* ph = Phis + (e % IB) * PLD;
+    const T* pl = PhiLo + (e % IB) * PLD;
     float s0 = 0.f, s1 = 0.f;
 #pragma unroll 4
     for (int j = 0; j < KP; j += 2) {
-      s0 = fmaf(to_f32(ph[j]), mu[j], s0);
-      s1 = fmaf(to_f32(ph[j + 1]), mu[j + 1], s1);
+      float p0 = to_f32(ph[j]), p1 = to_f32(ph[j + 1]);
+      if (BF) {
+        p0 += to_f32(pl[j]);
+        p1 += to_f32(pl[j + 1]);
+      }
+      s0 = fmaf(p0, mu[j], s0);
+      s1 = fmaf(p1, mu[j + 1], s1);
     }
     mv[e] = s0 + s1;
   }
@@ -806,13 +821,17 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
 #pragma unroll 2
         for (int k0 = 0; k0 < KP; k0 += 16) {
           const T* pa = Phis + m0 * PLD + k0 + 2 * t4;
+          const T* pl = PhiLo + m0 * PLD + k0 + 2 * t4;
           const uint32_t af[4] = {ld_b32(pa + g * PLD), ld_b32(pa + (g + 8) * PLD),
                                   ld_b32(pa + g * PLD + 8), ld_b32(pa + (g + 8) * PLD + 8)};
+          const uint32_t afl[4] = {ld_b32(pl + g * PLD), ld_b32(pl + (g + 8) * PLD),
+                                   ld_b32(pl + g * PLD + 8), ld_b32(pl + (g + 8) * PLD + 8)};
 #pragma unroll
           for (int q = 0; q < NZ; ++q) {
             const T* pb = Ys + q * TM * LDY + (n0 + g) * LDY + k0 + 2 * t4;
             const uint32_t bf[2] = {ld_b32(pb), ld_b32(pb + 8)};
             mma_bf16(z[q], af, bf);
+            mma_bf16(z[q], afl, bf);
           }
         }
       } else {
