@@ -120,6 +120,8 @@ _SIGS = {
     "mmsb_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(_P)]),
     "mmsb_destroy": (None, [_P]),
     "mmsb_upload_graph": (ctypes.c_int, [_P, ctypes.POINTER(Csr)]),
+    "mmsb_host_register": (ctypes.c_int, [_P, ctypes.c_size_t]),
+    "mmsb_host_unregister": (ctypes.c_int, [_P]),
     "mmsb_whiten": (ctypes.c_int, [_P, ctypes.POINTER(_D)]),
     "mmsb_stpm": (ctypes.c_int, [_P, _D]),
     "mmsb_postproc": (ctypes.c_int, [_P]),
@@ -283,6 +285,37 @@ class Graph:
     def scipy_blocks(self):
         return [b.to_scipy() for b in self.blocks]
 
+    def _arrays(self):
+        for b in self.blocks:
+            for a in (b.row_ptr, b.col_idx, b.val):
+                if a is not None and a.nbytes:
+                    yield a
+
+    def pin(self):
+        """Page-lock the blocks' host arrays (mmsb_host_register) so that
+        uploads copy them by direct DMA; undo with unpin()."""
+        for a in self._arrays():
+            pin_host(a)
+        return self
+
+    def unpin(self):
+        for a in self._arrays():
+            unpin_host(a)
+        return self
+
+
+def pin_host(a: np.ndarray):
+    """Page-lock a contiguous host array in place (mmsb_host_register)."""
+    if not a.flags["C_CONTIGUOUS"] and not a.flags["F_CONTIGUOUS"]:
+        raise ValueError("pin_host needs a contiguous array")
+    _check(lib().mmsb_host_register(a.ctypes.data, a.nbytes))
+    return a
+
+
+def unpin_host(a: np.ndarray):
+    _check(lib().mmsb_host_unregister(a.ctypes.data))
+    return a
+
 
 def generate(n, k, alpha0, p_in, p_out, seed=0, keep_pi=False) -> Graph:
     """Seeded synthetic MMSB graph (C++ generator in the library)."""
@@ -415,8 +448,14 @@ class Pipeline:
     def n_nodes(self):
         return int(lib().mmsb_num_nodes(self._h))
 
-    def pi(self):
-        out = np.zeros((self.k, self.n_nodes()), dtype=np.float32, order="F")
+    def pi(self, out=None):
+        """Memberships, k x N (column-major); out: a preallocated float32
+        array of that shape and order to fill (e.g. one pinned with pin_host)."""
+        shape = (self.k, self.n_nodes())
+        if out is None:
+            out = np.empty(shape, dtype=np.float32, order="F")
+        elif out.shape != shape or out.dtype != np.float32 or not out.flags["F_CONTIGUOUS"]:
+            raise ValueError(f"out must be a float32 column-major {shape} array")
         self._ck(lib().mmsb_get_pi(self._h, _fptr(out)))
         return out
 

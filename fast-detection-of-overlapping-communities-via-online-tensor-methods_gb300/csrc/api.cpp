@@ -158,6 +158,24 @@ mmsb_status mmsb_upload_graph(mmsb_ctx* c, const mmsb_csr blocks[MMSB_NUM_BLOCKS
   return guard(c, [&]() { pipeline_upload(c, blocks); });
 }
 
+mmsb_status mmsb_host_register(void* ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return MMSB_ERR_INVALID_ARG;
+  const cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  if (e == cudaSuccess) return MMSB_OK;
+  cudaGetLastError();
+  return e == cudaErrorInvalidValue || e == cudaErrorHostMemoryAlreadyRegistered
+             ? MMSB_ERR_INVALID_ARG
+             : MMSB_ERR_CUDA;
+}
+
+mmsb_status mmsb_host_unregister(void* ptr) {
+  if (!ptr) return MMSB_ERR_INVALID_ARG;
+  const cudaError_t e = cudaHostUnregister(ptr);
+  if (e == cudaSuccess) return MMSB_OK;
+  cudaGetLastError();
+  return e == cudaErrorHostMemoryNotRegistered ? MMSB_ERR_INVALID_ARG : MMSB_ERR_CUDA;
+}
+
 mmsb_status mmsb_whiten(mmsb_ctx* c, const double* const* sketches) {
   if (!c) return MMSB_ERR_INVALID_ARG;
   return guard(c, [&]() {

@@ -33,6 +33,10 @@ extern thread_local int64_t g_launch_count;
 // Y[n_rows x ld] (row-major) = alpha * G * P[n_cols x ld]; ld % 4 == 0.
 cudaError_t spmm_f32(const int64_t* rp, const int32_t* ci, const float* val, int64_t n_rows,
                      const float* P, int ld, float alpha, float* Y, cudaStream_t s);
+// Checks an uploaded block: ORs 1 into *bad for a decreasing row offset, 2
+// for a column index outside [0, n_cols).
+cudaError_t csr_validate(const int64_t* rp, const int32_t* ci, int64_t n_rows, int64_t n_cols,
+                         int64_t nnz, unsigned* bad, cudaStream_t s);
 // Transposed CSR (deterministic: columns sorted within each row).
 cudaError_t csr_transpose(const int64_t* rp, const int32_t* ci, const float* val, int64_t n_rows,
                           int64_t n_cols, int64_t nnz, int64_t* rpT, int32_t* ciT, float* valT,

@@ -9,6 +9,8 @@
 // are FP64.
 #include "common.cuh"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 
 namespace mmsb {
@@ -252,6 +254,132 @@ __global__ void __launch_bounds__(1024) chol_upper_kernel(int p, const double* _
 
 // ---- T = R^{-1} (upper), one warp per column ------------------------------------
 
+// The same factorisation on a cluster of CL CTAs, blocked by KB columns, for
+// p up to 512: column l of R lives in the shared memory of CTA l % CL.  Per
+// block J = [jb, jb + KB):
+//   1. every CTA gathers the (updated) diagonal block S_JJ through DSMEM and
+//      factors it (the drop rule of chol_upper_kernel, pivot by pivot);
+//   2. each CTA solves R_JJ^T X = S_J,l for its columns l past the block
+//      (forward substitution, zero where a pivot was dropped): row block J;
+//   3. after a cluster barrier every CTA gathers row block J and updates its
+//      columns: S[i, l] -= sum_{c in J} R[c, i] R[c, l], jb + KB <= i <= l.
+// Two cluster barriers per block (the second also orders every CTA's gather
+// of S_JJ before the owners overwrite those columns with R_JJ); the FP64
+// update (p^3 / 6 multiply-adds)
+// runs on CL SMs.  The steps equal the unblocked ones up to the order of the
+// FP64 sums.
+template <int CL, int KB>
+__global__ void __launch_bounds__(256) chol_upper_cluster_kernel(int p, const double* __restrict__ S,
+                                                                 int lds, double* __restrict__ R,
+                                                                 double drop2, unsigned* flags) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ double chs[];
+  const int rank = (int)cluster.block_rank();
+  const int ncl = (p + CL - 1) / CL;            // local columns: l = lc CL + rank
+  double* Rl = chs;                              // Rl[lc p + i]
+  double* BR = Rl + (size_t)ncl * p;             // row block: BR[c p + i] = R[jb + c, i]
+  __shared__ double DJ[KB * KB];                 // DJ[cc KB + c] = R[jb + c, jb + cc]
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int e = tid; e < ncl * p; e += nt) {
+    const int lc = e / p, i = e % p, l = lc * CL + rank;
+    Rl[e] = (l < p && i <= l) ? S[(int64_t)l * lds + i] : 0.0;
+  }
+  for (int jb = 0; jb < p; jb += KB) {
+    const int bs = min(KB, p - jb);
+    cluster.sync();  // the previous block's updates are complete everywhere
+    for (int e = tid; e < KB * KB; e += nt) {
+      const int c = e % KB, cc = e / KB;
+      double v = 0.0;
+      if (c <= cc && cc < bs) {
+        const int l = jb + cc;
+        v = cluster.map_shared_rank(Rl, l % CL)[(size_t)(l / CL) * p + jb + c];
+      }
+      DJ[e] = v;
+    }
+    __syncthreads();
+    if (warp == 0) {  // upper Cholesky of the diagonal block with the drop rule
+      for (int c = 0; c < bs; ++c) {
+        if (lane == 0) {
+          const double d = DJ[c * KB + c];
+          double r = 0.0;
+          if (d > drop2) {
+            r = sqrt(d);
+          } else if (!(d == d)) {
+            atomicOr(flags, kFlagNonFinite);
+          }
+          DJ[c * KB + c] = r;
+        }
+        __syncwarp();
+        const double r = DJ[c * KB + c];
+        for (int cc = c + 1 + lane; cc < bs; cc += 32) {
+          const double x = DJ[cc * KB + c];
+          DJ[cc * KB + c] = r > 0.0 ? x / r : 0.0;
+        }
+        __syncwarp();
+        for (int e = lane; e < KB * KB; e += 32) {
+          const int i = e % KB, cc = e / KB;
+          if (i > c && i <= cc && cc < bs) DJ[cc * KB + i] = fma(-DJ[i * KB + c], DJ[cc * KB + c], DJ[cc * KB + i]);
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    // row block J of this CTA's columns past the block: the forward
+    // substitution R_JJ^T x = S_J,l (a thread per column)
+    const int i0 = jb + bs;
+    for (int lc = tid; lc < ncl; lc += nt) {
+      const int l = lc * CL + rank;
+      if (l < i0 || l >= p) continue;
+      double* col = Rl + (size_t)lc * p + jb;
+      for (int c = 0; c < bs; ++c) {
+        double x = col[c];
+        for (int c2 = 0; c2 < c; ++c2) x = fma(-DJ[c * KB + c2], col[c2], x);
+        const double r = DJ[c * KB + c];
+        col[c] = r > 0.0 ? x / r : 0.0;
+      }
+    }
+    // every CTA has gathered S_JJ and row block J is complete everywhere;
+    // only now may the owners overwrite the block's own columns with R_JJ
+    cluster.sync();
+    for (int lc = tid; lc < ncl; lc += nt) {
+      const int l = lc * CL + rank;
+      if (l < jb || l >= i0) continue;
+      const int cc = l - jb;
+      double* col = Rl + (size_t)lc * p + jb;
+      for (int c = 0; c <= cc; ++c) col[c] = DJ[cc * KB + c];
+    }
+    if (i0 >= p) break;
+    for (int e = tid; e < bs * (p - i0); e += nt) {
+      const int c = e / (p - i0), i = i0 + e % (p - i0);
+      BR[(size_t)c * p + i] = cluster.map_shared_rank(Rl, i % CL)[(size_t)(i / CL) * p + jb + c];
+    }
+    __syncthreads();
+    // trailing update of this CTA's columns: a warp per column, lanes on rows
+    for (int lc = warp; lc < ncl; lc += nw) {
+      const int l = lc * CL + rank;
+      if (l < i0 || l >= p) continue;
+      double* col = Rl + (size_t)lc * p;
+      double rc[KB];
+#pragma unroll
+      for (int c = 0; c < KB; ++c) rc[c] = c < bs ? col[jb + c] : 0.0;
+      for (int i = i0 + lane; i <= l; i += 32) {
+        double x = col[i];
+#pragma unroll
+        for (int c = 0; c < KB; ++c) x = fma(-BR[(size_t)c * p + i], rc[c], x);
+        col[i] = x;
+      }
+    }
+    __syncthreads();
+  }
+  __syncthreads();  // the last block's copy of R_JJ is complete
+  for (int e = tid; e < ncl * p; e += nt) {
+    const int lc = e / p, i = e % p, l = lc * CL + rank;
+    if (l < p) R[(int64_t)l * p + i] = i <= l ? Rl[e] : 0.0;
+  }
+  cluster.sync();  // keep shared memory alive until every remote read is done
+}
+
 // Column j of T solves R t = e_j by back substitution in column (axpy) form:
 // for l = j..0: t_l = b_l / R_ll (0 where R_ll == 0), then b_i -= t_l R_il for
 // i < l.  Column l of R is contiguous, so each step is one coalesced axpy;
@@ -299,7 +427,6 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __res
                                                       unsigned* flags, int max_sweeps, float tol) {
   extern __shared__ float smem[];
   float* X = kSmem ? smem : gwork;  // column-major p x p
-  __shared__ int rot_count;
   __shared__ int order[512];
   __shared__ float nrm2[512];
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -310,15 +437,29 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __res
   int sweep = 0;
   // a group of 8 lanes per column pair: up to nt / 8 pairs of a round at once
   const int grp = tid >> 3, l8 = tid & 7, ngrp = nt >> 3;
+  // circle method: in round r, slot s pairs player a = 1 + (s - 1 + r) mod (m - 1)
+  // (player 0 for s = 0) with b = 1 + (m - 2 - s + r) mod (m - 1); both
+  // advance by one (wrapping inside 1 .. m - 1) from round to round.  A
+  // thread serves slots s = grp, grp + ngrp (up to m / 2 <= 256 slots).
+  const int w = m - 1;
+  auto wrap_next = [w](int v) { return v == w ? 1 : v + 1; };
   for (; sweep < max_sweeps; ++sweep) {
-    if (tid == 0) rot_count = 0;
-    __syncthreads();
+    int pa[2], pb[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int s = grp + h * ngrp;
+      pa[h] = s == 0 ? 0 : 1 + (s - 1) % w;
+      pb[h] = 1 + (m - 2 - s + 2 * w) % w;
+    }
+    int rotated = 0;  // any rotation by this thread's groups in this sweep
     for (int r = 0; r < m - 1; ++r) {
-      for (int s0 = 0; s0 < m / 2; s0 += ngrp) {
-        const int s = s0 + grp;
-        // circle method: player 0 fixed, the rest rotate by r
-        const int a = s == 0 ? 0 : 1 + ((s - 1 + r) % (m - 1));
-        const int b = 1 + ((m - 2 - s + r) % (m - 1));
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int s = grp + h * ngrp;
+        if (h * ngrp >= m / 2) break;  // uniform across the block
+        const int a = pa[h], b = pb[h];
+        if (s != 0) pa[h] = wrap_next(a);
+        pb[h] = wrap_next(b);
         const int i = min(a, b), j = max(a, b);
         const bool live = s < m / 2 && j < p;
         float* xi = X + (int64_t)(live ? i : 0) * p;
@@ -349,13 +490,12 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __res
             xi[u] = c * x - sn * y;
             xj[u] = sn * x + c * y;
           }
-          if (l8 == 0) atomicAdd(&rot_count, 1);
+          rotated = 1;
         }
       }
       __syncthreads();
     }
-    if (rot_count == 0) break;
-    __syncthreads();
+    if (!__syncthreads_or(rotated)) break;
   }
   // eigenvalue i = squared norm of column i
   for (int i = warp; i < p; i += nw) {
@@ -530,75 +670,204 @@ __global__ void __launch_bounds__(1024) cgs2_cols_kernel(int m, int p, const dou
   }
 }
 
+// The same CGS2 with the rows spread over a cluster of CL CTAs, so that the
+// FP64 work (about 4 m p^2 / 2 multiply-adds) runs on CL SMs instead of one.
+// CTA r keeps rows [r R, r R + R) of every finished column of Q in shared
+// memory; each projection pass forms partial dot products over its rows, the
+// cluster sums them (every CTA reads all partials through DSMEM, adding in
+// rank order, so all CTAs hold identical sums and take identical branches),
+// and each CTA updates its own rows.  Three cluster barriers per column
+// (pass 1 with |v|^2, pass 2, the final norm); the partial buffers alternate
+// so that a buffer is rewritten only after every CTA has read it.
+template <int CL>
+__global__ void __launch_bounds__(256) cgs2_cols_cluster_kernel(int m, int p,
+                                                                const double* __restrict__ P,
+                                                                int ldp, double* __restrict__ Q,
+                                                                int ldq, double tol) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ double csh[];
+  const int R = (m + CL - 1) / CL;                 // rows per CTA
+  const int rank = (int)cluster.block_rank();
+  const int r0 = rank * R, nr = max(0, min(R, m - r0));
+  double* Qs = csh;                                 // Qs[i R + rr] = Q[r0 + rr, i]
+  double* v = Qs + (size_t)R * p;                   // R
+  double* part = v + R;                             // 2 x (p + 1) partial sums
+  double* d = part + 2 * (p + 1);                   // p + 1 reduced sums
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  int buf = 0, kept = 0;
+  // partial sums of Q_i . v (i < cnt) and, with_norm, |v|^2 in slot cnt;
+  // then the cluster-wide sums into d[0 .. cnt]
+  auto reduce = [&](int cnt, bool with_norm) {
+    double* pb = part + buf * (p + 1);
+    for (int i = tid; i < cnt; i += nt) {
+      double s = 0.0;
+      for (int rr = 0; rr < nr; ++rr) s = fma(Qs[(size_t)i * R + rr], v[rr], s);
+      pb[i] = s;
+    }
+    if (with_norm && warp == 0) {
+      double s = 0.0;
+      for (int rr = lane; rr < nr; rr += 32) s = fma(v[rr], v[rr], s);
+#pragma unroll
+      for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+      if (lane == 0) pb[cnt] = s;
+    }
+    cluster.sync();
+    const int tot = cnt + (with_norm ? 1 : 0);
+    for (int i = tid; i < tot; i += nt) {
+      double s = 0.0;
+      for (int q = 0; q < CL; ++q) s += cluster.map_shared_rank(pb, q)[i];
+      d[i] = s;
+    }
+    buf ^= 1;
+    __syncthreads();
+  };
+  // v -= sum_{i < cnt} d_i Q_i over this CTA's rows (a warp per row)
+  auto subtract = [&](int cnt) {
+    for (int rr = warp; rr < nr; rr += nw) {
+      double s = 0.0;
+      for (int i = lane; i < cnt; i += 32) s = fma(d[i], Qs[(size_t)i * R + rr], s);
+#pragma unroll
+      for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+      if (lane == 0) v[rr] -= s;
+    }
+    __syncthreads();
+  };
+  for (int j = 0; j < p; ++j) {
+    for (int rr = tid; rr < nr; rr += nt) v[rr] = P[(int64_t)j * ldp + r0 + rr];
+    __syncthreads();
+    reduce(j, true);  // pass 1 dots and |v|^2
+    // the kept columns span R^m: the residual of v is round-off, about
+    // 1e-15 |v|, below tol whenever |v| < 1e10 tol, and the column is dropped
+    if (kept == m && sqrt(d[j]) < 1e10 * tol) {
+      for (int rr = tid; rr < nr; rr += nt) {
+        Qs[(size_t)j * R + rr] = 0.0;
+        Q[(int64_t)j * ldq + r0 + rr] = 0.0;
+      }
+      __syncthreads();
+      continue;
+    }
+    subtract(j);
+    reduce(j, false);  // pass 2
+    subtract(j);
+    reduce(0, true);   // |v|^2 after both passes
+    const double nn = sqrt(d[0]);
+    const double sc = nn > tol ? 1.0 / nn : 0.0;
+    for (int rr = tid; rr < nr; rr += nt) {
+      const double qv = v[rr] * sc;
+      Qs[(size_t)j * R + rr] = qv;
+      Q[(int64_t)j * ldq + r0 + rr] = qv;
+    }
+    if (nn > tol) ++kept;
+    __syncthreads();
+  }
+  cluster.sync();  // keep shared memory alive until every remote read is done
+}
+
+template <int CL>
+static cudaError_t launch_cgs2_cluster(int m, int p, const double* P, int ldp, double* Q, int ldq,
+                                       double tol, size_t sm, cudaStream_t s) {
+  static bool set = false;
+  if (!set) {
+    MMSB_CUDA_TRY(cudaFuncSetAttribute(cgs2_cols_cluster_kernel<CL>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    if (CL > 8)
+      MMSB_CUDA_TRY(cudaFuncSetAttribute(cgs2_cols_cluster_kernel<CL>,
+                                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    set = true;
+  }
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(CL);
+  lc.blockDim = dim3(256);
+  lc.dynamicSmemBytes = sm;
+  lc.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  lc.attrs = at;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, cgs2_cols_cluster_kernel<CL>, m, p, P, ldp, Q, ldq, tol);
+}
+
 // ---- Ogita-Aishima refinement of all eigenpairs (FP64) ------------------------------
 // Given A (n x n), X (approximate eigenvectors), R = I - X^T X and S = X^T A X,
 // computes E with X' = X + X E (Ogita & Aishima 2018, Algorithm 1); eigenvalue
 // estimates are written to lam.  One CTA (n <= 512).
 
-__global__ void __launch_bounds__(1024) oa_correction_kernel(int n, const double* __restrict__ A,
-                                                             const double* __restrict__ XtX,
-                                                             const double* __restrict__ S,
-                                                             double* __restrict__ E,
-                                                             double* __restrict__ lam,
-                                                             double* __restrict__ delta_state) {
+// Statistics (one CTA): lam_i = S_ii / (X^T X)_ii and the cluster threshold
+// delta = 2 (||S - diag(lam)|| + ||A|| ||I - X^T X||), spectral norms bounded by
+// the maximum column abs-sum (symmetric matrices) and ||A|| ~ max |lam_i|
+// (Frobenius norms would over-cluster by ~sqrt(n)).  A warp per column, lanes
+// along its contiguous rows.
+__global__ void __launch_bounds__(1024) oa_stats_kernel(int n, const double* __restrict__ XtX,
+                                                        const double* __restrict__ S,
+                                                        double* __restrict__ lam,
+                                                        double* __restrict__ delta_state) {
   __shared__ double red[3][32];
-  __shared__ double delta;
-  const int tid = threadIdx.x, nt = blockDim.x;
+  __shared__ double slam[512];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   for (int i = tid; i < n; i += nt) {
     const double xx = XtX[(int64_t)i * n + i];  // = 1 - R_ii
-    lam[i] = xx > 0.0 ? S[(int64_t)i * n + i] / xx : 0.0;
+    const double l = xx > 0.0 ? S[(int64_t)i * n + i] / xx : 0.0;
+    slam[i] = l;
+    lam[i] = l;
   }
   __syncthreads();
-  // spectral-norm bounds: ||M||_2 <= max column abs-sum for symmetric M,
-  // ||A||_2 ~ max |lambda| (Frobenius norms would over-cluster by ~sqrt(n))
   double fs = 0.0, fa = 0.0, fr = 0.0;
-  for (int j = tid; j < n; j += nt) {
+  for (int j = warp; j < n; j += nw) {
     double cs = 0.0, cr = 0.0;
-    for (int i = 0; i < n; ++i) {
+    for (int i = lane; i < n; i += 32) {
       const int64_t e = (int64_t)j * n + i;
-      cs += fabs(S[e] - (i == j ? lam[i] : 0.0));
+      cs += fabs(S[e] - (i == j ? slam[i] : 0.0));
       cr += fabs((i == j ? 1.0 : 0.0) - XtX[e]);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      cs += __shfl_xor_sync(0xffffffffu, cs, off);
+      cr += __shfl_xor_sync(0xffffffffu, cr, off);
     }
     fs = fmax(fs, cs);
     fr = fmax(fr, cr);
-    fa = fmax(fa, fabs(lam[j]));
+    fa = fmax(fa, fabs(slam[j]));
   }
-#pragma unroll
-  for (int off = 16; off; off >>= 1) {
-    fs = fmax(fs, __shfl_xor_sync(0xffffffffu, fs, off));
-    fa = fmax(fa, __shfl_xor_sync(0xffffffffu, fa, off));
-    fr = fmax(fr, __shfl_xor_sync(0xffffffffu, fr, off));
-  }
-  if ((tid & 31) == 0) {
-    red[0][tid >> 5] = fs;
-    red[1][tid >> 5] = fa;
-    red[2][tid >> 5] = fr;
+  if (lane == 0) {
+    red[0][warp] = fs;
+    red[1][warp] = fa;
+    red[2][warp] = fr;
   }
   __syncthreads();
   if (tid == 0) {
     double a = 0, b = 0, c = 0;
-    for (int w = 0; w < (nt >> 5); ++w) {
+    for (int w = 0; w < nw; ++w) {
       a = fmax(a, red[0][w]);
       b = fmax(b, red[1][w]);
       c = fmax(c, red[2][w]);
     }
-    delta = 2.0 * (a + b * c);
-    delta_state[0] = delta;  // reported for diagnostics
+    delta_state[0] = 2.0 * (a + b * c);
   }
-  __syncthreads();
-  const double dl = delta;
-  for (int64_t e = tid; e < (int64_t)n * n; e += nt) {
-    const int i = (int)(e % n), j = (int)(e / n);
-    const double r = (i == j ? 1.0 : 0.0) - XtX[e];
-    double v;
-    if (i == j) {
-      v = 0.5 * r;
-    } else {
-      const double gap = lam[j] - lam[i];
-      v = fabs(gap) > dl ? (S[e] + lam[j] * r) / gap : 0.5 * r;
-    }
-    E[e] = v;
+}
+
+// The correction E (Ogita & Aishima 2018, Algorithm 1): E_ii = R_ii / 2,
+// E_ij = (S_ij + lam_j R_ij) / (lam_j - lam_i) where |lam_j - lam_i| > delta,
+// else R_ij / 2, with R = I - X^T X.  One CTA row per column j (blockIdx.y),
+// spreading the n^2 FP64 divisions over the GPU.
+__global__ void __launch_bounds__(256) oa_correction_kernel(int n, const double* __restrict__ XtX,
+                                                            const double* __restrict__ S,
+                                                            double* __restrict__ E,
+                                                            const double* __restrict__ lam,
+                                                            const double* __restrict__ delta_state) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i >= n) return;
+  const int64_t e = (int64_t)j * n + i;
+  const double r = (i == j ? 1.0 : 0.0) - XtX[e];
+  double v = 0.5 * r;
+  if (i != j) {
+    const double gap = lam[j] - lam[i];
+    if (fabs(gap) > delta_state[0]) v = (S[e] + lam[j] * r) / gap;
   }
+  E[e] = v;
 }
 
 // columns of X reordered by descending lam (stable on ties by index)
@@ -788,9 +1057,56 @@ cudaError_t dgemm_small(bool ta, bool tb, int m, int n, int k, double alpha, con
   return cudaGetLastError();
 }
 
+template <int CL, int KB>
+static cudaError_t launch_chol_cluster(int p, const double* S, int lds, double* R, double drop2,
+                                       unsigned* flags, size_t sm, cudaStream_t s) {
+  static bool set = false;
+  if (!set) {
+    MMSB_CUDA_TRY(cudaFuncSetAttribute(chol_upper_cluster_kernel<CL, KB>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    if (CL > 8)
+      MMSB_CUDA_TRY(cudaFuncSetAttribute(chol_upper_cluster_kernel<CL, KB>,
+                                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    set = true;
+  }
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(CL);
+  lc.blockDim = dim3(256);
+  lc.dynamicSmemBytes = sm;
+  lc.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  lc.attrs = at;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, chol_upper_cluster_kernel<CL, KB>, p, S, lds, R, drop2, flags);
+}
+
 cudaError_t chol_upper_drop(int p, const double* S, int lds, double* R, double drop2,
                             unsigned* flags, cudaStream_t s) {
   if (p > 4096) return cudaErrorInvalidValue;
+  // p > 64: a 16-CTA cluster (8 where 16 cannot be co-scheduled) while the
+  // columns and one row block fit shared memory, else one CTA
+  constexpr int KB = 16;
+  static int wide = -1;
+  for (int cl : {16, 8}) {
+    if (p <= 64) break;
+    if (cl == 16 && wide == 0) continue;
+    const size_t sm = sizeof(double) * ((size_t)((p + cl - 1) / cl) + KB) * p;
+    if (sm > 200 * 1024) break;
+    cudaError_t e = cl == 16 ? launch_chol_cluster<16, KB>(p, S, lds, R, drop2, flags, sm, s)
+                             : launch_chol_cluster<8, KB>(p, S, lds, R, drop2, flags, sm, s);
+    if (e == cudaSuccess) {
+      if (cl == 16) wide = 1;
+      ++g_launch_count;
+      return e;
+    }
+    if (cl == 16 && wide == 1) return e;
+    cudaGetLastError();
+    if (cl == 16) wide = 0;
+  }
   chol_upper_kernel<<<1, 1024, sizeof(double) * p, s>>>(p, S, lds, R, drop2, flags);
   ++g_launch_count;
   return cudaGetLastError();
@@ -878,6 +1194,24 @@ cudaError_t axpy_f64(int64_t n, double a, const double* x, double* y, cudaStream
 cudaError_t mgs_cols(int m, int p, const double* P, int ldp, double* Q, int ldq, double tol,
                      cudaStream_t s) {
   if (m > 4096 || p > 4096) return cudaErrorInvalidValue;
+  // a 16-CTA cluster (8 where the device cannot co-schedule 16), else one CTA
+  static int wide = -1;
+  for (int cl : {16, 8}) {
+    if (cl == 16 && wide == 0) continue;
+    const int rows = (m + cl - 1) / cl;
+    const size_t smc = sizeof(double) * ((size_t)rows * p + rows + 3 * ((size_t)p + 1));
+    if (smc > 200 * 1024) break;
+    cudaError_t e = cl == 16 ? launch_cgs2_cluster<16>(m, p, P, ldp, Q, ldq, tol, smc, s)
+                             : launch_cgs2_cluster<8>(m, p, P, ldp, Q, ldq, tol, smc, s);
+    if (e == cudaSuccess) {
+      if (cl == 16) wide = 1;
+      ++g_launch_count;
+      return e;
+    }
+    if (cl == 16 && wide == 1) return e;
+    cudaGetLastError();
+    if (cl == 16) wide = 0;
+  }
   const size_t sm = sizeof(double) * ((size_t)9 * m + p);
   if (sm > 48 * 1024) return cudaErrorInvalidValue;
   cgs2_cols_kernel<<<1, 1024, sm, s>>>(m, p, P, ldp, Q, ldq, tol);
@@ -887,8 +1221,12 @@ cudaError_t mgs_cols(int m, int p, const double* P, int ldp, double* Q, int ldq,
 
 cudaError_t oa_correction(int n, const double* A, const double* XtX, const double* S, double* E,
                           double* lam, double* delta_state, cudaStream_t s) {
-  oa_correction_kernel<<<1, 1024, 0, s>>>(n, A, XtX, S, E, lam, delta_state);
-  ++g_launch_count;
+  (void)A;  // ||A|| enters through max |lam_i|
+  if (n > 512) return cudaErrorInvalidValue;
+  oa_stats_kernel<<<1, 1024, 0, s>>>(n, XtX, S, lam, delta_state);
+  oa_correction_kernel<<<dim3((unsigned)ceil_div(n, 256), (unsigned)n), 256, 0, s>>>(n, XtX, S, E,
+                                                                                    lam, delta_state);
+  g_launch_count += 2;
   return cudaGetLastError();
 }
 

@@ -268,6 +268,34 @@ cudaError_t spmm_f32(const int64_t* rp, const int32_t* ci, const float* val, int
   return launch_spmm<32>(rp, ci, val, n_rows, P, c4, alpha, Y, s);
 }
 
+// Input checks of an uploaded block (the transposes and SpMMs index with
+// these): bit 1 = a decreasing row offset, bit 2 = a column index outside
+// [0, n_cols).  Grid-stride over rows and nonzeros.
+__global__ void csr_validate_kernel(const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                    int64_t n_rows, int64_t n_cols, int64_t nnz,
+                                    unsigned* __restrict__ bad) {
+  unsigned f = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_rows; r += stride)
+    if (rp[r + 1] < rp[r]) f |= 1u;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nnz; j += stride) {
+    const int32_t c = ci[j];
+    if (c < 0 || (int64_t)c >= n_cols) f |= 2u;
+  }
+  f = __reduce_or_sync(0xffffffffu, f);
+  if (f && (threadIdx.x & 31) == 0) atomicOr(bad, f);
+}
+
+cudaError_t csr_validate(const int64_t* rp, const int32_t* ci, int64_t n_rows, int64_t n_cols,
+                         int64_t nnz, unsigned* bad, cudaStream_t s) {
+  const int T = 256;
+  const int64_t work = std::max(n_rows, nnz);
+  const unsigned G = (unsigned)std::max<int64_t>(1, std::min<int64_t>(kNumSMs * 8, ceil_div(work, T)));
+  csr_validate_kernel<<<G, T, 0, s>>>(rp, ci, n_rows, n_cols, nnz, bad);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
 cudaError_t csr_transpose(const int64_t* rp, const int32_t* ci, const float* val, int64_t n_rows,
                           int64_t n_cols, int64_t nnz, int64_t* rpT, int32_t* ciT, float* valT,
                           int32_t* scratch, cudaStream_t s) {

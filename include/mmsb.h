@@ -146,10 +146,21 @@ void mmsb_config_default(mmsb_config* cfg);
 mmsb_status mmsb_create(const mmsb_config* cfg, mmsb_ctx** out);
 void mmsb_destroy(mmsb_ctx* ctx);
 
-/* Copies the five blocks to the device and builds their transposes there.
+/* Copies the five blocks to the device, checks them there (row offsets
+ * non-decreasing, column indices inside the block) and builds their
+ * transposes.  A block that fails a check returns MMSB_ERR_INVALID_ARG and
+ * leaves the context without a graph.  Host buffers pinned with
+ * mmsb_host_register are copied at full link speed.
  * Replaces read_G_sparse x5 (CPU/IOfn.cpp:21-54; CommunityDetection.cpp:47-49,94-95)
  * and read_G (GPU/pre_proc.c:49-80). */
 mmsb_status mmsb_upload_graph(mmsb_ctx* ctx, const mmsb_csr blocks[MMSB_NUM_BLOCKS]);
+
+/* Page-locks (unlocks) an existing host buffer so that uploads from it and
+ * result downloads into it run as direct DMA instead of through staging
+ * copies.  No counterpart in the reference (its host path never leaves the
+ * CPU); a thin wrapper of cudaHostRegister / cudaHostUnregister. */
+mmsb_status mmsb_host_register(void* ptr, size_t bytes);
+mmsb_status mmsb_host_unregister(void* ptr);
 
 /* ---- pipeline stages ------------------------------------------------------ */
 

@@ -266,6 +266,50 @@ def test_errors_are_status_codes(mm, golden_cfg1):
         with pytest.raises(mm.MmsbError) as e:
             p.upload(bad)
         assert e.value.status == 1
+        # checked on the device: a column index past the block, a decreasing
+        # row offset; the context stays usable
+        good = g.graph(mm)
+        b0 = good.blocks[0]
+        ci = b0.col_idx.copy()
+        ci[b0.nnz // 2] = b0.n_cols
+        bad = g.graph(mm)
+        bad.blocks[0] = mm.CsrBlock(b0.n_rows, b0.n_cols, b0.row_ptr, ci)
+        with pytest.raises(mm.MmsbError, match="column index out of range") as e:
+            p.upload(bad)
+        assert e.value.status == 1
+        rp = b0.row_ptr.copy()
+        r = int(np.argmax(np.diff(rp) > 1))  # a row with two or more entries
+        rp[r + 1] = rp[r] - 1 if rp[r] > 0 else rp[r + 2] + 1
+        bad = g.graph(mm)
+        bad.blocks[0] = mm.CsrBlock(b0.n_rows, b0.n_cols, rp, b0.col_idx)
+        with pytest.raises(mm.MmsbError, match="decreasing row_ptr") as e:
+            p.upload(bad)
+        assert e.value.status == 1
+        with pytest.raises(mm.MmsbError) as e:
+            p.whiten()
+        assert e.value.status == 4  # a failed upload leaves no graph
+        p.upload(good).whiten()
+
+
+def test_pinned_upload_and_download_match(mm, golden_cfg1):
+    """Uploads from page-locked host arrays and downloads into a pinned
+    output give the same results as plain host memory."""
+    g = golden_cfg1
+    graph = g.graph(mm)
+    out = []
+    for pinned in (False, True):
+        with mm.Pipeline(k=g.k, alpha0=g.alpha0, stpm_method=mm.STPM_ONLINE, sweeps=2,
+                         minibatch=100, seed=4) as p:
+            if pinned:
+                graph.pin()
+                buf = mm.pin_host(np.empty((g.k, graph.n_nodes), np.float32, order="F"))
+            p.upload(graph).run()
+            out.append((p.pi(out=buf) if pinned else p.pi(), p.lam()))
+            if pinned:
+                graph.unpin()
+                mm.unpin_host(buf)
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
 
 
 def test_rank_deficient_graph(mm, oracle):
