@@ -419,84 +419,16 @@ __global__ void __launch_bounds__(256) trinv_upper_kernel(int p, const double* _
 
 // ---- one-sided Jacobi: eigenpairs of Y Y^T -------------------------------------
 
-template <bool kSmem>
-__global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __restrict__ Y,
-                                                      double* __restrict__ evals,
-                                                      double* __restrict__ evecs,
-                                                      float* __restrict__ gwork,
-                                                      unsigned* flags, int max_sweeps, float tol) {
-  extern __shared__ float smem[];
-  float* X = kSmem ? smem : gwork;  // column-major p x p
+// Eigenpairs from the converged columns of X (column-major, ld p): eigenvalue
+// = squared column norm, eigenvector = normalised column, sorted descending;
+// exactly zero columns are completed to an orthonormal basis.  Called by one
+// CTA (any block size that is a multiple of 32).
+__device__ void jacobi_finish(int p, const float* X, double* __restrict__ evals,
+                              double* __restrict__ evecs, unsigned* flags) {
   __shared__ int order[512];
   __shared__ float nrm2[512];
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-  for (int64_t e = tid; e < (int64_t)p * p; e += nt) X[e] = (float)Y[e];
-  const int m = p + (p & 1);  // players in the round-robin tournament
-  __syncthreads();
-  int sweep = 0;
-  // a group of 8 lanes per column pair: up to nt / 8 pairs of a round at once
-  const int grp = tid >> 3, l8 = tid & 7, ngrp = nt >> 3;
-  // circle method: in round r, slot s pairs player a = 1 + (s - 1 + r) mod (m - 1)
-  // (player 0 for s = 0) with b = 1 + (m - 2 - s + r) mod (m - 1); both
-  // advance by one (wrapping inside 1 .. m - 1) from round to round.  A
-  // thread serves slots s = grp, grp + ngrp (up to m / 2 <= 256 slots).
-  const int w = m - 1;
-  auto wrap_next = [w](int v) { return v == w ? 1 : v + 1; };
-  for (; sweep < max_sweeps; ++sweep) {
-    int pa[2], pb[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int s = grp + h * ngrp;
-      pa[h] = s == 0 ? 0 : 1 + (s - 1) % w;
-      pb[h] = 1 + (m - 2 - s + 2 * w) % w;
-    }
-    int rotated = 0;  // any rotation by this thread's groups in this sweep
-    for (int r = 0; r < m - 1; ++r) {
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int s = grp + h * ngrp;
-        if (h * ngrp >= m / 2) break;  // uniform across the block
-        const int a = pa[h], b = pb[h];
-        if (s != 0) pa[h] = wrap_next(a);
-        pb[h] = wrap_next(b);
-        const int i = min(a, b), j = max(a, b);
-        const bool live = s < m / 2 && j < p;
-        float* xi = X + (int64_t)(live ? i : 0) * p;
-        float* xj = X + (int64_t)(live ? j : 0) * p;
-        float al = 0.f, be = 0.f, ga = 0.f;
-        if (live) {
-#pragma unroll 4
-          for (int t = l8; t < p; t += 8) {
-            const float u = xi[t], v = xj[t];
-            al = fmaf(u, u, al);
-            be = fmaf(v, v, be);
-            ga = fmaf(u, v, ga);
-          }
-        }
-#pragma unroll
-        for (int off = 4; off; off >>= 1) {
-          al += __shfl_xor_sync(0xffffffffu, al, off);
-          be += __shfl_xor_sync(0xffffffffu, be, off);
-          ga += __shfl_xor_sync(0xffffffffu, ga, off);
-        }
-        if (live && fabsf(ga) > tol * sqrtf(al * be) && ga != 0.f) {
-          const float zeta = (be - al) / (2.f * ga);
-          const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-          const float c = rsqrtf(1.f + t * t), sn = c * t;
-#pragma unroll 4
-          for (int u = l8; u < p; u += 8) {
-            const float x = xi[u], y = xj[u];
-            xi[u] = c * x - sn * y;
-            xj[u] = sn * x + c * y;
-          }
-          rotated = 1;
-        }
-      }
-      __syncthreads();
-    }
-    if (!__syncthreads_or(rotated)) break;
-  }
   // eigenvalue i = squared norm of column i
   for (int i = warp; i < p; i += nw) {
     float s = 0.f;
@@ -579,7 +511,260 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __res
     __syncthreads();
     for (int u = tid; u < p; u += nt) evecs[(int64_t)r * p + u] = vsm[u] * wsm[0];
     __syncthreads();
+  }}
+
+template <bool kSmem>
+__global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __restrict__ Y,
+                                                      double* __restrict__ evals,
+                                                      double* __restrict__ evecs,
+                                                      float* __restrict__ gwork,
+                                                      unsigned* flags, int max_sweeps, float tol) {
+  extern __shared__ float smem[];
+  float* X = kSmem ? smem : gwork;  // column-major p x p
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int64_t e = tid; e < (int64_t)p * p; e += nt) X[e] = (float)Y[e];
+  const int m = p + (p & 1);  // players in the round-robin tournament
+  __syncthreads();
+  int sweep = 0;
+  // a group of 8 lanes per column pair: up to nt / 8 pairs of a round at once
+  const int grp = tid >> 3, l8 = tid & 7, ngrp = nt >> 3;
+  // circle method: in round r, slot s pairs player a = 1 + (s - 1 + r) mod (m - 1)
+  // (player 0 for s = 0) with b = 1 + (m - 2 - s + r) mod (m - 1); both
+  // advance by one (wrapping inside 1 .. m - 1) from round to round.  A
+  // thread serves slots s = grp, grp + ngrp (up to m / 2 <= 256 slots).
+  const int w = m - 1;
+  auto wrap_next = [w](int v) { return v == w ? 1 : v + 1; };
+  for (; sweep < max_sweeps; ++sweep) {
+    int pa[2], pb[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int s = grp + h * ngrp;
+      pa[h] = s == 0 ? 0 : 1 + (s - 1) % w;
+      pb[h] = 1 + (m - 2 - s + 2 * w) % w;
+    }
+    int rotated = 0;  // any rotation by this thread's groups in this sweep
+    for (int r = 0; r < m - 1; ++r) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int s = grp + h * ngrp;
+        if (h * ngrp >= m / 2) break;  // uniform across the block
+        const int a = pa[h], b = pb[h];
+        if (s != 0) pa[h] = wrap_next(a);
+        pb[h] = wrap_next(b);
+        const int i = min(a, b), j = max(a, b);
+        const bool live = s < m / 2 && j < p;
+        float* xi = X + (int64_t)(live ? i : 0) * p;
+        float* xj = X + (int64_t)(live ? j : 0) * p;
+        float al = 0.f, be = 0.f, ga = 0.f;
+        if (live) {
+#pragma unroll 4
+          for (int t = l8; t < p; t += 8) {
+            const float u = xi[t], v = xj[t];
+            al = fmaf(u, u, al);
+            be = fmaf(v, v, be);
+            ga = fmaf(u, v, ga);
+          }
+        }
+#pragma unroll
+        for (int off = 4; off; off >>= 1) {
+          al += __shfl_xor_sync(0xffffffffu, al, off);
+          be += __shfl_xor_sync(0xffffffffu, be, off);
+          ga += __shfl_xor_sync(0xffffffffu, ga, off);
+        }
+        if (live && fabsf(ga) > tol * sqrtf(al * be) && ga != 0.f) {
+          const float zeta = (be - al) / (2.f * ga);
+          const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+          const float c = rsqrtf(1.f + t * t), sn = c * t;
+#pragma unroll 4
+          for (int u = l8; u < p; u += 8) {
+            const float x = xi[u], y = xj[u];
+            xi[u] = c * x - sn * y;
+            xj[u] = sn * x + c * y;
+          }
+          rotated = 1;
+        }
+      }
+      __syncthreads();
+    }
+    if (!__syncthreads_or(rotated)) break;
   }
+  jacobi_finish(p, X, evals, evecs, flags);
+}
+
+// ---- one-sided Jacobi on a cluster (block round-robin) --------------------------
+//
+// The p columns form 16 blocks of b = ceil(p / 16) columns; CTA t of an
+// 8-CTA cluster holds two blocks in shared memory.  A sweep is 15 block rounds
+// of the circle method over the 16 blocks (every pair of blocks meets once);
+// in a block round each CTA rotates every column of its first block against
+// every column of its second (b rounds of b disjoint pairs), and in the first
+// block round of a sweep also the pairs inside each of its blocks.  So each
+// sweep visits every column pair once, as the cyclic method does, while all
+// rotations run on columns in local shared memory.  Between block rounds
+// each CTA pulls the two blocks of its next round from their holders through
+// DSMEM into its other buffer set (one cluster barrier per block round).
+// A pair group of 16 lanes rotates one pair; rotations use the same test and
+// formulas as jacobi_kernel.
+constexpr int kJcCtas = 8, kJcBlocks = 2 * kJcCtas, kJcLanes = 16;
+
+__host__ __device__ inline int jc_ld(int p) { return p + ((16 - p % 32) + 32) % 32; }  // == 16 mod 32
+__host__ __device__ inline int jc_b(int p) { return (p + kJcBlocks - 1) / kJcBlocks; }
+
+// blocks of CTA t in block round r (circle method, player 0 fixed)
+__device__ __forceinline__ void jc_players(int t, int r, int& a, int& b) {
+  constexpr int w = kJcBlocks - 1;
+  a = t == 0 ? 0 : 1 + ((t - 1 + r) % w);
+  b = 1 + ((kJcBlocks - 2 - t + r) % w);
+}
+
+__global__ void __launch_bounds__(512) jacobi_cluster_kernel(int p, const double* __restrict__ Y,
+                                                             double* __restrict__ evals,
+                                                             double* __restrict__ evecs,
+                                                             float* __restrict__ gwork,
+                                                             unsigned* flags, int max_sweeps,
+                                                             float tol) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) float jsm[];
+  const int ld = jc_ld(p), b = jc_b(p);
+  const int t = (int)cluster.block_rank();
+  // buffer set q holds slot 0 (first block) and slot 1 (second block)
+  auto slot = [&](int q, int sl) { return jsm + (size_t)(2 * q + sl) * b * ld; };
+  __shared__ int s_rot[2];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int grp = tid / kJcLanes, ln = tid % kJcLanes, ngrp = nt / kJcLanes;
+  auto ncols = [&](int x) { return max(0, min(b, p - x * b)); };
+  int cur = 0, pa, pb;
+  jc_players(t, 0, pa, pb);
+  for (int sl = 0; sl < 2; ++sl) {
+    const int x = sl ? pb : pa, nc = ncols(x);
+    float* dst = slot(0, sl);
+    for (int e = tid; e < b * ld; e += nt) {
+      const int c = e / ld, i = e % ld;
+      dst[e] = (c < nc && i < p) ? (float)Y[(int64_t)(x * b + c) * p + i] : 0.f;
+    }
+  }
+  if (tid == 0) s_rot[0] = s_rot[1] = 0;
+  __syncthreads();
+  // rotate column u against column v (both in local shared memory) if they
+  // are not yet orthogonal to tol; uniform shuffles across the warp
+  auto rotate = [&](float* u, float* v, bool live, int& rotated) {
+    float al = 0.f, be = 0.f, ga = 0.f;
+    if (live) {
+#pragma unroll 4
+      for (int i = ln; i < p; i += kJcLanes) {
+        const float x = u[i], y = v[i];
+        al = fmaf(x, x, al);
+        be = fmaf(y, y, be);
+        ga = fmaf(x, y, ga);
+      }
+    }
+#pragma unroll
+    for (int off = kJcLanes / 2; off; off >>= 1) {
+      al += __shfl_xor_sync(0xffffffffu, al, off);
+      be += __shfl_xor_sync(0xffffffffu, be, off);
+      ga += __shfl_xor_sync(0xffffffffu, ga, off);
+    }
+    if (live && fabsf(ga) > tol * sqrtf(al * be) && ga != 0.f) {
+      const float zeta = (be - al) / (2.f * ga);
+      const float tt = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+      const float c = rsqrtf(1.f + tt * tt), sn = c * tt;
+#pragma unroll 4
+      for (int i = ln; i < p; i += kJcLanes) {
+        const float x = u[i], y = v[i];
+        u[i] = c * x - sn * y;
+        v[i] = sn * x + c * y;
+      }
+      rotated = 1;
+    }
+  };
+  const int bp = b + (b & 1);  // players of the round-robin inside one block
+  bool go = true;
+  for (int sweep = 0; sweep < max_sweeps && go; ++sweep) {
+    int rotated = 0;
+    for (int r = 0; r < kJcBlocks - 1; ++r) {
+      float* A = slot(cur, 0);
+      float* B = slot(cur, 1);
+      const int na = ncols(pa), nb = ncols(pb);
+      if (r == 0) {  // pairs inside each block: groups [0, bp/2) block A, [bp/2, bp) block B
+        for (int rr = 0; rr < bp - 1; ++rr) {
+          for (int g0 = 0; g0 < bp; g0 += ngrp) {
+            const int g = g0 + grp, s = g % (bp / 2), side = g / (bp / 2);
+            int x, y;
+            {
+              const int w = bp - 1;
+              x = s == 0 ? 0 : 1 + ((s - 1 + rr) % w);
+              y = 1 + ((bp - 2 - s + rr) % w);
+            }
+            const int n = side ? nb : na;
+            const bool live = g < bp && x < n && y < n;
+            float* base = side ? B : A;
+            rotate(base + (size_t)(live ? x : 0) * ld, base + (size_t)(live ? y : 0) * ld, live,
+                   rotated);
+          }
+          __syncthreads();
+        }
+      }
+      for (int q = 0; q < b; ++q) {  // A[i] against B[(i + q) mod b]
+        for (int g0 = 0; g0 < b; g0 += ngrp) {
+          const int i = g0 + grp, j = (i + q) % b;
+          const bool live = i < b && i < na && j < nb;
+          rotate(A + (size_t)(live ? i : 0) * ld, B + (size_t)(live ? j : 0) * ld, live, rotated);
+        }
+        __syncthreads();
+      }
+      // end of the sweep: the cluster-wide decision travels with this barrier
+      const bool last = r == kJcBlocks - 2;
+      if (last) {
+        const int any = __syncthreads_or(rotated);
+        if (tid == 0) s_rot[sweep & 1] = any;
+      }
+      __threadfence_block();
+      cluster.sync();
+      if (last) {
+        int any = 0;
+        for (int q = 0; q < kJcCtas; ++q) any |= *cluster.map_shared_rank(&s_rot[sweep & 1], q);
+        if (!any || sweep + 1 >= max_sweeps) {
+          go = false;
+          break;  // every CTA decides alike; the blocks stay where they are
+        }
+      }
+      // pull the blocks of the next round from their holders into the other set
+      const int rn = (r + 1) % (kJcBlocks - 1);
+      int na2, nb2;
+      jc_players(t, rn, na2, nb2);
+      for (int sl = 0; sl < 2; ++sl) {
+        const int x = sl ? nb2 : na2;
+        int src = -1, ssl = 0;
+        for (int u = 0; u < kJcCtas; ++u) {
+          int ua, ub;
+          jc_players(u, r, ua, ub);
+          if (ua == x) { src = u; ssl = 0; }
+          if (ub == x) { src = u; ssl = 1; }
+        }
+        const float4* from = reinterpret_cast<const float4*>(cluster.map_shared_rank(slot(cur, ssl), src));
+        float4* to = reinterpret_cast<float4*>(slot(cur ^ 1, sl));
+        for (int e = tid; e < b * ld / 4; e += nt) to[e] = from[e];
+      }
+      cur ^= 1;
+      pa = na2;
+      pb = nb2;
+      __syncthreads();
+    }
+  }
+  // converged columns to the work array (column-major, ld p), then CTA 0
+  // forms the eigenpairs
+  for (int sl = 0; sl < 2; ++sl) {
+    const int x = sl ? pb : pa, nc = ncols(x);
+    const float* src = slot(cur, sl);
+    for (int e = tid; e < nc * p; e += nt) {
+      const int c = e / p, i = e % p;
+      gwork[(int64_t)(x * b + c) * p + i] = src[(size_t)c * ld + i];
+    }
+  }
+  __threadfence();
+  cluster.sync();
+  if (t == 0) jacobi_finish(p, gwork, evals, evecs, flags);
 }
 
 // ---- Gram-Schmidt of the columns of a small m x p FP64 matrix (one CTA) -------------
@@ -1129,6 +1314,33 @@ cudaError_t eig_from_factor(int p, const double* Y, double* evals, double* evecs
   // start (6 sweeps left 1e-3 off-diagonal mass at n = 200; 9-10 suffice)
   const int max_sweeps = 15;
   const float tol = 8.f * sqrtf((float)p) * 6e-8f;
+  // p >= 96: the 8-CTA cluster version while four blocks fit shared memory
+  if (p >= 96) {
+    const size_t smc = sizeof(float) * 4 * (size_t)jc_b(p) * jc_ld(p);
+    if (smc <= 200 * 1024) {
+      static bool set = false;
+      if (!set) {
+        MMSB_CUDA_TRY(cudaFuncSetAttribute(jacobi_cluster_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        set = true;
+      }
+      cudaLaunchConfig_t lc = {};
+      lc.gridDim = dim3(kJcCtas);
+      lc.blockDim = dim3(512);
+      lc.dynamicSmemBytes = smc;
+      lc.stream = s;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = kJcCtas;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      lc.attrs = at;
+      lc.numAttrs = 1;
+      ++g_launch_count;
+      return cudaLaunchKernelEx(&lc, jacobi_cluster_kernel, p, Y, evals, evecs, work, flags,
+                                max_sweeps, tol);
+    }
+  }
   if (sm <= 200 * 1024) {
     static bool attr_set = false;
     if (!attr_set) {
