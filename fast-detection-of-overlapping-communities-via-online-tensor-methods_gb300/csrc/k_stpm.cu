@@ -22,6 +22,8 @@
 // (orthogonality term, step, Newton-Schulz polar orthonormalisation) runs on
 // one cluster of KP / 8 CTAs exchanging column blocks by bulk copies.
 #include "common.cuh"
+
+#include <cstdlib>
 #include "k_stpm.cuh"
 
 #include <cooperative_groups.h>
@@ -1287,8 +1289,19 @@ int stpm_kp(int k) {
 }
 
 int stpm_partial_grid(int64_t count, bool bf16) {
-  const int64_t tiles = ceil_div(count, bf16 ? 64 : 32);
-  const int64_t g = std::max<int64_t>(1, std::min<int64_t>(tiles, 2 * kNumSMs));
+  // at least 64 nodes per CTA (two FP32 tiles, one BF16 tile): measured on
+  // 4,096-node minibatches at k = 100, 64 CTAs beat 128 (44 vs 53 us in FP32;
+  // staging Phi and the cluster reduction are per-CTA costs)
+  (void)bf16;
+  const int64_t tiles = ceil_div(count, 64);
+  // MMSB_CONTRACT_CTAS caps the contraction CTAs of single-graph runs (a
+  // tuning override; default 2 per SM)
+  static const int64_t cap = []() {
+    const char* e = std::getenv("MMSB_CONTRACT_CTAS");
+    const long v = e ? std::strtol(e, nullptr, 10) : 0;
+    return v > 0 ? (int64_t)v : (int64_t)2 * kNumSMs;
+  }();
+  const int64_t g = std::max<int64_t>(1, std::min<int64_t>(tiles, cap));
   return (int)round_up(g, kPartialCluster);
 }
 
