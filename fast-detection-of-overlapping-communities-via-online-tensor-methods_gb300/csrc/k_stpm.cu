@@ -650,7 +650,8 @@ struct Contract {
   static constexpr int PLD = KP + PAD, LDY = KP + PAD, LDC = TM + PAD;
   static constexpr int MTI = IB / 16, NTX = TM / 8;        // Z^T tiles: i (16) x nodes (8)
   static constexpr int MTJ = KP / 16, NTI = IB / 8;        // G tiles: j (16) x i (8)
-  static constexpr int GT = MTJ * NTI, GPW = (GT + 7) / 8;  // G tiles, per warp
+  static constexpr int NW = 16, NT = 32 * NW;               // warps, threads per CTA
+  static constexpr int GT = MTJ * NTI, GPW = (GT + NW - 1) / NW;  // G tiles, per warp
   static constexpr int KSTEP = BF ? 16 : 8;
   // the BF16 form keeps Phi as a pair of BF16 arrays (hi + lo): rounding Phi
   // itself to BF16 would bias every product Phi^T y of a step the same way
@@ -659,7 +660,7 @@ struct Contract {
       sizeof(T) * ((size_t)NPHI * IB * PLD + (size_t)3 * TM * LDY + (size_t)NC * IB * LDC);
   static constexpr size_t stage_bytes = sizeof(float) * ((size_t)KP * IB + 3 * IB + 4);
   static constexpr size_t region = ((tile_bytes > stage_bytes ? tile_bytes : stage_bytes) + 15) / 16 * 16;
-  static constexpr size_t smem = region + sizeof(float) * (3 * IB + 8 + 8 * 3 * IB);
+  static constexpr size_t smem = region + sizeof(float) * (3 * IB + NW + NW * 3 * IB);
   static_assert(NBC <= 4, "one loss slot per column block");
 };
 
@@ -710,39 +711,40 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
   T* CT = Ys + 3 * TM * LDY;              // NC coefficient tiles, i-major: CT[c IB LDC + ii LDC + x]
   T* PhiLo = CT + NC * IB * LDC;          // BF16 form: Phi - hi(Phi), same layout as Phis
   float* mv = reinterpret_cast<float*>(smraw + Cfg::region);  // m1 | m2 | m3 (IB each)
-  float* tred = mv + 3 * IB;                                  // 8 loss partials
-  float* dw = tred + 8;  // per-warp d-sums (3 IB each), summed in a fixed order at the end
+  constexpr int NW = Cfg::NW, NT = Cfg::NT;
+  float* tred = mv + 3 * IB;                                  // NW loss partials
+  float* dw = tred + NW;  // per-warp d-sums (3 IB each), summed in a fixed order at the end
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, g = lane >> 2, t4 = lane & 3;
   const int k = a.k;
 
   // Phi: loads issued in batches of 8 per thread so that their latencies overlap
   {
     constexpr int N = IB * PLD, B = 8;
-    for (int e0 = tid; e0 < N; e0 += 256 * B) {
+    for (int e0 = tid; e0 < N; e0 += NT * B) {
       float v[B];
 #pragma unroll
       for (int u = 0; u < B; ++u) {
-        const int e = e0 + 256 * u, i = i0 + e / PLD, j = e % PLD;
+        const int e = e0 + NT * u, i = i0 + e / PLD, j = e % PLD;
         v[u] = (e < N && i < k && j < k) ? __ldg(a.phi + (int64_t)i * k + j) : 0.f;
       }
 #pragma unroll
       for (int u = 0; u < B; ++u)
-        if (e0 + 256 * u < N) {
+        if (e0 + NT * u < N) {
           const T hi = to_elem<T>(v[u]);
-          Phis[e0 + 256 * u] = hi;
-          if (BF) PhiLo[e0 + 256 * u] = to_elem<T>(v[u] - to_f32(hi));
+          Phis[e0 + NT * u] = hi;
+          if (BF) PhiLo[e0 + NT * u] = to_elem<T>(v[u] - to_f32(hi));
         }
     }
   }
   // m_P = Phi^T mu_P with Phi as staged (mu_1..3 staged in dw, which is
   // free until the d-sums start)
-  for (int e = tid; e < 3 * KP; e += 256) {
+  for (int e = tid; e < 3 * KP; e += NT) {
     const int which = e / KP, j = e % KP;
     const float* mu = which == 0 ? a.mu1 : which == 1 ? a.mu2 : a.mu3;
     dw[e] = (mu && j < k) ? mu[j] : 0.f;
   }
   __syncthreads();
-  for (int e = tid; e < 3 * IB; e += 256) {
+  for (int e = tid; e < 3 * IB; e += NT) {
     const float* mu = dw + (e / IB) * KP;
     const T* ph = Phis + (e % IB) * PLD;
     const T* pl = PhiLo + (e % IB) * PLD;
@@ -760,8 +762,8 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
     mv[e] = s0 + s1;
   }
   __syncthreads();
-  for (int e = tid; e < 8 * 3 * IB; e += 256) dw[e] = 0.f;
-  if (tid < 8) tred[tid] = 0.f;
+  for (int e = tid; e < NW * 3 * IB; e += NT) dw[e] = 0.f;
+  if (tid < NW) tred[tid] = 0.f;
   __syncthreads();
 
   float gacc[Cfg::GPW][4];
@@ -781,11 +783,11 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
     constexpr int CH = 16 / (int)sizeof(T), NCH = KP / CH;
     {
       constexpr int N = 3 * TM * NCH, B = 4;
-      for (int e0 = tid; e0 < N; e0 += 256 * B) {
+      for (int e0 = tid; e0 < N; e0 += NT * B) {
         uint4 v[B];
 #pragma unroll
         for (int u = 0; u < B; ++u) {
-          const int e = e0 + 256 * u;
+          const int e = e0 + NT * u;
           const int q = e / (TM * NCH), rem = e % (TM * NCH), xx = rem / NCH, c = rem % NCH;
           v[u] = make_uint4(0u, 0u, 0u, 0u);
           if (e < N) {
@@ -802,7 +804,7 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
         }
 #pragma unroll
         for (int u = 0; u < B; ++u) {
-          const int e = e0 + 256 * u;
+          const int e = e0 + NT * u;
           if (e >= N) break;
           const int q = e / (TM * NCH), rem = e % (TM * NCH), xx = rem / NCH, c = rem % NCH;
           *reinterpret_cast<uint4*>(Ys + q * TM * LDY + xx * LDY + c * CH) = v[u];
@@ -812,7 +814,7 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
     __syncthreads();
 
     // ---- Z^T tiles (16 i x 8 x), C and the d-sums
-    for (int p = warp; p < Cfg::MTI * Cfg::NTX; p += 8) {
+    for (int p = warp; p < Cfg::MTI * Cfg::NTX; p += NW) {
       const int m0 = (p % Cfg::MTI) * 16, n0 = (p / Cfg::MTI) * 8;
       float z[NZ][4];
 #pragma unroll
@@ -925,7 +927,7 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
       for (int k0 = 0; k0 < TM; k0 += Cfg::KSTEP) {
 #pragma unroll
         for (int u = 0; u < Cfg::GPW; ++u) {
-          const int tt = warp + 8 * u;
+          const int tt = warp + NW * u;
           if (tt >= Cfg::GT) continue;
           const int m0 = (tt % Cfg::MTJ) * 16, n0 = (tt / Cfg::MTJ) * 8;
 #pragma unroll
@@ -974,7 +976,7 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
   if (NC > 0) {
 #pragma unroll
     for (int u = 0; u < Cfg::GPW; ++u) {
-      const int tt = warp + 8 * u;
+      const int tt = warp + NW * u;
       if (tt >= Cfg::GT) continue;
       const int m0 = (tt % Cfg::MTJ) * 16, n0 = (tt / Cfg::MTJ) * 8;
 #pragma unroll
@@ -985,16 +987,16 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
     }
   }
   __syncthreads();
-  for (int e = tid; e < 3 * IB; e += 256) {
+  for (int e = tid; e < 3 * IB; e += NT) {
     float v = 0.f;
 #pragma unroll
-    for (int w = 0; w < 8; ++w) v += dw[w * 3 * IB + e];
+    for (int w = 0; w < NW; ++w) v += dw[w * 3 * IB + e];
     stage[KP * IB + e] = v;
   }
   if (tid == 0) {
     float t = 0.f;
     if (MODE == kModeLoss)
-      for (int w = 0; w < 8; ++w) t += tred[w];
+      for (int w = 0; w < NW; ++w) t += tred[w];
     stage[KP * IB + 3 * IB] = t;
   }
   cg::cluster_group cluster = cg::this_cluster();
@@ -1004,7 +1006,7 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
   cluster.sync();
   float* gp = a.gpart + (int64_t)(blockIdx.x / CLP) * a.part_stride;
   const int slice = (STAGE + CLP - 1) / CLP;
-  for (int e = crank * slice + tid; e < min(STAGE, (crank + 1) * slice); e += 256) {
+  for (int e = crank * slice + tid; e < min(STAGE, (crank + 1) * slice); e += NT) {
     float v = 0.f;
 #pragma unroll
     for (int q = 0; q < CLP; ++q) v += cluster.map_shared_rank(stage, q)[e];
@@ -1023,14 +1025,14 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
 }
 
 template <int KP, int MODE, bool BF>
-__global__ void __launch_bounds__(256) stpm_contract_kernel(StpmPartialArgs a) {
+__global__ void __launch_bounds__(Contract<KP, MODE, BF>::NT) stpm_contract_kernel(StpmPartialArgs a) {
   contract_body<KP, MODE, BF>(a, gridDim.x);
 }
 
 // blockIdx.y selects the graph; its first a.nblocks CTAs (a multiple of the
 // cluster size) work, the rest and graphs without nodes this round leave
 template <int KP, int MODE, bool BF>
-__global__ void __launch_bounds__(256) stpm_contract_batched(const StpmPartialArgs* __restrict__ args) {
+__global__ void __launch_bounds__(Contract<KP, MODE, BF>::NT) stpm_contract_batched(const StpmPartialArgs* __restrict__ args) {
   const StpmPartialArgs a = args[blockIdx.y];
   if ((int)blockIdx.x >= a.nblocks || a.count <= 0) return;
   contract_body<KP, MODE, BF>(a, a.nblocks);
@@ -1093,7 +1095,7 @@ cudaError_t launch_partial_t(const StpmPartialArgs& a, int grid, cudaStream_t s)
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid, (unsigned)Contract<KP, MODE, BF>::NBC, 1);
-  cfg.blockDim = dim3(256, 1, 1);
+  cfg.blockDim = dim3(Contract<KP, MODE, BF>::NT, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -1146,7 +1148,7 @@ cudaError_t launch_partial_batched_t(const StpmPartialArgs* args, int graphs, in
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid, (unsigned)graphs, 1);
-  cfg.blockDim = dim3(256, 1, 1);
+  cfg.blockDim = dim3(Contract<KP, MODE, BF>::NT, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
