@@ -71,6 +71,11 @@ cudaError_t dgemm_small(bool ta, bool tb, int m, int n, int k, double alpha, con
 // Upper Cholesky S = R^T R with drop tolerance: a pivot <= drop2 zeroes row j of R.
 cudaError_t chol_upper_drop(int p, const double* S, int lds, double* R, double drop2,
                             unsigned* flags, cudaStream_t s);
+// The same factorisation computed in FP32 (R stored as FP64), for a
+// well-conditioned S such as the Gram of an already orthonormalised panel;
+// pivots <= 0 are dropped.
+cudaError_t chol_upper_drop_f32(int p, const double* S, int lds, double* R, unsigned* flags,
+                                cudaStream_t s);
 // T = R^{-1} for upper triangular R (rows with R_jj == 0 -> zero rows/cols of T).
 cudaError_t trinv_upper(int p, const double* R, double* T, cudaStream_t s);
 // Eigen-decomposition of Z = Y Y^T from Y (p x p, column-major FP64): one-sided
@@ -80,7 +85,8 @@ cudaError_t eig_from_factor(int p, const double* Y, double* evals, double* evecs
 // Modified Gram-Schmidt of the columns of an m x p FP64 matrix (reference drop rule).
 cudaError_t mgs_cols(int m, int p, const double* P, int ldp, double* Q, int ldq, double tol,
                      cudaStream_t s);
-// Ogita-Aishima eigen refinement pieces (see k_dense.cu).
+// Ogita-Aishima eigen refinement pieces (see k_dense.cu); delta_state holds 4
+// doubles (the cluster threshold, then scratch for its three maxima).
 cudaError_t oa_correction(int n, const double* A, const double* XtX, const double* S, double* E,
                           double* lam, double* delta_state, cudaStream_t s);
 cudaError_t sort_eigen(int n, const double* lam, const double* X, double* evals, double* evecs,

@@ -268,29 +268,30 @@ __global__ void __launch_bounds__(1024) chol_upper_kernel(int p, const double* _
 // update (p^3 / 6 multiply-adds)
 // runs on CL SMs.  The steps equal the unblocked ones up to the order of the
 // FP64 sums.
-template <int CL, int KB>
-__global__ void __launch_bounds__(256) chol_upper_cluster_kernel(int p, const double* __restrict__ S,
+template <int CL, int KB, typename T>
+__global__ void __launch_bounds__(256, 1) chol_upper_cluster_kernel(int p, const double* __restrict__ S,
                                                                  int lds, double* __restrict__ R,
                                                                  double drop2, unsigned* flags) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
-  extern __shared__ double chs[];
+  extern __shared__ __align__(16) unsigned char chraw[];
+  T* chs = reinterpret_cast<T*>(chraw);
   const int rank = (int)cluster.block_rank();
   const int ncl = (p + CL - 1) / CL;            // local columns: l = lc CL + rank
-  double* Rl = chs;                              // Rl[lc p + i]
-  double* BR = Rl + (size_t)ncl * p;             // row block: BR[c p + i] = R[jb + c, i]
-  __shared__ double DJ[KB * KB];                 // DJ[cc KB + c] = R[jb + c, jb + cc]
+  T* Rl = chs;                                   // Rl[lc p + i]
+  T* BR = Rl + (size_t)ncl * p;                  // row block: BR[c p + i] = R[jb + c, i]
+  __shared__ T DJ[KB * KB];                 // DJ[cc KB + c] = R[jb + c, jb + cc]
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   for (int e = tid; e < ncl * p; e += nt) {
     const int lc = e / p, i = e % p, l = lc * CL + rank;
-    Rl[e] = (l < p && i <= l) ? S[(int64_t)l * lds + i] : 0.0;
+    Rl[e] = (l < p && i <= l) ? (T)S[(int64_t)l * lds + i] : (T)0;
   }
   for (int jb = 0; jb < p; jb += KB) {
     const int bs = min(KB, p - jb);
     cluster.sync();  // the previous block's updates are complete everywhere
     for (int e = tid; e < KB * KB; e += nt) {
       const int c = e % KB, cc = e / KB;
-      double v = 0.0;
+      T v = 0;
       if (c <= cc && cc < bs) {
         const int l = jb + cc;
         v = cluster.map_shared_rank(Rl, l % CL)[(size_t)(l / CL) * p + jb + c];
@@ -301,9 +302,9 @@ __global__ void __launch_bounds__(256) chol_upper_cluster_kernel(int p, const do
     if (warp == 0) {  // upper Cholesky of the diagonal block with the drop rule
       for (int c = 0; c < bs; ++c) {
         if (lane == 0) {
-          const double d = DJ[c * KB + c];
-          double r = 0.0;
-          if (d > drop2) {
+          const T d = DJ[c * KB + c];
+          T r = 0;
+          if (d > (T)drop2) {
             r = sqrt(d);
           } else if (!(d == d)) {
             atomicOr(flags, kFlagNonFinite);
@@ -311,10 +312,10 @@ __global__ void __launch_bounds__(256) chol_upper_cluster_kernel(int p, const do
           DJ[c * KB + c] = r;
         }
         __syncwarp();
-        const double r = DJ[c * KB + c];
+        const T r = DJ[c * KB + c];
         for (int cc = c + 1 + lane; cc < bs; cc += 32) {
-          const double x = DJ[cc * KB + c];
-          DJ[cc * KB + c] = r > 0.0 ? x / r : 0.0;
+          const T x = DJ[cc * KB + c];
+          DJ[cc * KB + c] = r > (T)0 ? x / r : (T)0;
         }
         __syncwarp();
         for (int e = lane; e < KB * KB; e += 32) {
@@ -331,12 +332,12 @@ __global__ void __launch_bounds__(256) chol_upper_cluster_kernel(int p, const do
     for (int lc = tid; lc < ncl; lc += nt) {
       const int l = lc * CL + rank;
       if (l < i0 || l >= p) continue;
-      double* col = Rl + (size_t)lc * p + jb;
+      T* col = Rl + (size_t)lc * p + jb;
       for (int c = 0; c < bs; ++c) {
-        double x = col[c];
+        T x = col[c];
         for (int c2 = 0; c2 < c; ++c2) x = fma(-DJ[c * KB + c2], col[c2], x);
-        const double r = DJ[c * KB + c];
-        col[c] = r > 0.0 ? x / r : 0.0;
+        const T r = DJ[c * KB + c];
+        col[c] = r > (T)0 ? x / r : (T)0;
       }
     }
     // every CTA has gathered S_JJ and row block J is complete everywhere;
@@ -346,7 +347,7 @@ __global__ void __launch_bounds__(256) chol_upper_cluster_kernel(int p, const do
       const int l = lc * CL + rank;
       if (l < jb || l >= i0) continue;
       const int cc = l - jb;
-      double* col = Rl + (size_t)lc * p + jb;
+      T* col = Rl + (size_t)lc * p + jb;
       for (int c = 0; c <= cc; ++c) col[c] = DJ[cc * KB + c];
     }
     if (i0 >= p) break;
@@ -359,12 +360,12 @@ __global__ void __launch_bounds__(256) chol_upper_cluster_kernel(int p, const do
     for (int lc = warp; lc < ncl; lc += nw) {
       const int l = lc * CL + rank;
       if (l < i0 || l >= p) continue;
-      double* col = Rl + (size_t)lc * p;
-      double rc[KB];
+      T* col = Rl + (size_t)lc * p;
+      T rc[KB];
 #pragma unroll
-      for (int c = 0; c < KB; ++c) rc[c] = c < bs ? col[jb + c] : 0.0;
+      for (int c = 0; c < KB; ++c) rc[c] = c < bs ? col[jb + c] : (T)0;
       for (int i = i0 + lane; i <= l; i += 32) {
-        double x = col[i];
+        T x = col[i];
 #pragma unroll
         for (int c = 0; c < KB; ++c) x = fma(-BR[(size_t)c * p + i], rc[c], x);
         col[i] = x;
@@ -375,7 +376,7 @@ __global__ void __launch_bounds__(256) chol_upper_cluster_kernel(int p, const do
   __syncthreads();  // the last block's copy of R_JJ is complete
   for (int e = tid; e < ncl * p; e += nt) {
     const int lc = e / p, i = e % p, l = lc * CL + rank;
-    if (l < p) R[(int64_t)l * p + i] = i <= l ? Rl[e] : 0.0;
+    if (l < p) R[(int64_t)l * p + i] = i <= l ? (double)Rl[e] : 0.0;
   }
   cluster.sync();  // keep shared memory alive until every remote read is done
 }
@@ -403,8 +404,11 @@ __global__ void __launch_bounds__(256) trinv_upper_kernel(int p, const double* _
     const double* rc = R + (int64_t)l * p;
     const double rll = rc[l];
     const double tl = rll != 0.0 ? bl / rll : 0.0;
+    // only slots holding rows i <= l take part: a warp-uniform branch per
+    // slot, so the FP64 pipe (~2 DFMA per clock per SM) does no dead work
 #pragma unroll
     for (int q = 0; q < kSlots; ++q) {
+      if (q > ql) break;
       const int i = lane + 32 * q;
       if (q == ql && lane == ll) b[q] = tl;
       if (i < l) b[q] = fma(-tl, rc[i], b[q]);
@@ -981,56 +985,38 @@ static cudaError_t launch_cgs2_cluster(int m, int p, const double* P, int ldp, d
 // computes E with X' = X + X E (Ogita & Aishima 2018, Algorithm 1); eigenvalue
 // estimates are written to lam.  One CTA (n <= 512).
 
-// Statistics (one CTA): lam_i = S_ii / (X^T X)_ii and the cluster threshold
-// delta = 2 (||S - diag(lam)|| + ||A|| ||I - X^T X||), spectral norms bounded by
-// the maximum column abs-sum (symmetric matrices) and ||A|| ~ max |lam_i|
-// (Frobenius norms would over-cluster by ~sqrt(n)).  A warp per column, lanes
-// along its contiguous rows.
-__global__ void __launch_bounds__(1024) oa_stats_kernel(int n, const double* __restrict__ XtX,
-                                                        const double* __restrict__ S,
-                                                        double* __restrict__ lam,
-                                                        double* __restrict__ delta_state) {
-  __shared__ double red[3][32];
-  __shared__ double slam[512];
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-  for (int i = tid; i < n; i += nt) {
-    const double xx = XtX[(int64_t)i * n + i];  // = 1 - R_ii
-    const double l = xx > 0.0 ? S[(int64_t)i * n + i] / xx : 0.0;
-    slam[i] = l;
-    lam[i] = l;
+// Statistics: lam_i = S_ii / (X^T X)_ii and the three maxima behind the
+// cluster threshold delta = 2 (||S - diag(lam)|| + ||A|| ||I - X^T X||):
+// spectral norms bounded by the maximum column abs-sum (symmetric matrices),
+// ||A|| ~ max |lam_i| (Frobenius norms would over-cluster by ~sqrt(n)).  A
+// warp per column, lanes along its contiguous rows, eight columns per CTA;
+// the maxima (non-negative, so their IEEE bit patterns order like the
+// values) are combined with atomicMax into mx[0..2], zeroed beforehand.
+__global__ void __launch_bounds__(256) oa_stats_kernel(int n, const double* __restrict__ XtX,
+                                                       const double* __restrict__ S,
+                                                       double* __restrict__ lam,
+                                                       unsigned long long* __restrict__ mx) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int j = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (j >= n) return;
+  const double xx = XtX[(int64_t)j * n + j];  // = 1 - R_jj
+  const double lj = xx > 0.0 ? S[(int64_t)j * n + j] / xx : 0.0;
+  double cs = 0.0, cr = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    const int64_t e = (int64_t)j * n + i;
+    cs += fabs(S[e] - (i == j ? lj : 0.0));
+    cr += fabs((i == j ? 1.0 : 0.0) - XtX[e]);
   }
-  __syncthreads();
-  double fs = 0.0, fa = 0.0, fr = 0.0;
-  for (int j = warp; j < n; j += nw) {
-    double cs = 0.0, cr = 0.0;
-    for (int i = lane; i < n; i += 32) {
-      const int64_t e = (int64_t)j * n + i;
-      cs += fabs(S[e] - (i == j ? slam[i] : 0.0));
-      cr += fabs((i == j ? 1.0 : 0.0) - XtX[e]);
-    }
 #pragma unroll
-    for (int off = 16; off; off >>= 1) {
-      cs += __shfl_xor_sync(0xffffffffu, cs, off);
-      cr += __shfl_xor_sync(0xffffffffu, cr, off);
-    }
-    fs = fmax(fs, cs);
-    fr = fmax(fr, cr);
-    fa = fmax(fa, fabs(slam[j]));
+  for (int off = 16; off; off >>= 1) {
+    cs += __shfl_xor_sync(0xffffffffu, cs, off);
+    cr += __shfl_xor_sync(0xffffffffu, cr, off);
   }
   if (lane == 0) {
-    red[0][warp] = fs;
-    red[1][warp] = fa;
-    red[2][warp] = fr;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    double a = 0, b = 0, c = 0;
-    for (int w = 0; w < nw; ++w) {
-      a = fmax(a, red[0][w]);
-      b = fmax(b, red[1][w]);
-      c = fmax(c, red[2][w]);
-    }
-    delta_state[0] = 2.0 * (a + b * c);
+    lam[j] = lj;
+    atomicMax(mx + 0, (unsigned long long)__double_as_longlong(cs));
+    atomicMax(mx + 1, (unsigned long long)__double_as_longlong(fabs(lj)));
+    atomicMax(mx + 2, (unsigned long long)__double_as_longlong(cr));
   }
 }
 
@@ -1042,15 +1028,19 @@ __global__ void __launch_bounds__(256) oa_correction_kernel(int n, const double*
                                                             const double* __restrict__ S,
                                                             double* __restrict__ E,
                                                             const double* __restrict__ lam,
-                                                            const double* __restrict__ delta_state) {
+                                                            const unsigned long long* __restrict__ mx,
+                                                            double* __restrict__ delta_state) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  const double dl = 2.0 * (__longlong_as_double((long long)mx[0]) +
+                           __longlong_as_double((long long)mx[1]) * __longlong_as_double((long long)mx[2]));
+  if (i == 0 && j == 0) delta_state[0] = dl;  // reported for diagnostics
   if (i >= n) return;
   const int64_t e = (int64_t)j * n + i;
   const double r = (i == j ? 1.0 : 0.0) - XtX[e];
   double v = 0.5 * r;
   if (i != j) {
     const double gap = lam[j] - lam[i];
-    if (fabs(gap) > delta_state[0]) v = (S[e] + lam[j] * r) / gap;
+    if (fabs(gap) > dl) v = (S[e] + lam[j] * r) / gap;
   }
   E[e] = v;
 }
@@ -1242,15 +1232,15 @@ cudaError_t dgemm_small(bool ta, bool tb, int m, int n, int k, double alpha, con
   return cudaGetLastError();
 }
 
-template <int CL, int KB>
+template <int CL, int KB, typename T>
 static cudaError_t launch_chol_cluster(int p, const double* S, int lds, double* R, double drop2,
                                        unsigned* flags, size_t sm, cudaStream_t s) {
   static bool set = false;
   if (!set) {
-    MMSB_CUDA_TRY(cudaFuncSetAttribute(chol_upper_cluster_kernel<CL, KB>,
+    MMSB_CUDA_TRY(cudaFuncSetAttribute(chol_upper_cluster_kernel<CL, KB, T>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     if (CL > 8)
-      MMSB_CUDA_TRY(cudaFuncSetAttribute(chol_upper_cluster_kernel<CL, KB>,
+      MMSB_CUDA_TRY(cudaFuncSetAttribute(chol_upper_cluster_kernel<CL, KB, T>,
                                          cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     set = true;
   }
@@ -1266,11 +1256,12 @@ static cudaError_t launch_chol_cluster(int p, const double* S, int lds, double* 
   at[0].val.clusterDim.z = 1;
   lc.attrs = at;
   lc.numAttrs = 1;
-  return cudaLaunchKernelEx(&lc, chol_upper_cluster_kernel<CL, KB>, p, S, lds, R, drop2, flags);
+  return cudaLaunchKernelEx(&lc, chol_upper_cluster_kernel<CL, KB, T>, p, S, lds, R, drop2, flags);
 }
 
-cudaError_t chol_upper_drop(int p, const double* S, int lds, double* R, double drop2,
-                            unsigned* flags, cudaStream_t s) {
+template <typename T>
+static cudaError_t chol_upper_drop_t(int p, const double* S, int lds, double* R, double drop2,
+                                     unsigned* flags, cudaStream_t s) {
   if (p > 4096) return cudaErrorInvalidValue;
   // p > 64: a 16-CTA cluster (8 where 16 cannot be co-scheduled) while the
   // columns and one row block fit shared memory, else one CTA
@@ -1279,10 +1270,10 @@ cudaError_t chol_upper_drop(int p, const double* S, int lds, double* R, double d
   for (int cl : {16, 8}) {
     if (p <= 64) break;
     if (cl == 16 && wide == 0) continue;
-    const size_t sm = sizeof(double) * ((size_t)((p + cl - 1) / cl) + KB) * p;
+    const size_t sm = sizeof(T) * ((size_t)((p + cl - 1) / cl) + KB) * p;
     if (sm > 200 * 1024) break;
-    cudaError_t e = cl == 16 ? launch_chol_cluster<16, KB>(p, S, lds, R, drop2, flags, sm, s)
-                             : launch_chol_cluster<8, KB>(p, S, lds, R, drop2, flags, sm, s);
+    cudaError_t e = cl == 16 ? launch_chol_cluster<16, KB, T>(p, S, lds, R, drop2, flags, sm, s)
+                             : launch_chol_cluster<8, KB, T>(p, S, lds, R, drop2, flags, sm, s);
     if (e == cudaSuccess) {
       if (cl == 16) wide = 1;
       ++g_launch_count;
@@ -1297,9 +1288,20 @@ cudaError_t chol_upper_drop(int p, const double* S, int lds, double* R, double d
   return cudaGetLastError();
 }
 
+cudaError_t chol_upper_drop(int p, const double* S, int lds, double* R, double drop2,
+                            unsigned* flags, cudaStream_t s) {
+  return chol_upper_drop_t<double>(p, S, lds, R, drop2, flags, s);
+}
+
+cudaError_t chol_upper_drop_f32(int p, const double* S, int lds, double* R, unsigned* flags,
+                                cudaStream_t s) {
+  return chol_upper_drop_t<float>(p, S, lds, R, 0.0, flags, s);
+}
+
 cudaError_t trinv_upper(int p, const double* R, double* T, cudaStream_t s) {
   if (p > 512) return cudaErrorInvalidValue;
-  const int warps = 8;
+  // two columns per CTA: the FP64 work spreads over ~p / 2 SMs
+  const int warps = 2;
   trinv_upper_kernel<<<(unsigned)ceil_div(p, warps), warps * 32, (size_t)warps * p * sizeof(double),
                        s>>>(p, R, T);
   ++g_launch_count;
@@ -1435,9 +1437,12 @@ cudaError_t oa_correction(int n, const double* A, const double* XtX, const doubl
                           double* lam, double* delta_state, cudaStream_t s) {
   (void)A;  // ||A|| enters through max |lam_i|
   if (n > 512) return cudaErrorInvalidValue;
-  oa_stats_kernel<<<1, 1024, 0, s>>>(n, XtX, S, lam, delta_state);
+  // delta_state[1..3] hold the three maxima (as bit patterns) between the kernels
+  unsigned long long* mx = reinterpret_cast<unsigned long long*>(delta_state + 1);
+  MMSB_CUDA_TRY(cudaMemsetAsync(mx, 0, 3 * sizeof(unsigned long long), s));
+  oa_stats_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(n, XtX, S, lam, mx);
   oa_correction_kernel<<<dim3((unsigned)ceil_div(n, 256), (unsigned)n), 256, 0, s>>>(n, XtX, S, E,
-                                                                                    lam, delta_state);
+                                                                                    lam, mx, delta_state);
   g_launch_count += 2;
   return cudaGetLastError();
 }

@@ -147,8 +147,8 @@ void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A
     ck(transpose_f64(n, R, Y, s), "eig R^T");
   }
   ck(eig_from_factor(n, Y, lam, X, work, c->flags, s), "jacobi");
-  double* dstate = c->tbuf<double>(tag + ".edelta", 1);
-  ck(cudaMemsetAsync(dstate, 0, sizeof(double), s), "delta");
+  double* dstate = c->tbuf<double>(tag + ".edelta", 4);  // delta + three maxima
+  ck(cudaMemsetAsync(dstate, 0, 4 * sizeof(double), s), "delta");
   for (int step = 0; step < 4; ++step) {
     ck(dgemm_small(true, false, n, n, n, 1.0, X, n, X, n, 0.0, G, n, s), "X^T X");
     ck(dgemm_small(false, false, n, n, n, 1.0, A, n, X, n, 0.0, AX, n, s), "A X");
@@ -200,7 +200,8 @@ Nys svd_sym_nystrom(mmsb_ctx* c, const std::string& tag, const float* A, int lda
   ck(trinv_upper(m, R1, T1, s), "trinv1");
   ck(panel_times_small(A, lda, m, n, T1, m, m, Q1, ldq, s), "Q1");
   ck(gram_tsk(Q1, ldq, m, Q1, ldq, m, n, 1.0, S2, part, cap, s), "gram2");
-  ck(chol_upper_drop(m, S2, m, R2, 1e-300, c->flags, s), "chol2");
+  // S2 = Q1^T Q1 is close to I: its factor needs no more than FP32 (Q1 itself is FP32)
+  ck(chol_upper_drop_f32(m, S2, m, R2, c->flags, s), "chol2");
   ck(dgemm_small(false, false, m, m, m, 1.0, R2, m, R1, m, 0.0, RA, m, s), "R_A");
   // Q_A = Q1 R2^{-1} with R2 ~ I: products with Q_A use Q1 and T2 = R2^{-1}
   double* T2 = c->tbuf<double>(tag + ".T2", (size_t)m * m);
