@@ -215,12 +215,12 @@ __device__ __forceinline__ void warp_tile_3xtf32(const float* __restrict__ pa,
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       ah[q] = tf32_round(av[q]);
-      al[q] = tf32_round(av[q] - __uint_as_float(ah[q]));
+      al[q] = __float_as_uint(av[q] - __uint_as_float(ah[q]));  // the MMA reads its top 19 bits
     }
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       bh[q] = tf32_round(bv[q]);
-      bl[q] = tf32_round(bv[q] - __uint_as_float(bh[q]));
+      bl[q] = __float_as_uint(bv[q] - __uint_as_float(bh[q]));
     }
     mma_tf32(c0, ah, bh);
     mma_tf32(c1, ah, bl);
@@ -690,9 +690,12 @@ __device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], const void* p) {
                : "r"(smem_addr(p)));
 }
 
+// v = hi + lo with hi rounded to TF32; lo is passed as full FP32 bits: a TF32
+// MMA reads only the top 19 bits of an operand, so lo enters truncated to
+// TF32 (|error| <= 2^-10 |lo| <= 2^-21 |v|) without a second conversion
 __device__ __forceinline__ void split_tf32(float v, uint32_t& hi, uint32_t& lo) {
   hi = tf32_round(v);
-  lo = tf32_round(v - __uint_as_float(hi));
+  lo = __float_as_uint(v - __uint_as_float(hi));
 }
 
 template <int KP, int MODE, bool BF>
