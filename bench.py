@@ -619,6 +619,65 @@ def run_precision(args, ws, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_io(args, ws, rank):
+    """The file contract on the default graph: its five blocks written as the
+    reference's COO text input (mmsb_write_coo) and read back by the parallel
+    reader in the reference's compat mode, on one host thread and on all (up
+    to 16), and the binary CSR container written and read; MB/s of text."""
+    if rank != 0:
+        return
+    import tempfile
+    mm = load_pkg()
+    wl = dict(WORKLOAD)
+    graph = make_graph(mm, wl)
+    res = {}
+    with tempfile.TemporaryDirectory() as td:
+        files = []
+        t0 = time.perf_counter()
+        for b, blk in enumerate(graph.blocks):
+            f = Path(td) / f"g{b}.txt"
+            mm.write_coo(f, blk)
+            files.append((f, blk.n_rows, blk.n_cols))
+        t_write = time.perf_counter() - t0
+        text_bytes = sum(f.stat().st_size for f, _, _ in files)
+        for threads in (1, 0):
+            env = dict(os.environ)
+            code = ("import sys, time, json; sys.path.insert(0, %r); import bench; mm = bench.load_pkg(); "
+                    "fs = json.loads(sys.argv[1]); ts = []\n"
+                    "for r in range(%d):\n"
+                    "    t0 = time.perf_counter()\n"
+                    "    for f, a, b in fs: mm.read_coo(f, a, b, compat=True)\n"
+                    "    ts.append(time.perf_counter() - t0)\n"
+                    "print(min(ts))") % (str(ROOT), max(1, args.steps))
+            if threads:
+                env["MMSB_IO_THREADS"] = str(threads)
+            else:
+                env.pop("MMSB_IO_THREADS", None)
+            out = subprocess.run([sys.executable, "-c", code, json.dumps([[str(f), a, b] for f, a, b in files])],
+                                 env=env, capture_output=True, text=True, check=True)
+            res["read_s_1thread" if threads else "read_s"] = float(out.stdout.strip().splitlines()[-1])
+        t0 = time.perf_counter()
+        for b, blk in enumerate(graph.blocks):
+            mm.write_csr(Path(td) / f"g{b}.csr", blk)
+        t_bw = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for b in range(len(graph.blocks)):
+            mm.read_csr(Path(td) / f"g{b}.csr")
+        t_br = time.perf_counter() - t0
+        bin_bytes = sum((Path(td) / f"g{b}.csr").stat().st_size for b in range(len(graph.blocks)))
+    mb = text_bytes / 1e6
+    line = {"metric": "coo_text_parse_MB_per_s", "value": mb / res["read_s"], "unit": "MB/s",
+            "n_gpus": 0, "steps": args.steps, "higher_is_better": True, "data": "synthetic",
+            "config": {"workload": wl["name"] + "-coo-files", "text_MB": mb,
+                       "nnz": int(sum(b.nnz for b in graph.blocks)), "threads": os.cpu_count()},
+            "parse_MB_per_s_1_thread": mb / res["read_s_1thread"],
+            "parallel_speedup": res["read_s_1thread"] / res["read_s"],
+            "write_coo_MB_per_s": mb / t_write,
+            "binary_csr": {"MB": bin_bytes / 1e6, "write_MB_per_s": bin_bytes / 1e6 / t_bw,
+                           "read_MB_per_s": bin_bytes / 1e6 / t_br}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -631,6 +690,8 @@ def main():
                     help="the batching configuration (256 graphs) instead of the default")
     ap.add_argument("--precision", action="store_true",
                     help="the precision configuration (n = 2M, k = 200, BF16 form vs FP32 vs FP64)")
+    ap.add_argument("--io", action="store_true",
+                    help="the file contract: COO text parse/write and binary CSR on the default graph")
     args = ap.parse_args()
     wl = dict(WORKLOAD)
     if args.n:
@@ -639,6 +700,9 @@ def main():
     ws, rank, local = dist_env()
     if args.batch and args.impl != "reference":
         run_batch(args, ws, rank, local)
+        return
+    if args.io and args.impl != "reference":
+        run_io(args, ws, rank)
         return
     if args.precision and args.impl != "reference":
         run_precision(args, ws, rank, local)

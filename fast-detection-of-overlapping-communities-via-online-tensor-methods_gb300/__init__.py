@@ -176,6 +176,14 @@ _SIGS = {
                                                ctypes.c_int64]),
     "mmsb_write_triplets_f64": (ctypes.c_int, [ctypes.c_char_p, _D, ctypes.c_int64,
                                                ctypes.c_int64]),
+    "mmsb_write_dense_f32": (ctypes.c_int, [ctypes.c_char_p, _F, ctypes.c_int64]),
+    "mmsb_write_dense_f64": (ctypes.c_int, [ctypes.c_char_p, _D, ctypes.c_int64]),
+    "mmsb_write_coo": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Csr)]),
+    "mmsb_write_csr": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Csr)]),
+    "mmsb_read_csr": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P)]),
+    "mmsb_pvalues": (ctypes.c_int, [_P, _F, ctypes.c_int32, _D, _D, _D]),
+    "mmsb_get_convergence": (ctypes.c_int, [_P, _D, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
+    "mmsb_write_gpu_outputs": (ctypes.c_int, [_P, ctypes.c_char_p]),
 }
 
 
@@ -344,12 +352,7 @@ def generate(n, k, alpha0, p_in, p_out, seed=0, keep_pi=False) -> Graph:
         L.mmsb_host_graph_free(h)
 
 
-def read_coo(path, n_rows, n_cols, datatype=0, compat=False) -> CsrBlock:
-    """read_G_sparse (IOfn.cpp:21-54); compat=True reproduces its quirks."""
-    L = lib()
-    h = _P()
-    _check(L.mmsb_read_coo(str(path).encode(), n_rows, n_cols, datatype, int(compat),
-                           ctypes.byref(h)))
+def _block_from_handle(L, h) -> CsrBlock:
     try:
         c = Csr()
         _check(L.mmsb_host_graph_block(h, 0, ctypes.byref(c)))
@@ -359,6 +362,46 @@ def read_coo(path, n_rows, n_cols, datatype=0, compat=False) -> CsrBlock:
         return CsrBlock(c.n_rows, c.n_cols, rp, ci, val)
     finally:
         L.mmsb_host_graph_free(h)
+
+
+def read_coo(path, n_rows, n_cols, datatype=0, compat=False) -> CsrBlock:
+    """read_G_sparse (IOfn.cpp:21-54) on up to 16 threads; compat=True
+    reproduces its loop exactly (see mmsb_read_coo)."""
+    L = lib()
+    h = _P()
+    _check(L.mmsb_read_coo(str(path).encode(), n_rows, n_cols, datatype, int(compat),
+                           ctypes.byref(h)))
+    return _block_from_handle(L, h)
+
+
+def write_coo(path, block: CsrBlock):
+    """The input contract: 1-based "row col[ value]" lines (mmsb_write_coo)."""
+    c = block.ctype()
+    _check(lib().mmsb_write_coo(str(path).encode(), ctypes.byref(c)))
+
+
+def write_csr(path, block: CsrBlock):
+    """Binary CSR container (mmsb_write_csr)."""
+    c = block.ctype()
+    _check(lib().mmsb_write_csr(str(path).encode(), ctypes.byref(c)))
+
+
+def read_csr(path) -> CsrBlock:
+    L = lib()
+    h = _P()
+    _check(L.mmsb_read_csr(str(path).encode(), ctypes.byref(h)))
+    return _block_from_handle(L, h)
+
+
+def write_dense(path, m):
+    """write_mat (GPU/post_proc.c:45-59): one "%5.25e" value per line, in
+    column-major order."""
+    m = np.asfortranarray(m)
+    if m.dtype == np.float32:
+        _check(lib().mmsb_write_dense_f32(str(path).encode(), m.ctypes.data_as(_F), m.size))
+    else:
+        m = np.asfortranarray(m, dtype=np.float64)
+        _check(lib().mmsb_write_dense_f64(str(path).encode(), m.ctypes.data_as(_D), m.size))
 
 
 def write_triplets(path, m):
@@ -458,6 +501,33 @@ class Pipeline:
             raise ValueError(f"out must be a float32 column-major {shape} array")
         self._ck(lib().mmsb_get_pi(self._h, _fptr(out)))
         return out
+
+    def pvalues(self, truth):
+        """Correlation, t statistic and two-sided p-value (Pvalue.cpp) of every
+        (estimated, true) community pair; truth: K x N memberships in the node
+        order [X|A|B|C].  Returns three k x K FP64 arrays."""
+        truth = np.asfortranarray(truth, dtype=np.float32)
+        K = truth.shape[0]
+        if truth.shape[1] != self.n_nodes():
+            raise ValueError("truth must be K x N")
+        out = [np.zeros((self.k, K), dtype=np.float64, order="F") for _ in range(3)]
+        self._ck(lib().mmsb_pvalues(self._h, _fptr(truth), K, *(o.ctypes.data_as(_D) for o in out)))
+        return tuple(out)
+
+    def convergence(self):
+        """Convergence trace of the last stpm (mmsb_get_convergence)."""
+        n = ctypes.c_int64()
+        self._ck(lib().mmsb_get_convergence(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.float64)
+        if n.value:
+            self._ck(lib().mmsb_get_convergence(self._h, out.ctypes.data_as(_D), n.value,
+                                                ctypes.byref(n)))
+        return out
+
+    def write_gpu_outputs(self, directory):
+        """The GPU tree's output files (mmsb_write_gpu_outputs)."""
+        self._ck(lib().mmsb_write_gpu_outputs(self._h, str(directory).encode()))
+        return self
 
     def sets(self):
         words = (self.k + 31) // 32

@@ -1,6 +1,9 @@
 // C ABI (include/mmsb.h).  Every entry point converts exceptions into a
 // status code and records the message in the context; nothing exits.
 #include <cmath>
+#include <cstdio>
+#include <string>
+#include <algorithm>
 #include <functional>
 #include <cstring>
 #include <memory>
@@ -230,6 +233,133 @@ mmsb_status mmsb_get_pi(mmsb_ctx* c, float* pi) {
   return guard(c, [&]() {
     d2h(c, pi, c->pi, sizeof(float) * (size_t)mmsb_num_nodes(c) * c->k);
     ck(cudaStreamSynchronize(c->s), "sync");
+  });
+}
+
+mmsb_status mmsb_pvalues(mmsb_ctx* c, const float* truth, int32_t k_true, double* corr,
+                         double* tstat, double* pval) {
+  if (!c || !truth || k_true < 1) return MMSB_ERR_INVALID_ARG;
+  if (!c->have_post) return MMSB_ERR_STATE;
+  return guard(c, [&]() {
+    const int k = c->k, K = k_true;
+    const int64_t N = mmsb_num_nodes(c);
+    if (N < 1) throw MmsbError(MMSB_ERR_STATE, "no nodes");
+    cudaStream_t s = c->s;
+    float* T = c->tbuf<float>("eval.truth", (size_t)N * K);
+    ck(cudaMemcpyAsync(T, truth, sizeof(float) * (size_t)N * K, cudaMemcpyHostToDevice, s), "H2D truth");
+    const int mx = std::max(k, K);
+    double* part = c->tbuf<double>("eval.part", colstats_partials(N, mx));
+    double* mean = c->tbuf<double>("eval.mean", (size_t)k + K);
+    double* var = c->tbuf<double>("eval.var", (size_t)k + K);
+    ck(column_stats(c->pi, k, k, N, part, mean, var, s), "stats");
+    ck(column_stats(T, K, K, N, part, mean + k, var + k, s), "stats");
+    float* Ac = c->tbuf<float>("eval.ac", (size_t)N * k);
+    float* Bc = c->tbuf<float>("eval.bc", (size_t)N * K);
+    ck(center_columns(c->pi, k, k, N, mean, Ac, s), "centre");
+    ck(center_columns(T, K, K, N, mean + k, Bc, s), "centre");
+    double* C = c->tbuf<double>("eval.c", (size_t)k * K);
+    const int64_t cap = (int64_t)gram_tsk_partials(N, k, K);
+    double* gp = c->tbuf<double>("eval.gram", (size_t)cap);
+    ck(gram_tsk(Ac, k, k, Bc, K, K, N, 1.0, C, gp, cap, s), "cross products");
+    double* out = c->tbuf<double>("eval.out", (size_t)3 * k * K);
+    const size_t kk = (size_t)k * K;
+    ck(pair_pvalues(C, k, K, N, var, var + k, out, out + kk, out + 2 * kk, c->flags, s), "p-values");
+    if (corr) d2h(c, corr, out, sizeof(double) * kk);
+    if (tstat) d2h(c, tstat, out + kk, sizeof(double) * kk);
+    if (pval) d2h(c, pval, out + 2 * kk, sizeof(double) * kk);
+    ck(cudaStreamSynchronize(s), "sync");
+    check_device_flags(c, "p-values");
+  });
+}
+
+mmsb_status mmsb_get_convergence(mmsb_ctx* c, double* out, int64_t cap, int64_t* count) {
+  if (!c || (cap > 0 && !out)) return MMSB_ERR_INVALID_ARG;
+  if (!c->have_phi) return MMSB_ERR_STATE;
+  return guard(c, [&]() {
+    if (count) *count = c->conv_count;
+    const int64_t n = std::min<int64_t>(std::max<int64_t>(cap, 0), c->conv_count);
+    if (n > 0) d2h(c, out, c->conv, sizeof(double) * (size_t)n);
+    ck(cudaStreamSynchronize(c->s), "sync");
+  });
+}
+
+mmsb_status mmsb_write_gpu_outputs(mmsb_ctx* c, const char* dir) {
+  if (!c || !dir) return MMSB_ERR_INVALID_ARG;
+  if (!c->have_post) return MMSB_ERR_STATE;
+  return guard(c, [&]() {
+    const int k = c->k;
+    const int64_t N = mmsb_num_nodes(c);
+    std::vector<float> pi((size_t)N * k), phi((size_t)k * k);
+    std::vector<double> lam(k), conv((size_t)c->conv_count);
+    d2h(c, pi.data(), c->pi, sizeof(float) * pi.size());
+    d2h(c, phi.data(), c->phi, sizeof(float) * phi.size());
+    d2h(c, lam.data(), c->lambda, sizeof(double) * k);
+    if (!conv.empty()) d2h(c, conv.data(), c->conv, sizeof(double) * conv.size());
+    ck(cudaStreamSynchronize(c->s), "sync");
+    // file names of GPU/stpm.h:82-91: <name>_<NCOM>_<ALPHA_0>_<LEARN_RATE>.txt
+    char tail[96];
+    std::snprintf(tail, sizeof(tail), "_%d_%g_%g.txt", k, c->cfg.alpha0, c->cfg.lr0);
+    auto path = [&](const char* name) { return std::string(dir) + "/" + name + tail; };
+    auto io = [&](mmsb_status st, const std::string& f) {
+      if (st != MMSB_OK) throw MmsbError(MMSB_ERR_IO, "writing " + f);
+    };
+    // Pi_X, Pi_A, Pi_B, Pi_C: k x n_P column-major slices of Pi (write_mat,
+    // GPU/post_proc.c:110-114)
+    const char* names[4] = {"Pi_X", "Pi_A", "Pi_B", "Pi_C"};
+    const int64_t part[4] = {c->nX, c->nA, c->nB, c->nC};
+    int64_t off = 0;
+    for (int q = 0; q < 4; ++q) {
+      const std::string f = path(names[q]);
+      io(mmsb_write_dense_f32(f.c_str(), pi.data() + off * k, part[q] * k), f);
+      off += part[q];
+    }
+    // evecs: Phi column-major; evals: the Dirichlet weights
+    // lambda_i^-2 / sum_j lambda_j^-2 (GPU/stpm.c:848-870)
+    {
+      const std::string f = path("evecs");
+      io(mmsb_write_dense_f32(f.c_str(), phi.data(), (int64_t)k * k), f);
+    }
+    std::vector<double> alpha(k);
+    double sum = 0.0;
+    for (int i = 0; i < k; ++i) {
+      alpha[i] = 1.0 / (lam[i] * lam[i]);
+      sum += alpha[i];
+    }
+    for (int i = 0; i < k; ++i) alpha[i] /= sum;
+    {
+      const std::string f = path("evals");
+      io(mmsb_write_dense_f64(f.c_str(), alpha.data(), k), f);
+    }
+    {
+      const std::string f = path("frob_norm");
+      io(mmsb_write_dense_f64(f.c_str(), conv.data(), (int64_t)conv.size()), f);
+    }
+    // sim_info (GPU/stpm.c:944-963), times in seconds of this library's stages
+    const std::string f = path("sim_info");
+    FILE* fp = std::fopen(f.c_str(), "w");
+    if (!fp) throw MmsbError(MMSB_ERR_IO, "writing " + f);
+    const bool online = c->cfg.stpm_method != MMSB_STPM_BATCH_POWER;
+    const int64_t per = online ? std::max<int64_t>(1, c->stats.stpm_steps / std::max(1, c->cfg.sweeps)) : 1;
+    const double pre = c->stats.whiten_ms / 1e3, stpm = c->stats.stpm_ms / 1e3, post = c->stats.post_ms / 1e3;
+    std::fprintf(fp, "Total number of nodes          = %d\n", (int)N);
+    std::fprintf(fp, "Number of nodes in partition X = %d\n", (int)c->nX);
+    std::fprintf(fp, "Number of nodes in partition A = %d\n", (int)c->nA);
+    std::fprintf(fp, "Number of nodes in partition B = %d\n", (int)c->nB);
+    std::fprintf(fp, "Number of nodes in partition C = %d\n", (int)c->nC);
+    std::fprintf(fp, "Number of nodes communities    = %d\n", k);
+    std::fprintf(fp, "Alpha_0 (Dirichlet parameter)  = %5.25e\n", c->cfg.alpha0);
+    std::fprintf(fp, "Learning rate = %5.25e\n", c->cfg.lr0);
+    std::fprintf(fp, "Threshold for STPM convergence    = %5.25e\n", c->cfg.tol);
+    std::fprintf(fp, "Pseudoinverse numerical tolerance = %5.25e\n", c->cfg.pinv_tol);
+    std::fprintf(fp, "Total number of Frob Norm values written to file = %d\n", (int)conv.size());
+    std::fprintf(fp, "Number of iterations between convergence test    = %d\n", (int)per);
+    std::fprintf(fp, "Maximum number of stochastic iterations allowed  = %d\n",
+                 (int)(online ? c->stats.stpm_steps : c->cfg.max_iter));
+    std::fprintf(fp, "Exec Time Pre Proc  = %5.25e (Seconds)\n", pre);
+    std::fprintf(fp, "Exec Time STPM      = %5.25e (Seconds)\n", stpm);
+    std::fprintf(fp, "Exec Time Post Proc = %5.25e (Seconds)\n", post);
+    std::fprintf(fp, "Total Exec Time     = %5.25e (Seconds)\n", pre + stpm + post);
+    if (std::fclose(fp) != 0) throw MmsbError(MMSB_ERR_IO, "writing " + f);
   });
 }
 

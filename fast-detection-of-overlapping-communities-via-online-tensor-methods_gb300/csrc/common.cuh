@@ -112,6 +112,8 @@ cudaError_t fill_f64(double* p, int64_t n, double v, cudaStream_t s);
 cudaError_t axpy_f64(int64_t n, double a, const double* x, double* y, cudaStream_t s);
 
 // ---- small element-wise helpers (k_misc.cu) -----------------------------------
+// *out = ||phi - snap||_F (FP64; out may be null), then snap = phi (n floats).
+cudaError_t phi_delta(int64_t n, const float* phi, float* snap, double* out, cudaStream_t s);
 
 cudaError_t sig_from_evals(int k, const double* ev, double* sig, cudaStream_t s);
 cudaError_t scale_cols_pinv(int rows, int k, double* F, int ldf, const double* sig, double tol,
@@ -135,5 +137,21 @@ cudaError_t mask_cols(int rows, int k, double* F, int ldf, const double* sig, do
 cudaError_t set_row_scaled(int rows, int cols, double* B, int ldb, int row, double alpha,
                            const double* v, cudaStream_t s);
 cudaError_t eye_mask(int m, int p, const double* R, int ldr, double* Q, int ldq, cudaStream_t s);
+
+// ---- ground-truth evaluation (k_eval.cu) --------------------------------------
+
+// Mean and population variance of each of the m columns of a node-major
+// n x m FP32 panel (ld), FP64; part holds colstats_partials(n, m) doubles.
+size_t colstats_partials(int64_t n, int m);
+cudaError_t column_stats(const float* X, int ld, int m, int64_t n, double* part, double* mean,
+                         double* var, cudaStream_t s);
+// Y (n x m, ld m) = X - mean per column, FP32.
+cudaError_t center_columns(const float* X, int ld, int m, int64_t n, const double* mean, float* Y,
+                           cudaStream_t s);
+// Correlation, t statistic and two-sided p-value (Pvalue.cpp:85-235) of every
+// pair from C = A_c^T B_c (k x K, column-major), n and the variances.
+cudaError_t pair_pvalues(const double* C, int k, int K, int64_t n, const double* va,
+                         const double* vb, double* corr, double* tstat, double* pval,
+                         unsigned* flags, cudaStream_t s);
 
 }  // namespace mmsb

@@ -54,6 +54,8 @@ struct mmsb_ctx {
   float* pi = nullptr;                        // N x k
   uint32_t* bits = nullptr;                   // N x words
   unsigned* flags = nullptr;                  // device status word
+  double* conv = nullptr;                     // convergence trace of the last mmsb_stpm
+  int64_t conv_count = 0;
   double* dscalar = nullptr;                  // device scalars (errors, losses)
 
   std::map<std::string, std::pair<void*, size_t>> ws;

@@ -1,5 +1,5 @@
-// Host-side graph handling: seeded MMSB generator, the reference's COO text
-// contract (reader and triplet writer) and the CSR container.
+// Host-side graph handling: seeded MMSB generator and the CSR container (the
+// file formats live in io.cpp).
 //
 // Generator (synthetic stand-in for the reference's data/ graphs):
 //   pi_i ~ Dirichlet(alpha0/k * 1);  B = q*J + (p-q)*I;
@@ -356,144 +356,4 @@ extern "C" mmsb_status mmsb_host_graph_pi(const mmsb_host_graph* g, float* pi) {
   if (!g || !pi || g->pi.empty()) return MMSB_ERR_INVALID_ARG;
   std::memcpy(pi, g->pi.data(), g->pi.size() * sizeof(float));
   return MMSB_OK;
-}
-
-// ---------------------------------------------------------------------------
-// COO text contract (CPU/IOfn.cpp:21-54)
-
-namespace {
-
-struct Scanner {
-  const char* p;
-  const char* e;
-  // skips whitespace; true if a number follows
-  bool number(double* x) {
-    while (p < e && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r' || *p == '\v' || *p == '\f'))
-      ++p;
-    if (p >= e) return false;
-    char* end = nullptr;
-    errno = 0;
-    double v = std::strtod(p, &end);
-    if (end == p) return false;
-    *x = v;
-    p = end;
-    return true;
-  }
-};
-
-}  // namespace
-
-extern "C" mmsb_status mmsb_read_coo(const char* path, int64_t n_rows, int64_t n_cols,
-                                     int32_t datatype, int32_t compat, mmsb_host_graph** out) {
-  if (!path || !out || n_rows < 0 || n_cols < 0 || n_rows > INT32_MAX || n_cols > INT32_MAX)
-    return MMSB_ERR_INVALID_ARG;
-  *out = nullptr;
-  FILE* f = std::fopen(path, "rb");
-  if (!f) return MMSB_ERR_IO;
-  std::string buf;
-  {
-    char tmp[1 << 16];
-    size_t got;
-    while ((got = std::fread(tmp, 1, sizeof(tmp), f)) > 0) buf.append(tmp, got);
-    std::fclose(f);
-  }
-  Scanner sc{buf.data(), buf.data() + buf.size()};
-  std::vector<int64_t> rows;
-  std::vector<int32_t> cols;
-  std::vector<float> vals;
-  const int per = datatype == 1 ? 3 : 2;
-  double t[3] = {0, 0, 1};
-  bool have_last = false;
-  for (;;) {
-    const char* before = sc.p;
-    int got = 0;
-    while (got < per && sc.number(&t[got])) ++got;
-    if (got == 0) {
-      // The reference loops while(!feof): anything after the last number
-      // (e.g. the final newline) lets one more iteration push the previous
-      // triplet again (IOfn.cpp:36-49).
-      if (compat && have_last && before < sc.e) {
-        rows.push_back(rows.back());
-        cols.push_back(cols.back());
-        vals.push_back(vals.back());
-      }
-      break;
-    }
-    if (got < per) {
-      if (!compat) return MMSB_ERR_IO;
-      break;
-    }
-    const int64_t r = (int64_t)t[0] - 1, c = (int64_t)t[1] - 1;
-    if (r < 0 || r >= n_rows || c < 0 || c >= n_cols) return MMSB_ERR_IO;
-    rows.push_back(r);
-    cols.push_back((int32_t)c);
-    vals.push_back(datatype == 1 ? (float)t[2] : 1.0f);
-    have_last = true;
-  }
-  std::unique_ptr<mmsb_host_graph> g(new mmsb_host_graph());
-  HostCsr m = csr_from_triplets(n_rows, n_cols, rows, cols, &vals, compat != 0);
-  if (compat) {
-    // prune(TOLERANCE): Eigen drops |v| <= 1e-6 * dummy_precision (1e-12)
-    HostCsr pr;
-    pr.n_rows = m.n_rows;
-    pr.n_cols = m.n_cols;
-    pr.row_ptr.assign(m.n_rows + 1, 0);
-    for (int64_t r = 0; r < m.n_rows; ++r) {
-      for (int64_t p = m.row_ptr[r]; p < m.row_ptr[r + 1]; ++p)
-        if (std::fabs((double)m.val[p]) > 1e-18) {
-          pr.col.push_back(m.col[p]);
-          pr.val.push_back(m.val[p]);
-        }
-      pr.row_ptr[r + 1] = (int64_t)pr.col.size();
-    }
-    m.row_ptr.swap(pr.row_ptr);
-    m.col.swap(pr.col);
-    m.val.swap(pr.val);
-  }
-  bool binary = true;
-  for (float v : m.val)
-    if (v != 1.0f) {
-      binary = false;
-      break;
-    }
-  if (binary) std::vector<float>().swap(m.val);
-  g->blocks[0] = std::move(m);
-  g->n_blocks = 1;
-  *out = g.release();
-  return MMSB_OK;
-}
-
-namespace {
-
-template <typename T>
-mmsb_status write_triplets(const char* path, const T* m, int64_t rows, int64_t cols) {
-  if (!path || (!m && rows * cols > 0)) return MMSB_ERR_INVALID_ARG;
-  FILE* f = std::fopen(path, "w");
-  if (!f) return MMSB_ERR_IO;
-  char line[96];
-  for (int64_t c = 0; c < cols; ++c)
-    for (int64_t r = 0; r < rows; ++r) {
-      const double v = (double)m[c * rows + r];
-      if (v == 0.0) continue;
-      // std::ostream default formatting == %g with 6 significant digits
-      int len = std::snprintf(line, sizeof(line), "%lld\t%lld\t%g\n", (long long)(r + 1),
-                              (long long)(c + 1), v);
-      if (std::fwrite(line, 1, (size_t)len, f) != (size_t)len) {
-        std::fclose(f);
-        return MMSB_ERR_IO;
-      }
-    }
-  return std::fclose(f) == 0 ? MMSB_OK : MMSB_ERR_IO;
-}
-
-}  // namespace
-
-extern "C" mmsb_status mmsb_write_triplets_f32(const char* path, const float* m, int64_t rows,
-                                               int64_t cols) {
-  return write_triplets(path, m, rows, cols);
-}
-
-extern "C" mmsb_status mmsb_write_triplets_f64(const char* path, const double* m, int64_t rows,
-                                               int64_t cols) {
-  return write_triplets(path, m, rows, cols);
 }

@@ -158,7 +158,36 @@ unsigned blocks(int64_t n, int T = 256) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(8 * kNumSMs, ceil_div(n, T)));
 }
 
+// ||Phi - snap||_F (FP64) into *out, then snap = Phi (one CTA): the
+// convergence trace of the online methods, one value per sweep
+__global__ void __launch_bounds__(256) phi_delta_kernel(int64_t n, const float* __restrict__ phi,
+                                                        float* __restrict__ snap,
+                                                        double* __restrict__ out) {
+  __shared__ double red[8];
+  double s = 0.0;
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+    const double d = (double)phi[e] - (double)snap[e];
+    s = fma(d, d, s);
+    snap[e] = phi[e];
+  }
+#pragma unroll
+  for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    if (out) *out = sqrt(t);
+  }
+}
+
 }  // namespace
+
+cudaError_t phi_delta(int64_t n, const float* phi, float* snap, double* out, cudaStream_t s) {
+  phi_delta_kernel<<<1, 256, 0, s>>>(n, phi, snap, out);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
 
 cudaError_t sig_from_evals(int k, const double* ev, double* sig, cudaStream_t s) {
   sig_from_evals_kernel<<<blocks(k), 256, 0, s>>>(k, ev, sig);

@@ -123,6 +123,8 @@ struct Nys {
 
 }  // namespace
 
+void check_device_flags(mmsb_ctx* c, const char* stage) { check_flags(c, stage); }
+
 // Symmetric positive semi-definite eigen-decomposition (n <= 512), eigenvalues
 // descending: FP32 one-sided Jacobi on the Cholesky factor (run to
 // convergence), then four FP64 Ogita-Aishima refinement steps (quadratic
@@ -790,10 +792,18 @@ void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
     const double p_main = p0 * inv_x, p_s1 = p2 * inv_x, p_s0 = p1;
     float* G = c->tbuf<float>("G", (size_t)k * k);
     double err = 0.0;
+    // ||Phi - Phi_old||_F of every iteration (the GPU tree's frob_norm file,
+    // GPU/stpm.c:743), up to its buffer size
+    constexpr int64_t kConvCap = 100000;
+    c->conv = c->tbuf<double>("conv", kConvCap);
+    c->conv_count = 0;
     for (int64_t it = 1;; ++it) {
       if (c->stop.load()) throw MmsbError(MMSB_ERR_STOPPED, "stop requested");
       stpm_pass(c, kModePlain, 1, 2, 0, 0, nx, p_main, p_s0, p_s1, 1.0, G, nullptr);
       ck(stpm_batch_update(k, c->phi, G, c->lambda, c->dscalar, s), "batch update");
+      if (c->conv_count < kConvCap)
+        ck(cudaMemcpyAsync(c->conv + c->conv_count++, c->dscalar, sizeof(double),
+                           cudaMemcpyDeviceToDevice, s), "trace");
       c->stats.stpm_steps = it;
       if (it >= c->cfg.min_iter) {
         ck(cudaMemcpyAsync(&err, c->dscalar, sizeof(double), cudaMemcpyDeviceToHost, s), "err");
@@ -809,11 +819,19 @@ void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
     return;
   }
   const int64_t rounds = stpm_online_rounds(c);
+  const int64_t per = std::max<int64_t>(1, rounds / std::max(1, c->cfg.sweeps));
+  // ||Phi - Phi at the previous sweep's end||_F after every sweep
+  float* snap = c->tbuf<float>("phi_snap", (size_t)k * k);
+  c->conv = c->tbuf<double>("conv", (size_t)std::max(1, c->cfg.sweeps));
+  c->conv_count = 0;
+  ck(phi_delta((int64_t)k * k, c->phi, snap, nullptr, s), "trace");
   OnlineRound rd;
   for (int64_t r = 0; r < rounds; ++r) {
     if (c->stop.load()) throw MmsbError(MMSB_ERR_STOPPED, "stop requested");
     stpm_online_round(c, r, &rd);
     stpm_step(c, rd);
+    if ((r + 1) % per == 0)
+      ck(phi_delta((int64_t)k * k, c->phi, snap, c->conv + c->conv_count++, s), "trace");
   }
   stpm_finish_online(c, rounds);
 }

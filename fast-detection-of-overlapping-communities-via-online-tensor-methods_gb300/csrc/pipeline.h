@@ -15,6 +15,8 @@ void ck(cudaError_t e, const char* what);
 
 // eigen-pairs (descending) of a symmetric PSD n x n device matrix (n <= 512)
 // factor: optional Y with A = Y Y^T (skips the Cholesky)
+// Reads and clears the device flag word; throws on a set flag (stage names it).
+void check_device_flags(mmsb_ctx* c, const char* stage);
 void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A, double* evals,
                      double* V, const double* factor = nullptr, cudaStream_t stream = nullptr);
 

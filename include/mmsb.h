@@ -191,6 +191,30 @@ int64_t mmsb_num_nodes(const mmsb_ctx* ctx); /* n_X + n_A + n_B + n_C */
 /* Normalised memberships, k x N column-major over the node order [X|A|B|C]
  * (CommunityDetection.cpp:121-139). */
 mmsb_status mmsb_get_pi(mmsb_ctx* ctx, float* pi);
+/* Ground-truth evaluation (CPU/Pvalue.cpp:85-235, the hypothesis test the
+ * reference ships for matching recovered to true communities): for every
+ * pair (i, j) of an estimated community i (row of Pi) and a true community j
+ * (row j of truth, a k_true x N column-major host array in the node order
+ * [X|A|B|C], e.g. data/Pi_true_*), the Pearson correlation over the N nodes,
+ * t = r sqrt((N-2)/(1-r^2)) and the two-sided p-value from the incomplete
+ * beta function with the reference's branch rules.  Outputs are k x k_true
+ * column-major FP64 (entry i + j k); any may be NULL.  Requires
+ * mmsb_postproc. */
+mmsb_status mmsb_pvalues(mmsb_ctx* ctx, const float* truth, int32_t k_true, double* corr,
+                         double* tstat, double* pval);
+/* Convergence trace of the last mmsb_stpm: batch power, ||Phi - Phi_old||_F
+ * of every iteration (the GPU tree's frob_norm values, GPU/stpm.c:743, up to
+ * 100000); online/adjoint, ||Phi - Phi at the previous sweep's end||_F after
+ * every sweep.  Copies min(cap, count) values; *count gets the total. */
+mmsb_status mmsb_get_convergence(mmsb_ctx* ctx, double* out, int64_t cap, int64_t* count);
+/* The GPU tree's output files (GPU/post_proc.c:110-114, GPU/stpm.c:915-963)
+ * into directory dir, named <name>_<k>_<alpha0>_<lr0>.txt as GPU/stpm.h:82-91:
+ * Pi_X, Pi_A, Pi_B, Pi_C (normalised Pi, k x n_P column-major), evecs (Phi,
+ * k x k column-major), evals (Dirichlet weights lambda^-2 / sum lambda^-2),
+ * frob_norm (the convergence trace) -- one "%5.25e" value per line -- and
+ * sim_info (sizes, parameters and stage times). */
+mmsb_status mmsb_write_gpu_outputs(mmsb_ctx* ctx, const char* dir);
+
 /* Community sets {i : pi(i,node) > tau}: N words of ceil(k/32) uint32 each. */
 mmsb_status mmsb_get_sets(mmsb_ctx* ctx, uint32_t* bits);
 mmsb_status mmsb_get_lambda(mmsb_ctx* ctx, double* lambda);  /* k */
@@ -302,12 +326,16 @@ mmsb_status mmsb_host_graph_pi(const mmsb_host_graph* g, float* pi);
 
 /* ---- file contract (CPU/IOfn.cpp:21-67) ----------------------------------- */
 
-/* Reads a 1-based COO text block ("row col" or "row col value" per line,
- * datatype 0/1).  compat != 0 reproduces the reference reader exactly:
- * the last triplet is pushed twice when the file ends after a newline
- * (IOfn.cpp:36-49 feof loop) and duplicates are summed, then entries with
- * |v| <= 1e-6 are pruned.  compat == 0 de-duplicates instead.  The block
- * is owned by a host graph handle freed with mmsb_host_graph_free. */
+/* Reads a 1-based COO text block ("row col" or "row col value", any
+ * whitespace, datatype 0/1), parsed on up to 16 threads.  compat != 0
+ * reproduces the reference reader (read_G_sparse, IOfn.cpp:21-54) exactly:
+ * its while(!feof) loop pushes the last triplet a second time unless the last
+ * number ends the file, completes a trailing partial triplet with the
+ * previous values, sums duplicates and prunes |v| <= 1e-18 (prune(1e-6)).
+ * compat == 0: no extra triplet, a partial triplet is an error, the last
+ * duplicate wins, nothing is pruned.  A non-number token is an error (the
+ * reference would loop forever).  The block is owned by a host graph handle
+ * freed with mmsb_host_graph_free. */
 mmsb_status mmsb_read_coo(const char* path, int64_t n_rows, int64_t n_cols,
                           int32_t datatype, int32_t compat, mmsb_host_graph** out);
 /* Writes "row\tcol\tvalue" 1-based triplets of the nonzeros of a column-major
@@ -317,6 +345,20 @@ mmsb_status mmsb_write_triplets_f32(const char* path, const float* m, int64_t ro
                                     int64_t cols);
 mmsb_status mmsb_write_triplets_f64(const char* path, const double* m, int64_t rows,
                                     int64_t cols);
+/* write_mat (GPU/post_proc.c:45-59): count values, one "%5.25e" per line. */
+mmsb_status mmsb_write_dense_f32(const char* path, const float* m, int64_t count);
+mmsb_status mmsb_write_dense_f64(const char* path, const double* m, int64_t count);
+/* A block in the input contract read by mmsb_read_coo: 1-based "row col"
+ * lines (val == NULL) or "row col value" (9 significant digits), row by row.
+ * No counterpart in the reference (it only reads this format). */
+mmsb_status mmsb_write_coo(const char* path, const mmsb_csr* m);
+/* Binary CSR container, no counterpart in the reference: "MMSBCSR" + version
+ * byte 1, int64 n_rows, n_cols, nnz, int32 has_values, int32 0, int64
+ * row_ptr[n_rows + 1], int32 col_idx[nnz], float val[nnz] if has_values,
+ * little-endian.  mmsb_read_csr checks the structure (offsets 0..nnz,
+ * non-decreasing, columns in range) and returns a host graph of one block. */
+mmsb_status mmsb_write_csr(const char* path, const mmsb_csr* m);
+mmsb_status mmsb_read_csr(const char* path, mmsb_host_graph** out);
 
 /* ---- batched solver (many independent graphs) ----------------------------
  * No counterpart in the reference, which solves one graph per process.  Each

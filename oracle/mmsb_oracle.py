@@ -319,3 +319,136 @@ def postprocess(Gxa, Gba, Gca, wh, lam, phi, tol=TOLERANCE):
 
 def community_sets(pi, tau):
     return pi > tau
+
+
+# ---- file contract and ground-truth evaluation ------------------------------
+
+def read_coo_reference(text, n_rows, n_cols, datatype=0):
+    """read_G_sparse (IOfn.cpp:21-54) on a COO text: the while(!feof) loop of
+    fscanf("%lf") reads "row col" (datatype 0) or "row col value" per pass.  A
+    read that meets the end of the file leaves its variable unchanged and sets
+    EOF; a number that ends exactly at the end of the file also sets EOF.  So
+    after the last complete triplet one more pass pushes the previous triplet
+    again unless the last number ended the file, and a trailing partial
+    triplet is completed with the previous values.  Triplets are summed
+    (setFromTriplets), then prune(1e-6) keeps |v| > 1e-18.  Returns CSR.
+    (Files shorter than one triplet and non-numbers are undefined behaviour in
+    the reference; they are rejected here with ValueError.)"""
+    toks, ends = [], []
+    for m in __import__("re").finditer(r"\S+", text):
+        toks.append(float(m.group(0)))
+        ends.append(m.end())
+    per = 3 if datatype == 1 else 2
+    if len(toks) < per:
+        raise ValueError("shorter than one triplet")
+    last_eof = ends[-1] == len(text)
+    trip, cur, i, eof = [], [None] * per, 0, False
+    while not eof:
+        for f in range(per):
+            if i < len(toks):
+                cur[f] = toks[i]
+                if i == len(toks) - 1 and last_eof:
+                    eof = True
+                i += 1
+            else:
+                eof = True
+        trip.append(tuple(cur))
+    r = np.array([int(t[0] - 1) for t in trip])
+    c = np.array([int(t[1] - 1) for t in trip])
+    v = np.array([t[2] if per == 3 else 1.0 for t in trip])
+    if (r < 0).any() or (r >= n_rows).any() or (c < 0).any() or (c >= n_cols).any():
+        raise ValueError("index out of range")
+    m = sp.coo_matrix((v, (r, c)), shape=(n_rows, n_cols)).tocsr()
+    m.sum_duplicates()
+    m.data[np.abs(m.data) <= 1e-18] = 0.0
+    m.eliminate_zeros()
+    return m
+
+
+def _betacf(a, b, x):
+    """Continued fraction of the incomplete beta function by the modified
+    Lentz method (Numerical Recipes 6.4), as Pvalue.cpp:121-185 evaluates it:
+    stop when |del - 1| <= 3e-7, FPMIN 1e-30."""
+    fpmin, eps = 1e-30, 3e-7
+    qab, qap, qam = a + b, a + 1.0, a - 1.0
+    c, d = 1.0, 1.0 - qab * x / qap
+    d = fpmin if abs(d) < fpmin else d
+    d = 1.0 / d
+    h = d
+    m = 0
+    while m <= 100000:
+        m += 1
+        m2 = 2 * m
+        aa = m * (b - m) * x / ((qam + m2) * (a + m2))
+        d = 1.0 + aa * d
+        d = fpmin if abs(d) < fpmin else d
+        c = 1.0 + aa / c
+        c = fpmin if abs(c) < fpmin else c
+        d = 1.0 / d
+        h = h * d * c
+        aa = -(a + m) * (qab + m) * x / ((a + m2) * (qap + m2))
+        d = 1.0 + aa * d
+        d = fpmin if abs(d) < fpmin else d
+        c = 1.0 + aa / c
+        c = fpmin if abs(c) < fpmin else c
+        d = 1.0 / d
+        dl = d * c
+        h = h * dl
+        if abs(dl - 1.0) <= eps:
+            return h
+    raise ValueError("betacf did not converge")
+
+
+# Lanczos coefficients of Numerical Recipes' gammln (6.1), Pvalue.cpp:189-204
+_GAMMLN_COF = (76.18009173, -86.50532033, 24.01409822, -1.231739516, 0.120858003e-2, -0.536382e-5)
+
+
+def _gammln(xx):
+    x = xx - 1.0
+    tmp = x + 5.5
+    tmp -= (x + 0.5) * np.log(tmp)
+    ser = 1.0
+    for cof in _GAMMLN_COF:
+        x += 1.0
+        ser += cof / x
+    return -tmp + np.log(2.50662827465 * ser)
+
+
+def _betainc(a, b, x):
+    """Pvalue.cpp:206-230 (regularised incomplete beta)."""
+    if x == 0 or x == 1:
+        bt = 0.0
+    else:
+        bt = np.exp(_gammln(a + b) - _gammln(a) - _gammln(b) + a * np.log(x) + b * np.log(1.0 - x))
+    if x < (a + 1.0) / (a + b + 2.0):
+        return bt * _betacf(a, b, x) / a
+    return 1.0 - bt * _betacf(b, a, 1.0 - x) / b
+
+
+def pvalue_stats(x, y):
+    """(correlation, t statistic, p-value) of Calculate_Correlation /
+    Calculate_Tstat / Calculate_Pvalue (Pvalue.cpp:85-235): population
+    moments, t = r sqrt((n-2)/(1-r^2)), two-sided p from the incomplete beta
+    function with n-2 degrees of freedom.  The reference's branch order is
+    kept: p is 0.5 (so 1 is returned) unless n-2 != 1, n-2 <= 1e7 and neither
+    t is NaN nor n-2 <= 0."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    n = len(x)
+    mx, my = x.sum() / n, y.sum() / n
+    cov = ((x - mx) * (y - my)).sum() / n
+    sx = np.sqrt(((x - mx) ** 2).sum() / n)
+    sy = np.sqrt(((y - my) ** 2).sum() / n)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = cov / (sx * sy)
+        t_raw = r * np.sqrt((n - 2) / (1 - r * r))
+    t = -abs(t_raw)
+    dof = float(n - 2)
+    nans = np.isnan(t) or dof <= 0
+    if dof != 1 and dof <= 1e7 and not nans:
+        p = 0.5 * _betainc(0.5 * dof, 0.5, dof / (dof + t * t))
+        if t > 0:
+            p = 1 - p
+    else:
+        p = 0.5
+    return float(r), float(t_raw), float(2 * p)
