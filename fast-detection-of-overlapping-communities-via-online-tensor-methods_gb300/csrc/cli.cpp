@@ -4,13 +4,17 @@
 //   mmsb_cli NX NA NB NC KHID alpha0 DATATYPE Gx_a Gx_b Gx_c Gb_a Gc_a PI_OUT WHITE_OUT
 //            [--method=batch|online|adjoint] [--sweeps=N] [--minibatch=N] [--seed=N]
 //            [--tau=X] [--lambda-out=FILE] [--reader=compat|strict] [--device=N]
+//            [--gpu-out=DIR]
 //
 // Same positional arguments and output files as the reference: PI_OUT gets the
 // normalised memberships as 1-based "community<TAB>node<TAB>value" triplets of
 // the nonzeros over the node order [X|A|B|C] and WHITE_OUT the whitening
 // matrix (write_pi, IOfn.cpp:57-67).  The reference's own reader is
-// reproduced by default (--reader=compat).  Errors print a message and exit
-// with 1 (file) or 2 (device), like the reference's exit codes.
+// reproduced by default (--reader=compat); a block file ending in ".csr" is
+// read as this library's binary CSR container instead.  --gpu-out=DIR also
+// writes the GPU tree's output files (Pi_X/A/B/C, evecs, evals, frob_norm,
+// sim_info).  Errors print a message and exit with 1 (file) or 2 (device),
+// like the reference's exit codes.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -44,7 +48,7 @@ int main(int argc, char** argv) {
                  "usage: %s NX NA NB NC KHID alpha0 DATATYPE Gx_a Gx_b Gx_c Gb_a Gc_a PI_OUT "
                  "WHITE_OUT [--method=batch|online|adjoint] [--sweeps=N] [--minibatch=N] "
                  "[--seed=N] [--tau=X] [--lambda-out=FILE] [--reader=compat|strict] "
-                 "[--device=N]\n",
+                 "[--device=N] [--gpu-out=DIR]\n",
                  argv[0]);
     return 1;
   }
@@ -58,7 +62,7 @@ int main(int argc, char** argv) {
   const char* files[5] = {argv[8], argv[9], argv[10], argv[11], argv[12]};
   const char* pi_out = argv[13];
   const char* white_out = argv[14];
-  std::string lambda_out;
+  std::string lambda_out, gpu_out;
   int compat = 1;
   for (int i = 15; i < argc; ++i) {
     std::string v;
@@ -80,6 +84,8 @@ int main(int argc, char** argv) {
       compat = v != "strict";
     } else if (opt(argv[i], "--device", &v)) {
       cfg.device = std::atoi(v.c_str());
+    } else if (opt(argv[i], "--gpu-out", &v)) {
+      gpu_out = v;
     } else {
       std::fprintf(stderr, "unknown option %s\n", argv[i]);
       return 1;
@@ -91,8 +97,16 @@ int main(int argc, char** argv) {
   mmsb_host_graph* h[5] = {};
   mmsb_csr blocks[5];
   for (int b = 0; b < 5; ++b) {
-    mmsb_status st = mmsb_read_coo(files[b], n[rows_part[b]], n[cols_part[b]], cfg.datatype,
-                                   compat, &h[b]);
+    const size_t len = std::strlen(files[b]);
+    const bool bin = len > 4 && std::strcmp(files[b] + len - 4, ".csr") == 0;
+    mmsb_status st = bin ? mmsb_read_csr(files[b], &h[b])
+                         : mmsb_read_coo(files[b], n[rows_part[b]], n[cols_part[b]], cfg.datatype,
+                                         compat, &h[b]);
+    if (st == MMSB_OK && bin) {
+      mmsb_csr c;
+      mmsb_host_graph_block(h[b], 0, &c);
+      if (c.n_rows != n[rows_part[b]] || c.n_cols != n[cols_part[b]]) st = MMSB_ERR_IO;
+    }
     if (st != MMSB_OK) {
       std::fprintf(stderr, "reading %s failed\n", files[b]);
       return 1;
@@ -127,6 +141,10 @@ int main(int argc, char** argv) {
         for (int i = 0; i < cfg.k; ++i) std::fprintf(f, "%.17g\n", lam[i]);
         std::fclose(f);
       }
+    }
+    if (rc == 0 && !gpu_out.empty() && mmsb_write_gpu_outputs(ctx, gpu_out.c_str()) != MMSB_OK) {
+      std::fprintf(stderr, "writing the GPU-tree outputs to %s failed\n", gpu_out.c_str());
+      rc = 1;
     }
     mmsb_stats s;
     mmsb_get_stats(ctx, &s);

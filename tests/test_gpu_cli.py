@@ -52,3 +52,37 @@ def test_cli_matches_pipeline_and_reference(mm, golden_cfg1, tmp_path):
     nz = colsum > 0
     assert nz.mean() > 0.9
     np.testing.assert_allclose(colsum[nz], 1.0, atol=1e-4)
+
+
+def test_cli_binary_inputs_and_gpu_tree_outputs(mm, golden_cfg1, tmp_path):
+    """Blocks given as binary CSR files (".csr") and --gpu-out: the same
+    memberships as COO text inputs, plus the GPU tree's files."""
+    g = golden_cfg1
+    names = ["Gx_a", "Gx_b", "Gx_c", "Gb_a", "Gc_a"]
+    nX, nA, nB, nC = (int(x) for x in g["parts"])
+    shapes = [(nX, nA), (nX, nB), (nX, nC), (nB, nA), (nC, nA)]
+    txt, csr = [], []
+    for n, (r_, c_) in zip(names, shapes):
+        blk = mm.CsrBlock(r_, c_, g[f"{n}_rp"].astype(np.int64), g[f"{n}_ci"].astype(np.int32))
+        txt.append(str(tmp_path / f"{n}.txt"))
+        csr.append(str(tmp_path / f"{n}.csr"))
+        mm.write_coo(txt[-1], blk)
+        mm.write_csr(csr[-1], blk)
+    out = {}
+    for kind, files in (("txt", txt), ("csr", csr)):
+        pi_f, white_f = str(tmp_path / f"pi_{kind}.txt"), str(tmp_path / f"white_{kind}.txt")
+        d = tmp_path / f"gpu_{kind}"
+        d.mkdir()
+        r = subprocess.run([str(mm.CLI_PATH), str(nX), str(nA), str(nB), str(nC), str(g.k),
+                            repr(g.alpha0), "0", *files, pi_f, white_f, "--method=online",
+                            "--sweeps=2", "--minibatch=100", "--seed=3", "--reader=strict",
+                            f"--gpu-out={d}"], capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+        out[kind] = (open(pi_f).read(), d)
+    assert out["txt"][0] == out["csr"][0]
+    d = out["csr"][1]
+    tail = f"_{g.k}_{g.alpha0:g}_1.txt"
+    for name, n in (("Pi_X", nX), ("Pi_A", nA), ("Pi_B", nB), ("Pi_C", nC)):
+        assert len((d / f"{name}{tail}").read_text().splitlines()) == g.k * n
+    assert len((d / f"frob_norm{tail}").read_text().splitlines()) == 2
+    assert (d / f"sim_info{tail}").exists() and (d / f"evals{tail}").exists()
