@@ -182,6 +182,8 @@ _SIGS = {
     "mmsb_write_csr": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Csr)]),
     "mmsb_read_csr": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P)]),
     "mmsb_pvalues": (ctypes.c_int, [_P, _F, ctypes.c_int32, _D, _D, _D]),
+    "mmsb_op_gram": (ctypes.c_int, [_F, ctypes.c_int64, ctypes.c_int32, _F, ctypes.c_int32,
+                                    ctypes.c_double, _D]),
     "mmsb_get_convergence": (ctypes.c_int, [_P, _D, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]),
     "mmsb_write_gpu_outputs": (ctypes.c_int, [_P, ctypes.c_char_p]),
 }
@@ -705,6 +707,18 @@ def spmm(block: CsrBlock, P, transpose=False, alpha=1.0):
     _check(lib().mmsb_op_spmm(ctypes.byref(c), int(transpose), _fptr(P), P.shape[1], alpha,
                               _fptr(Y)))
     return Y
+
+
+def gram(A, B, alpha=1.0):
+    """alpha A^T B for n x pa and n x pb FP32 panels (mmsb_op_gram), FP64."""
+    A = np.ascontiguousarray(A, dtype=np.float32)
+    B = np.ascontiguousarray(B, dtype=np.float32)
+    if A.shape[0] != B.shape[0]:
+        raise ValueError("A and B need the same number of rows")
+    S = np.zeros((A.shape[1], B.shape[1]), dtype=np.float64, order="F")
+    _check(lib().mmsb_op_gram(_fptr(A), A.shape[0], A.shape[1], _fptr(B), B.shape[1], alpha,
+                              S.ctypes.data_as(_D)))
+    return S
 
 
 def symeig(A):

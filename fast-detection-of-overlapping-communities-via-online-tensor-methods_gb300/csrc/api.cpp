@@ -606,6 +606,31 @@ mmsb_status mmsb_op_spmm(const mmsb_csr* g, int transpose, const float* P, int64
   });
 }
 
+mmsb_status mmsb_op_gram(const float* A, int64_t n, int32_t pa, const float* B, int32_t pb,
+                         double alpha, double* S) {
+  if (!A || !B || !S || n < 1 || pa < 1 || pb < 1 || pa > 4096 || pb > 4096)
+    return MMSB_ERR_INVALID_ARG;
+  mmsb_config cfg;
+  mmsb_config_default(&cfg);
+  mmsb_ctx* c = nullptr;
+  mmsb_status st = mmsb_create(&cfg, &c);
+  if (st != MMSB_OK) return st;
+  std::unique_ptr<mmsb_ctx> own(c);
+  return guard(c, [&]() {
+    float* dA = c->tbuf<float>("A", (size_t)n * pa);
+    float* dB = c->tbuf<float>("B", (size_t)n * pb);
+    double* dS = c->tbuf<double>("S", (size_t)pa * pb);
+    const int64_t cap = (int64_t)gram_tsk_partials(n, pa, pb);
+    double* part = c->tbuf<double>("part", (size_t)cap);
+    ck(cudaMemcpyAsync(dA, A, sizeof(float) * n * pa, cudaMemcpyHostToDevice, c->s), "H2D");
+    ck(cudaMemcpyAsync(dB, B, sizeof(float) * n * pb, cudaMemcpyHostToDevice, c->s), "H2D");
+    ck(gram_tsk(dA, pa, pa, dB, pb, pb, n, alpha, dS, part, cap, c->s, c->flags), "gram");
+    d2h(c, S, dS, sizeof(double) * pa * pb);
+    ck(cudaStreamSynchronize(c->s), "sync");
+    check_device_flags(c, "gram");
+  });
+}
+
 mmsb_status mmsb_op_symeig(const double* A, int32_t n, double* evals, double* evecs) {
   if (!A || !evals || !evecs || n < 1 || n > 512) return MMSB_ERR_INVALID_ARG;
   mmsb_config cfg;

@@ -56,9 +56,17 @@ cudaError_t unwhiten_normprob(const int64_t* rp, const int32_t* ci, const float*
 
 // S[pa x pb] (column-major FP64) = alpha * A^T B, A: n x pa (lda), B: n x pb (ldb),
 // row-major FP32; FP32 partial sums over row chunks, FP64 across chunks.
+// (tensor cores, tcgen05 kind::tf32 with the 3xTF32 split, when both sides
+// have >= 64 columns and n >= 4096; flags receives a timeout of its bounded
+// waits)
 cudaError_t gram_tsk(const float* A, int lda, int pa, const float* B, int ldb, int pb, int64_t n,
                      double alpha, double* S, double* partials, int64_t partials_cap,
-                     cudaStream_t s);
+                     cudaStream_t s, unsigned* flags = nullptr);
+inline bool gram_use_tc(int64_t n, int pa, int pb) { return pa >= 64 && pb >= 64 && n >= 4096; }
+int gram_tc_nsplit(int64_t n, int pa, int pb);
+cudaError_t gram_tc_partial(const float* A, int lda, int pa, const float* B, int ldb, int pb,
+                            int64_t n, double* partials, int nsplit, unsigned* flags,
+                            cudaStream_t s);
 size_t gram_tsk_partials(int64_t n, int pa, int pb);
 // Y[n x ldy] (row-major FP32) = M[n x ldm] (first p cols) * F (p x q, column-major FP64, ldf);
 // columns q..ldy-1 of Y are zeroed.

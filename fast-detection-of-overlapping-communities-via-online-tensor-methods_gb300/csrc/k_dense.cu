@@ -1188,12 +1188,23 @@ unsigned grid_for(int64_t n, int T = 256) {
 }  // namespace
 
 size_t gram_tsk_partials(int64_t n, int pa, int pb) {
-  return (size_t)gram_nsplit(n, pa, pb) * pa * pb;
+  const int ns = gram_use_tc(n, pa, pb) ? gram_tc_nsplit(n, pa, pb) : gram_nsplit(n, pa, pb);
+  return (size_t)ns * pa * pb;
 }
 
 cudaError_t gram_tsk(const float* A, int lda, int pa, const float* B, int ldb, int pb, int64_t n,
                      double alpha, double* S, double* partials, int64_t partials_cap,
-                     cudaStream_t s) {
+                     cudaStream_t s, unsigned* flags) {
+  if (gram_use_tc(n, pa, pb)) {
+    // tcgen05 (kind::tf32, 3xTF32) partials over row splits, then the FP64 sum
+    const int nsplit = gram_tc_nsplit(n, pa, pb);
+    if ((int64_t)nsplit * pa * pb > partials_cap) return cudaErrorInvalidValue;
+    MMSB_CUDA_TRY(gram_tc_partial(A, lda, pa, B, ldb, pb, n, partials, nsplit, flags, s));
+    gram_reduce_kernel<<<grid_for((int64_t)pa * pb), 256, 0, s>>>(partials, nsplit,
+                                                                   (int64_t)pa * pb, alpha, S);
+    ++g_launch_count;
+    return cudaGetLastError();
+  }
   const int nsplit = gram_nsplit(n, pa, pb);
   if ((int64_t)nsplit * pa * pb > partials_cap) return cudaErrorInvalidValue;
   const int64_t rows_per_split = round_up(ceil_div(n, nsplit), GR);

@@ -278,6 +278,12 @@ mmsb_status mmsb_op_spmm(const mmsb_csr* g, int transpose, const float* P, int64
                          float alpha, float* Y);
 /* Symmetric eigen-decomposition of an n x n positive semi-definite matrix
  * (column-major, n <= 512), eigenvalues descending; vectors column-major n x n. */
+/* S (pa x pb, column-major FP64) = alpha A^T B for node-major FP32 panels A
+ * (n x pa) and B (n x pb), host arrays: the tall-skinny Gram of the Nystrom
+ * chain (X^T (X R) products of CPU/Spectral.cpp:228-246 and the CholQR
+ * Grams), on the tensor cores (tcgen05, 3xTF32) when pa, pb >= 64. */
+mmsb_status mmsb_op_gram(const float* A, int64_t n, int32_t pa, const float* B, int32_t pb,
+                         double alpha, double* S);
 mmsb_status mmsb_op_symeig(const double* A, int32_t n, double* evals, double* evecs);
 
 /* No counterpart in the reference.  Y = alpha * G^T * P for callers that
