@@ -31,8 +31,11 @@ extern thread_local int64_t g_launch_count;
 // ---- sparse (k_sparse.cu) ---------------------------------------------------
 
 // Y[n_rows x ld] (row-major) = alpha * G * P[n_cols x ld]; ld % 4 == 0.
+// p_rows (rows of P, i.e. columns of G), when given, lets panels far larger
+// than L2 run as column slices that stay L2-resident.
 cudaError_t spmm_f32(const int64_t* rp, const int32_t* ci, const float* val, int64_t n_rows,
-                     const float* P, int ld, float alpha, float* Y, cudaStream_t s);
+                     const float* P, int ld, float alpha, float* Y, cudaStream_t s,
+                     int64_t p_rows = 0);
 // Checks an uploaded block: ORs 1 into *bad for a decreasing row offset, 2
 // for a column index outside [0, n_cols).
 cudaError_t csr_validate(const int64_t* rp, const int32_t* ci, int64_t n_rows, int64_t n_cols,

@@ -25,20 +25,21 @@ __device__ __forceinline__ void fma4(float4& a, float v, const float4& x) {
   a.w = fmaf(v, x.w, a.w);
 }
 
-// G lanes per row; every lane accumulates chunks (base + gl) and (base + G + gl).
+// G lanes per row; every lane accumulates chunks (base + gl) and (base + G + gl)
+// of the 16-byte column chunks [cb, ce) (rows of P and Y have c4 chunks).
 template <int G>
 __global__ void __launch_bounds__(256) spmm_rows_kernel(
     const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
     const float* __restrict__ val, int64_t n_rows, const float4* __restrict__ P, int c4,
-    float alpha, float4* __restrict__ Y) {
+    float alpha, float4* __restrict__ Y, int cb, int ce) {
   const int lane = threadIdx.x & 31;
   const int gl = lane % G;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
   if (row >= n_rows) return;
   const int64_t beg = rp[row], end = rp[row + 1];
-  for (int base = 0; base < c4; base += 2 * G) {
+  for (int base = cb; base < ce; base += 2 * G) {
     const int ch0 = base + gl, ch1 = base + G + gl;
-    const bool h0 = ch0 < c4, h1 = ch1 < c4;
+    const bool h0 = ch0 < ce, h1 = ch1 < ce;
     float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
     int64_t j = beg;
     for (; j + 4 <= end; j += 4) {
@@ -80,12 +81,13 @@ __global__ void __launch_bounds__(256) spmm_rows_kernel(
 
 template <int G>
 cudaError_t launch_spmm(const int64_t* rp, const int32_t* ci, const float* val, int64_t n_rows,
-                        const float* P, int c4, float alpha, float* Y, cudaStream_t s) {
+                        const float* P, int c4, float alpha, float* Y, cudaStream_t s,
+                        int cb = 0, int ce = -1) {
   const int threads = 256;
   const int64_t blocks = ceil_div(n_rows * G, threads);
   spmm_rows_kernel<G><<<(unsigned)blocks, threads, 0, s>>>(
       rp, ci, val, n_rows, reinterpret_cast<const float4*>(P), c4, alpha,
-      reinterpret_cast<float4*>(Y));
+      reinterpret_cast<float4*>(Y), cb, ce < 0 ? c4 : ce);
   ++g_launch_count;
   return cudaGetLastError();
 }
@@ -256,10 +258,26 @@ __global__ void __launch_bounds__(256) unwhiten_normprob_kernel(
 }  // namespace
 
 cudaError_t spmm_f32(const int64_t* rp, const int32_t* ci, const float* val, int64_t n_rows,
-                     const float* P, int ld, float alpha, float* Y, cudaStream_t s) {
+                     const float* P, int ld, float alpha, float* Y, cudaStream_t s,
+                     int64_t p_rows) {
   if (ld % 4 != 0) return cudaErrorInvalidValue;
   if (n_rows == 0) return cudaSuccess;
   const int c4 = ld / 4;
+  // a panel far larger than L2 (129 MB): column slices of <= 64 MB, one pass
+  // over the CSR each, so that every slice's gathered rows stay L2-resident
+  if (p_rows > 0 && (double)p_rows * ld * sizeof(float) > 96e6) {
+    int w4 = (int)std::min<int64_t>(c4, std::max<int64_t>(8, (int64_t)(64e6 / (16.0 * p_rows))));
+    w4 = std::max(8, w4 / 8 * 8);
+    for (int cb = 0; cb < c4; cb += w4) {
+      const int ce = std::min(c4, cb + w4);
+      cudaError_t e = w4 >= 64   ? launch_spmm<32>(rp, ci, val, n_rows, P, c4, alpha, Y, s, cb, ce)
+                      : w4 >= 32 ? launch_spmm<16>(rp, ci, val, n_rows, P, c4, alpha, Y, s, cb, ce)
+                      : w4 >= 16 ? launch_spmm<8>(rp, ci, val, n_rows, P, c4, alpha, Y, s, cb, ce)
+                                 : launch_spmm<4>(rp, ci, val, n_rows, P, c4, alpha, Y, s, cb, ce);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
   if (c4 <= 2) return launch_spmm<1>(rp, ci, val, n_rows, P, c4, alpha, Y, s);
   if (c4 <= 4) return launch_spmm<2>(rp, ci, val, n_rows, P, c4, alpha, Y, s);
   if (c4 <= 8) return launch_spmm<4>(rp, ci, val, n_rows, P, c4, alpha, Y, s);

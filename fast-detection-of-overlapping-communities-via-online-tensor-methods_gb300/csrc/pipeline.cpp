@@ -105,11 +105,11 @@ void spmm(mmsb_ctx* c, const DevCsr& g, const float* P, int ld, float alpha, flo
   const size_t slot = c->spmm_events.size();
   if (slot < c->spmm_pool.size()) {
     ck(cudaEventRecord(c->spmm_pool[slot].first, st), "event");
-    ck(spmm_f32(g.rp, g.ci, g.val, g.n_rows, P, ld, alpha, Y, st), "spmm");
+    ck(spmm_f32(g.rp, g.ci, g.val, g.n_rows, P, ld, alpha, Y, st, g.n_cols), "spmm");
     ck(cudaEventRecord(c->spmm_pool[slot].second, st), "event");
     c->spmm_events.push_back(slot);
   } else {
-    ck(spmm_f32(g.rp, g.ci, g.val, g.n_rows, P, ld, alpha, Y, st), "spmm");
+    ck(spmm_f32(g.rp, g.ci, g.val, g.n_rows, P, ld, alpha, Y, st, g.n_cols), "spmm");
   }
   c->stats.spmm_launches += 1;
   c->stats.spmm_bytes += 8.0 * (g.n_rows + 1) + 4.0 * g.nnz * (g.val ? 2 : 1) +
