@@ -66,6 +66,8 @@ struct mmsb_ctx {
   // event pairs around the STPM contraction (0) and step (1) launches
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kpool[2];
   size_t kused[2] = {0, 0};
+  int64_t klaunched[2] = {0, 0};  // launches since the last collect (timed or not)
+  bool ksample = true;             // time the next STPM launches with events
 
   ~mmsb_ctx();
   // grow-only named workspace buffer of at least `bytes` bytes

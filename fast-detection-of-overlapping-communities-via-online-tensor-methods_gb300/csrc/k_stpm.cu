@@ -322,6 +322,13 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   }
   __syncthreads();
   cluster.sync();  // Phi read and barriers initialised everywhere before any copy
+  // launched with programmatic serialization after the contraction, the
+  // prologue above overlapped its tail (Phi is final: the contraction lets
+  // this kernel start only after its own wait on the previous step); from
+  // here on its partials are read, so wait for it to complete, and let the
+  // next contraction be scheduled (it waits for this kernel in turn)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   uint32_t parity[2] = {0u, 0u};
   int nbcast = 0;
   bool timed_out = false;
@@ -706,6 +713,10 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
                 LDC = Cfg::LDC;
   constexpr int IB = Cfg::IB;
   static_assert(KP % 16 == 0 && KP <= 256, "KP");
+  // programmatic serialization: wait for the previous kernel (the step that
+  // wrote Phi), then let the next one be scheduled early
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   extern __shared__ __align__(16) unsigned char smraw[];
   // this CTA's columns of Phi: i0 + ii, ii < IB (i local below)
   const int cb = (Cfg::NBC > 1) ? (int)blockIdx.y : 0, i0 = cb * IB;
@@ -1101,13 +1112,15 @@ cudaError_t launch_partial_t(const StpmPartialArgs& a, int grid, cudaStream_t s)
   cfg.blockDim = dim3(Contract<KP, MODE, BF>::NT, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = kPartialCluster;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;  // see contract_body
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 2;
   MMSB_CUDA_TRY(cudaLaunchKernelEx(&cfg, stpm_contract_kernel<KP, MODE, BF>, a));
   ++g_launch_count;
   return cudaGetLastError();
@@ -1198,13 +1211,15 @@ cudaError_t launch_step_t(const StpmUpdateArgs& a, cudaStream_t s) {
   cfg.blockDim = dim3(512, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = CL;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;  // see step_body
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 2;
   MMSB_CUDA_TRY(cudaLaunchKernelEx(&cfg, stpm_step_kernel<KP, CL>, a));
   ++g_launch_count;
   return cudaGetLastError();

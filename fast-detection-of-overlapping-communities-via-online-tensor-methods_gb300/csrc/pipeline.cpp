@@ -527,6 +527,13 @@ struct PartialOut {
 // summed by collect_kernel_times after the STPM loop
 template <typename F>
 static void timed_launch(mmsb_ctx* c, int which, F&& launch) {
+  ++c->klaunched[which];
+  if (!c->ksample) {
+    // untimed: nothing between this launch and its neighbours, so that the
+    // STPM kernels' programmatic serialization can overlap them
+    launch();
+    return;
+  }
   auto& pool = c->kpool[which];
   if (c->kused[which] == pool.size()) {
     std::pair<cudaEvent_t, cudaEvent_t> pr{};
@@ -551,10 +558,15 @@ static void collect_kernel_times(mmsb_ctx* c) {
       ck(cudaEventElapsedTime(&t, c->kpool[w][i].first, c->kpool[w][i].second), "elapsed");
       ms += t;
     }
+    // timed launches are a sample of all (every 8th minibatch step): scale
+    // their mean to every launch
+    if (c->kused[w] > 0) ms *= (double)c->klaunched[w] / (double)c->kused[w];
     *out[w] += ms;
-    *cnt[w] += (int64_t)c->kused[w];
+    *cnt[w] += c->klaunched[w];
     c->kused[w] = 0;
+    c->klaunched[w] = 0;
   }
+  c->ksample = true;
 }
 
 StpmPartialArgs stpm_partial_args(mmsb_ctx* c, int q1, int q2, int q3, int64_t begin,
@@ -707,7 +719,8 @@ int64_t stpm_online_rounds(const mmsb_ctx* c) {
 
 // one minibatch update: partial contractions, then the fused reduction +
 // Phi - beta (3 theta O - gscale G) + polar orthonormalisation on one cluster
-static void stpm_step(mmsb_ctx* c, const OnlineRound& rd) {
+static void stpm_step(mmsb_ctx* c, const OnlineRound& rd, bool timed = true) {
+  c->ksample = timed;
   PartialOut po = stpm_partials(c, rd.mode, 0, 1, 2, rd.x0, rd.cnt, rd.c0, rd.c2, rd.bf16);
   StpmUpdateArgs u = stpm_online_update_args(c, rd, po.gpart, po.stride, po.grid);
   timed_launch(c, 1, [&]() { ck(stpm_update(u, c->s), "stpm_step"); });
@@ -829,7 +842,7 @@ void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
   for (int64_t r = 0; r < rounds; ++r) {
     if (c->stop.load()) throw MmsbError(MMSB_ERR_STOPPED, "stop requested");
     stpm_online_round(c, r, &rd);
-    stpm_step(c, rd);
+    stpm_step(c, rd, r % 8 == 0);
     if ((r + 1) % per == 0)
       ck(phi_delta((int64_t)k * k, c->phi, snap, c->conv + c->conv_count++, s), "trace");
   }
