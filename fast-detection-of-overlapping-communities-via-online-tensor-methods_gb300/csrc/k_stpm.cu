@@ -321,6 +321,20 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  if (a.step_mode == kStepOnline) {
+    // the mean terms phi_i . mu of this block's columns (a warp per dot
+    // product, lanes along the k entries): Phi and mu only, so before the wait
+    for (int e = tid / 32; e < 3 * NB; e += blockDim.x / 32) {
+      const int which = e / NB, jb = e % NB, i = c0 + jb;
+      const float* mu = which == 0 ? a.mu1 : which == 1 ? a.mu2 : a.mu3;
+      float sv = 0.f;
+      if (i < k && mu)
+        for (int j = lane; j < k; j += 32) sv = fmaf(Xa[i * XLD + j], mu[j], sv);
+#pragma unroll
+      for (int off = 16; off; off >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, off);
+      if (lane == 0) mv[which * KP + jb] = sv;
+    }
+  }
   cluster.sync();  // Phi read and barriers initialised everywhere before any copy
   // launched with programmatic serialization after the contraction, the
   // prologue above overlapped its tail (Phi is final: the contraction lets
@@ -376,20 +390,22 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     return !__syncthreads_or(!ok);
   };
   if (a.step_mode == kStepOnline) {
-    // G block (columns c0 .. c0+NB) from the per-CTA partials, plus the mean
-    // terms phi_i . mu (a warp per dot product, lanes along the k entries)
-    for (int e = tid / 32; e < 3 * NB; e += blockDim.x / 32) {
-      const int which = e / NB, jb = e % NB, i = c0 + jb;
-      const float* mu = which == 0 ? a.mu1 : which == 1 ? a.mu2 : a.mu3;
-      float sv = 0.f;
-      if (i < k && mu)
-        for (int j = lane; j < k; j += 32) sv = fmaf(X[i * XLD + j], mu[j], sv);
+    // G block (columns c0 .. c0+NB) from the per-CTA partials.  The first 8
+    // partials of this thread's (up to) two G entries are loaded together
+    // with the d-sum partials, so that one round trip covers them all.
+    constexpr int kPre = 2, kPreParts = 8;
+    float gpre[kPre][kPreParts];
 #pragma unroll
-      for (int off = 16; off; off >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, off);
-      if (lane == 0) mv[which * KP + jb] = sv;
+    for (int h = 0; h < kPre; ++h) {
+      const int e = tid + h * (int)blockDim.x, jb = e / KP, j = e % KP, i = c0 + jb;
+      const bool live = e < NB * KP && i < k && j < k;
+#pragma unroll
+      for (int u = 0; u < kPreParts; ++u)
+        gpre[h][u] = (live && u < a.nparts)
+                         ? __ldg(a.gpart + (int64_t)u * a.part_stride + (int64_t)i * k + j)
+                         : 0.f;
     }
-    __syncthreads();
-    // per-column sums of the d partials (3 x NB), then the contraction block
+    // per-column sums of the d partials (3 x NB)
     for (int e = tid / 32; e < 3 * NB; e += blockDim.x / 32) {
       const int which = e / NB, jb = e % NB, i = c0 + jb;
       float sd = 0.f;
@@ -408,6 +424,18 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
         const float* gp = a.gpart + (int64_t)i * k + j;
         float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
         int pp = 0;
+        const int h = (e - tid) / (int)blockDim.x;  // 0 or 1 for the preloaded entries
+        if (h < kPre) {
+#pragma unroll
+          for (int h2 = 0; h2 < kPre; ++h2)
+            if (h2 == h) {
+              s0 += gpre[h2][0] + gpre[h2][4];
+              s1 += gpre[h2][1] + gpre[h2][5];
+              s2 += gpre[h2][2] + gpre[h2][6];
+              s3 += gpre[h2][3] + gpre[h2][7];
+            }
+          pp = kPreParts;
+        }
         for (; pp + 8 <= a.nparts; pp += 8) {
           float v[8];
 #pragma unroll
@@ -565,7 +593,9 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       __syncthreads();
     }
   }
-  cluster.sync();  // every CTA has read the statistics slots
+  // (red[] is written only by post_stats above, and every CTA finished its
+  // update before the first cluster barrier: no second barrier is needed
+  // before the first broadcast of the loop)
   float lo = kNsLowerGuess;  // lower bound (guess at first) on sigma(X_t)
   float prev_err = 1e30f;    // max|A_{t-1} - I|
   for (; !done && it < a.max_ns; ++it) {
