@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(int p, const double* __res
 // DSMEM into its other buffer set (one cluster barrier per block round).
 // A pair group of 16 lanes rotates one pair; rotations use the same test and
 // formulas as jacobi_kernel.
-constexpr int kJcCtas = 8, kJcBlocks = 2 * kJcCtas, kJcLanes = 16;
+constexpr int kJcCtas = 8, kJcBlocks = 2 * kJcCtas;
 
 __host__ __device__ inline int jc_ld(int p) { return p + ((16 - p % 32) + 32) % 32; }  // == 16 mod 32
 __host__ __device__ inline int jc_b(int p) { return (p + kJcBlocks - 1) / kJcBlocks; }
@@ -621,6 +621,9 @@ __device__ __forceinline__ void jc_players(int t, int r, int& a, int& b) {
   b = 1 + ((kJcBlocks - 2 - t + r) % w);
 }
 
+// LANES lanes rotate one pair: 32 (a warp, shorter dependent chains) while a
+// block has at most 16 columns, else 16 so that 32 pairs fit a round
+template <int LANES>
 __global__ void __launch_bounds__(512) jacobi_cluster_kernel(int p, const double* __restrict__ Y,
                                                              double* __restrict__ evals,
                                                              double* __restrict__ evecs,
@@ -636,7 +639,7 @@ __global__ void __launch_bounds__(512) jacobi_cluster_kernel(int p, const double
   auto slot = [&](int q, int sl) { return jsm + (size_t)(2 * q + sl) * b * ld; };
   __shared__ int s_rot[2];
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int grp = tid / kJcLanes, ln = tid % kJcLanes, ngrp = nt / kJcLanes;
+  const int grp = tid / LANES, ln = tid % LANES, ngrp = nt / LANES;
   auto ncols = [&](int x) { return max(0, min(b, p - x * b)); };
   int cur = 0, pa, pb;
   jc_players(t, 0, pa, pb);
@@ -656,7 +659,7 @@ __global__ void __launch_bounds__(512) jacobi_cluster_kernel(int p, const double
     float al = 0.f, be = 0.f, ga = 0.f;
     if (live) {
 #pragma unroll 4
-      for (int i = ln; i < p; i += kJcLanes) {
+      for (int i = ln; i < p; i += LANES) {
         const float x = u[i], y = v[i];
         al = fmaf(x, x, al);
         be = fmaf(y, y, be);
@@ -664,7 +667,7 @@ __global__ void __launch_bounds__(512) jacobi_cluster_kernel(int p, const double
       }
     }
 #pragma unroll
-    for (int off = kJcLanes / 2; off; off >>= 1) {
+    for (int off = LANES / 2; off; off >>= 1) {
       al += __shfl_xor_sync(0xffffffffu, al, off);
       be += __shfl_xor_sync(0xffffffffu, be, off);
       ga += __shfl_xor_sync(0xffffffffu, ga, off);
@@ -674,7 +677,7 @@ __global__ void __launch_bounds__(512) jacobi_cluster_kernel(int p, const double
       const float tt = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
       const float c = rsqrtf(1.f + tt * tt), sn = c * tt;
 #pragma unroll 4
-      for (int i = ln; i < p; i += kJcLanes) {
+      for (int i = ln; i < p; i += LANES) {
         const float x = u[i], y = v[i];
         u[i] = c * x - sn * y;
         v[i] = sn * x + c * y;
@@ -1331,11 +1334,12 @@ cudaError_t eig_from_factor(int p, const double* Y, double* evals, double* evecs
   if (p >= 96) {
     const size_t smc = sizeof(float) * 4 * (size_t)jc_b(p) * jc_ld(p);
     if (smc <= 200 * 1024) {
-      static bool set = false;
-      if (!set) {
-        MMSB_CUDA_TRY(cudaFuncSetAttribute(jacobi_cluster_kernel,
+      const bool wide = jc_b(p) <= 16;
+      static bool set[2] = {false, false};
+      if (!set[wide]) {
+        MMSB_CUDA_TRY(cudaFuncSetAttribute(wide ? jacobi_cluster_kernel<32> : jacobi_cluster_kernel<16>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        set = true;
+        set[wide] = true;
       }
       cudaLaunchConfig_t lc = {};
       lc.gridDim = dim3(kJcCtas);
@@ -1350,8 +1354,10 @@ cudaError_t eig_from_factor(int p, const double* Y, double* evals, double* evecs
       lc.attrs = at;
       lc.numAttrs = 1;
       ++g_launch_count;
-      return cudaLaunchKernelEx(&lc, jacobi_cluster_kernel, p, Y, evals, evecs, work, flags,
-                                max_sweeps, tol);
+      return wide ? cudaLaunchKernelEx(&lc, jacobi_cluster_kernel<32>, p, Y, evals, evecs, work,
+                                       flags, max_sweeps, tol)
+                  : cudaLaunchKernelEx(&lc, jacobi_cluster_kernel<16>, p, Y, evals, evecs, work,
+                                       flags, max_sweeps, tol);
     }
   }
   if (sm <= 200 * 1024) {
