@@ -279,6 +279,9 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   using S = StepSmem<KP, CL>;
   constexpr int NB = S::NB, XLD = S::XLD;
   static_assert(NB == 8 || NB == 16, "column block of 8 or 16");
+  // one warp of the 512 threads issues the copy to each rank; the statistics
+  // of the tiles and of the ranks are reduced across the lanes of a warp
+  static_assert(CL <= 16 && S::TILES <= 32, "cluster or tile count");
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   extern __shared__ __align__(16) float sm[];
@@ -381,9 +384,10 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     // before any copy overwrites it
     if (S::SB) cluster.sync();
     const int bi = dn == Xa ? 0 : 1;
-    if (tid < CL)
+    // one issuing thread per warp: copies issued by lanes of one warp serialise
+    if (lane == 0 && (tid >> 5) < CL)
       bulk_copy_to_rank(dn + c0 * XLD, Otc, (uint32_t)(sizeof(float) * NB * XLD), &s_full[bi],
-                        (uint32_t)tid);
+                        (uint32_t)(tid >> 5));
     if (tid == 0) mbar_arrive_expect_tx(&s_full[bi], (uint32_t)(sizeof(float) * KP * XLD));
     const bool ok = mbar_wait_bounded(&s_full[bi], parity[bi]);
     parity[bi] ^= 1u;
@@ -532,20 +536,25 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       }
     });
     __syncthreads();
-    if (tid == 0) {
-      float m = 0.f, e = 0.f, f = 0.f;
-      for (int jb = 0; jb < NB; ++jb) {
-        float cs = 0.f;
-        for (int mt = 0; mt < S::MT; ++mt) cs += colpart[mt * NB + jb];
-        m = fmaxf(m, cs);
+    if (tid < 32) {  // warp 0: lane jb sums column jb, lane t takes tile t
+      float m = 0.f;
+      if (lane < NB) {
+#pragma unroll
+        for (int mt = 0; mt < S::MT; ++mt) m += colpart[mt * NB + lane];
       }
-      for (int t = 0; t < S::TILES; ++t) {
-        e = fmaxf(e, errpart[t]);
-        f += fropart[t];
+      float e = lane < S::TILES ? errpart[lane] : 0.f;
+      float f = lane < S::TILES ? fropart[lane] : 0.f;
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+        e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, off));
+        f += __shfl_xor_sync(0xffffffffu, f, off);
       }
-      s_abs = m;
-      s_err = e;
-      s_fro = f;
+      if (lane == 0) {
+        s_abs = m;
+        s_err = e;
+        s_fro = f;
+      }
     }
     __syncthreads();
   };
@@ -559,15 +568,25 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       r[2 * CL + rank] = s_fro;
     }
   };
-  auto reduce_stats = [&](const float* src, int stride, float& gabs, float& gerr, float& gfro) {
-    gabs = 0.f;
-    gerr = 0.f;
-    gfro = 0.f;
-    for (int q = 0; q < CL; ++q) {
-      gabs = fmaxf(gabs, src[q * stride]);
-      gerr = fmaxf(gerr, src[q * stride + 1]);
-      gfro += src[q * stride + 2];
+  // rank q's statistics at src[q * qs + {0, fs, 2 fs}], reduced by every
+  // warp across its lanes (the xor butterfly gives every lane, and so every
+  // warp and every CTA, the same bits: IEEE addition is commutative)
+  auto reduce_stats = [&](const float* src, int qs, int fs, float& gabs, float& gerr, float& gfro) {
+    float x = 0.f, y = 0.f, z = 0.f;
+    if (lane < CL) {
+      x = src[lane * qs];
+      y = src[lane * qs + fs];
+      z = src[lane * qs + 2 * fs];
     }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, off));
+      y = fmaxf(y, __shfl_xor_sync(0xffffffffu, y, off));
+      z += __shfl_xor_sync(0xffffffffu, z, off);
+    }
+    gabs = x;
+    gerr = y;
+    gfro = z;
   };
   // initial scaling: sigma_max^2 <= ||X^T X||_1
   gram_stats(0.f, 1.f);
@@ -576,13 +595,9 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   int it = 0;
   bool done = timed_out, last = false;
   if (!done) {
-    float gabs = 0.f, gerr = 0.f, gfro = 0.f;
-    for (int q = 0; q < CL; ++q) {
-      gabs = fmaxf(gabs, red[q]);
-      gerr = fmaxf(gerr, red[CL + q]);
-      gfro += red[2 * CL + q];
-    }
-    if (!(gerr == gerr) || !(gabs == gabs)) {
+    float gabs, gerr, gfro;
+    reduce_stats(red, 1, CL, gabs, gerr, gfro);
+    if (!(gerr == gerr) || !(gabs == gabs) || !(gfro == gfro)) {
       if (tid == 0 && rank == 0) atomicOr(a.flags, kFlagNonFinite);
       done = true;
     } else if (gerr < a.ns_tol) {
@@ -607,7 +622,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       break;
     }
     float gabs, gerr, gfro;
-    reduce_stats(dn + KP, NB * XLD, gabs, gerr, gfro);  // A_t's statistics, from every rank
+    reduce_stats(dn + KP, NB * XLD, 1, gabs, gerr, gfro);  // A_t's statistics, from every rank
     if (!(gerr == gerr) || !(gabs == gabs) || !(gfro == gfro)) {
       if (tid == 0 && rank == 0) atomicOr(a.flags, kFlagNonFinite);
       done = true;
