@@ -108,7 +108,7 @@ __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
 // scaled Newton-Schulz: first guess of the smallest singular value after
 // the initial scaling, the error below which the plain step is used, and a
 // cap on the scale that keeps f(a sigma) > 0 for sigma slightly above 1
-constexpr float kNsLowerGuess = 2e-2f;
+constexpr float kNsLowerGuess = 1e-2f;
 constexpr float kNsPlainBelow = 0.1f;
 constexpr float kNsMaxScale = 1.7f;
 __device__ __forceinline__ float ns_poly(float y) { return y * (1.5f - 0.5f * y * y); }
@@ -231,14 +231,15 @@ __device__ __forceinline__ void warp_tile_3xtf32(const float* __restrict__ pa,
 }
 
 // Tile products of the step.  Warp w < TILES * KS owns tile w % TILES and
-// half w / TILES of the K range (KS = 2); the halves meet in `part`.
+// half w / TILES of the K range (KS = 2); the halves meet in `part`.  A warp
+// calls pre(tile) before it reads the tile's operands.
 // kProdGram:  A_blk = X^T X[:, c0 .. c0+NB)   (A(m=i, k=r) = X[i XLD + r])
 // kProdTimes: P_blk = X B_blk                 (A(m=r, k=i) = X[i XLD + r])
 enum StepProd : int { kProdGram = 0, kProdTimes = 1 };
 
-template <int KP, int CL, int PROD, typename Epi>
+template <int KP, int CL, int PROD, typename Pre, typename Epi>
 __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const float* __restrict__ Bm,
-                                           int c0, float* __restrict__ part, Epi&& epi) {
+                                           int c0, float* __restrict__ part, Pre&& pre, Epi&& epi) {
   using S = StepSmem<KP, CL>;
   constexpr int XLD = S::XLD;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -254,6 +255,7 @@ __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const fl
     const bool active = warp < S::TILES * S::KS;
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     if (active) {
+      pre(tile);
       product(tile, ks * (KP / 2), ks * (KP / 2) + KP / 2, acc);
       if (ks == 1) {
 #pragma unroll
@@ -268,6 +270,7 @@ __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const fl
   } else {
     for (int tile = warp; tile < S::TILES; tile += nw) {
       float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      pre(tile);
       product(tile, 0, KP, acc);
       epi(acc, (tile % S::MT) * 16, (tile / S::MT) * 8, tile);
     }
@@ -294,8 +297,8 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   float* mv = part + (S::KS == 2 ? S::TILES * 128 : 0);  // m1, m2, m3 (+ pad) for this block
   float* red = mv + 4 * KP;       // initial statistics of the CL ranks (3 x CL)
   float* dcol = red + 3 * CL;     // 3 * NB d-sums (online step)
-  __shared__ float s_abs, s_err, s_fro;
-  __shared__ __align__(8) uint64_t s_full[2];  // "next iterate arrived" for Xa / Xb
+  __shared__ float s_nrm, s_err, s_fro;
+  __shared__ __align__(8) uint64_t s_blk[2][16];  // block q of Xa / Xb arrived
   const int k = a.k;
   const int c0 = rank * NB;
   const int tid = threadIdx.x, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
@@ -318,9 +321,8 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     }
   }
   for (int e = tid; e < 2 * NB * XLD; e += blockDim.x) Ot[e] = 0.f;
-  if (tid == 0) {
-    mbar_init(&s_full[0], 1);
-    mbar_init(&s_full[1], 1);
+  if (tid < 2 * CL) {
+    mbar_init(&s_blk[tid / CL][tid % CL], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -346,9 +348,11 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   // next contraction be scheduled (it waits for this kernel in turn)
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  uint32_t parity[2] = {0u, 0u};
+  uint32_t parity = 0u;  // bit b: phase parity awaited on the barriers of buffer b
   int nbcast = 0;
   bool timed_out = false;
+  bool wait_failed = false;  // a per-block wait of this thread gave up
+  constexpr uint32_t kBlockBytes = sizeof(float) * NB * XLD;
 
   float* X = Xa;   // current iterate
   float* dn = Xb;  // next iterate (the same offset in every CTA of the cluster)
@@ -357,41 +361,70 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     X = dn;
     dn = tt;
   };
+  auto buf_of = [&](const float* b) { return b == Xa ? 0 : 1; };
+  auto no_wait = [](int) {};
   // P = alpha X B_blk + beta_self X[:, blk] + gamma Gb, zero outside k x k,
-  // staged (with this CTA's statistics s_abs, s_err, s_fro in the padding
-  // rows KP.. of its first column) and sent to every rank's next buffer;
-  // returns once the whole next iterate has arrived (false on a timeout)
-  auto times_and_broadcast = [&](float alpha, float beta_self, const float* Gsrc, float gamma) {
+  // with this CTA's statistics s_nrm, s_err, s_fro in the padding rows KP..
+  // of its first column: written into this CTA's block of the next buffer
+  // and, staged, sent to every other rank's.  Returns without waiting: block
+  // q of a buffer completes on that buffer's barrier s_blk[.][q].
+  auto times_and_send = [&](float alpha, float beta_self, const float* Gsrc, float gamma) {
     float* Otc = Ot + (nbcast & 1) * NB * XLD;
     ++nbcast;
-    step_tiles<KP, CL, kProdTimes>(X, Ab, c0, part, [&](const float (&acc)[4], int m0, int n0, int) {
+    float* own = dn + c0 * XLD;
+    step_tiles<KP, CL, kProdTimes>(X, Ab, c0, part, no_wait, [&](const float (&acc)[4], int m0, int n0, int) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int r = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
         float v = alpha * acc[q] + beta_self * X[col * XLD + r];
         if (Gsrc) v += gamma * Gsrc[jb * XLD + r];
-        Otc[jb * XLD + r] = (r < k && col < k) ? v : 0.f;
+        v = (r < k && col < k) ? v : 0.f;
+        Otc[jb * XLD + r] = v;
+        if (!S::SB) own[jb * XLD + r] = v;  // the other buffer: nobody reads it now
       }
     });
     if (tid == 0) {
-      Otc[KP] = s_abs;
+      Otc[KP] = s_nrm;
       Otc[KP + 1] = s_err;
       Otc[KP + 2] = s_fro;
+      if (!S::SB) {
+        own[KP] = s_nrm;
+        own[KP + 1] = s_err;
+        own[KP + 2] = s_fro;
+      }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // staging -> async proxy
     __syncthreads();
-    // single buffer: every CTA has finished reading the current iterate
-    // before any copy overwrites it
-    if (S::SB) cluster.sync();
-    const int bi = dn == Xa ? 0 : 1;
-    // one issuing thread per warp: copies issued by lanes of one warp serialise
-    if (lane == 0 && (tid >> 5) < CL)
-      bulk_copy_to_rank(dn + c0 * XLD, Otc, (uint32_t)(sizeof(float) * NB * XLD), &s_full[bi],
-                        (uint32_t)(tid >> 5));
-    if (tid == 0) mbar_arrive_expect_tx(&s_full[bi], (uint32_t)(sizeof(float) * KP * XLD));
-    const bool ok = mbar_wait_bounded(&s_full[bi], parity[bi]);
-    parity[bi] ^= 1u;
+    if (S::SB) {
+      // single buffer: every CTA has finished reading the current iterate
+      // before any copy, or this CTA's own block, overwrites it
+      cluster.sync();
+      for (int e = tid; e < NB * XLD; e += blockDim.x) own[e] = Otc[e];
+      __syncthreads();
+    }
+    const int bi = buf_of(dn), w = tid >> 5;
+    // one issuing thread per warp (copies issued by lanes of one warp
+    // serialise); a CTA's copies leave about in warp order at the SM's
+    // outgoing bandwidth, so rank q sends to q+1, q+2, ... first: every rank
+    // then receives its blocks spread over the exchange, not all at its end
+    if (lane == 0 && w < CL - 1)
+      bulk_copy_to_rank(own, Otc, kBlockBytes, &s_blk[bi][rank], (uint32_t)((rank + 1 + w) % CL));
+    if (tid < CL && tid != rank) mbar_arrive_expect_tx(&s_blk[bi][tid], kBlockBytes);
+  };
+  // every block of X has arrived (false after a timeout of any thread's wait)
+  auto wait_all = [&]() -> bool {
+    const int bi = buf_of(X);
+    bool ok = !wait_failed;
+    if (tid < CL && tid != rank) ok = mbar_wait_bounded(&s_blk[bi][tid], (parity >> bi) & 1u) && ok;
+    parity ^= 1u << bi;
+    wait_failed = false;
     return !__syncthreads_or(!ok);
+  };
+  // the blocks of X holding the columns that are rows m0 .. m0+15 of a Gram tile
+  auto wait_rows = [&](int tile) {
+    const int bi = buf_of(X), m0 = (tile % S::MT) * 16;
+    for (int q = m0 / NB; q <= (m0 + 15) / NB; ++q)
+      if (q != rank && !mbar_wait_bounded(&s_blk[bi][q], (parity >> bi) & 1u)) wait_failed = true;
   };
   if (a.step_mode == kStepOnline) {
     // G block (columns c0 .. c0+NB) from the per-CTA partials.  The first 8
@@ -466,7 +499,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       Gb[jb * XLD + j] = gval;
     }
     // Phi' = Phi - beta (3 theta Phi (Phi^T Phi)^.2 - gscale G)   (Util.cpp:259-272)
-    step_tiles<KP, CL, kProdGram>(X, nullptr, c0, part, [&](const float (&acc)[4], int m0, int n0, int) {
+    step_tiles<KP, CL, kProdGram>(X, nullptr, c0, part, no_wait, [&](const float (&acc)[4], int m0, int n0, int) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int i = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1);
@@ -474,11 +507,14 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       }
     });
     __syncthreads();
-    if (!times_and_broadcast(-a.beta * a.theta3, 1.f, Gb, a.beta * a.gscale)) timed_out = true;
+    times_and_send(-a.beta * a.theta3, 1.f, Gb, a.beta * a.gscale);
     swap_buffers();
+    if (!wait_all()) timed_out = true;
   }
   // Scaled Newton-Schulz polar iteration X <- X (3 a I - a^3 X^T X) / 2.
-  // After the first scaling every singular value of X lies in [l, 1]; with
+  // After the first scaling (by ||X^T X||_F^(-1/2): sigma_max^2 <= ||X^T X||_F,
+  // nearly equal when one singular value dominates, as the gradient term
+  // makes it) every singular value of X lies in [l, 1]; with
   // f(y) = 3y/2 - y^3/2 the step maps sigma to f(a sigma), and
   // a = sqrt(3 / (1 + l + l^2)) makes f(a l) = f(a), so the lower end grows by
   // up to sqrt(3) * 3/2 ~ 2.6x per iteration instead of 3/2 (the scaled
@@ -491,17 +527,20 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   // with the broadcast of X_{t+1}; if they show X_t had already converged,
   // X_{t+1} is discarded.  The scale of step t therefore uses
   // the statistics of A_{t-1}; every CTA derives the same a from the same
-  // exchanged numbers.
+  // exchanged numbers.  The exchange is bandwidth-bound, so the Gram of
+  // X_{t+1} starts while its blocks arrive: a warp waits only for the blocks
+  // holding its tile's columns, and the statistics are applied after the
+  // products (Ab holds A_blk until then).
   //
-  // gram_stats: A_blk = X^T X[:, blk] with its statistics (max column abs
-  // sum, max |A - I|, ||A - I||_F^2 over the block) in s_abs, s_err, s_fro,
-  // and Ab = d0 I + d1 A_blk.
-  // (per-tile partial statistics are summed by one thread in a fixed order,
-  // so the result does not depend on warp timing)
-  __shared__ float colpart[S::MT * NB], errpart[S::TILES], fropart[S::TILES];
-  auto gram_stats = [&](float d0, float d1) {
-    step_tiles<KP, CL, kProdGram>(X, nullptr, c0, part, [&](const float (&acc)[4], int m0, int n0, int tile) {
-      float er = 0.f, fr = 0.f, ca[2] = {0.f, 0.f};
+  // gram_stats: A_blk = X^T X[:, blk] into Ab with its statistics
+  // (||A||_F^2, max |A - I|, ||A - I||_F^2 over the block) in s_nrm, s_err,
+  // s_fro; pre(tile) runs before a warp reads the tile's columns.
+  // (per-tile partial statistics are reduced in a fixed order, so the
+  // result does not depend on warp timing)
+  __shared__ float nrmpart[S::TILES], errpart[S::TILES], fropart[S::TILES];
+  auto gram_stats = [&](auto&& pre) {
+    step_tiles<KP, CL, kProdGram>(X, nullptr, c0, part, pre, [&](const float (&acc)[4], int m0, int n0, int tile) {
+      float er = 0.f, fr = 0.f, na = 0.f;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int i = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
@@ -511,59 +550,47 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
           const float d = v - (diag ? 1.f : 0.f);
           er = fmaxf(er, fabsf(d));
           fr = fmaf(d, d, fr);
-          ca[q & 1] += fabsf(v);
+          na = fmaf(v, v, na);
         }
-        Ab[jb * XLD + i] = (diag ? d0 : 0.f) + d1 * v;
-      }
-#pragma unroll
-      for (int off = 4; off < 32; off <<= 1) {  // over g: lanes with the same t4
-        ca[0] += __shfl_xor_sync(0xffffffffu, ca[0], off);
-        ca[1] += __shfl_xor_sync(0xffffffffu, ca[1], off);
+        Ab[jb * XLD + i] = v;
       }
 #pragma unroll
       for (int off = 16; off; off >>= 1) {
         er = fmaxf(er, __shfl_xor_sync(0xffffffffu, er, off));
         fr += __shfl_xor_sync(0xffffffffu, fr, off);
-      }
-      const int mt = m0 / 16;
-      if (g == 0) {
-        colpart[mt * NB + n0 + 2 * t4] = ca[0];
-        colpart[mt * NB + n0 + 2 * t4 + 1] = ca[1];
+        na += __shfl_xor_sync(0xffffffffu, na, off);
       }
       if (lane == 0) {
+        nrmpart[tile] = na;
         errpart[tile] = er;
         fropart[tile] = fr;
       }
     });
     __syncthreads();
-    if (tid < 32) {  // warp 0: lane jb sums column jb, lane t takes tile t
-      float m = 0.f;
-      if (lane < NB) {
-#pragma unroll
-        for (int mt = 0; mt < S::MT; ++mt) m += colpart[mt * NB + lane];
-      }
+    if (tid < 32) {  // warp 0: lane t takes tile t
+      float m = lane < S::TILES ? nrmpart[lane] : 0.f;
       float e = lane < S::TILES ? errpart[lane] : 0.f;
       float f = lane < S::TILES ? fropart[lane] : 0.f;
 #pragma unroll
       for (int off = 16; off; off >>= 1) {
-        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+        m += __shfl_xor_sync(0xffffffffu, m, off);
         e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, off));
         f += __shfl_xor_sync(0xffffffffu, f, off);
       }
       if (lane == 0) {
-        s_abs = m;
+        s_nrm = m;
         s_err = e;
         s_fro = f;
       }
     }
     __syncthreads();
   };
-  // initial statistics: rank q's [abs sum | max error | Frobenius^2] go to
-  // red[q], red[CL + q], red[2 CL + q] of every rank
+  // initial statistics: rank q's [||A_blk||_F^2 | max error | Frobenius^2]
+  // go to red[q], red[CL + q], red[2 CL + q] of every rank
   auto post_stats = [&]() {
     if (tid < CL) {
       float* r = cluster.map_shared_rank(red, tid);
-      r[rank] = s_abs;
+      r[rank] = s_nrm;
       r[CL + rank] = s_err;
       r[2 * CL + rank] = s_fro;
     }
@@ -571,7 +598,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   // rank q's statistics at src[q * qs + {0, fs, 2 fs}], reduced by every
   // warp across its lanes (the xor butterfly gives every lane, and so every
   // warp and every CTA, the same bits: IEEE addition is commutative)
-  auto reduce_stats = [&](const float* src, int qs, int fs, float& gabs, float& gerr, float& gfro) {
+  auto reduce_stats = [&](const float* src, int qs, int fs, float& gnrm, float& gerr, float& gfro) {
     float x = 0.f, y = 0.f, z = 0.f;
     if (lane < CL) {
       x = src[lane * qs];
@@ -580,30 +607,39 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     }
 #pragma unroll
     for (int off = 16; off; off >>= 1) {
-      x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, off));
+      x += __shfl_xor_sync(0xffffffffu, x, off);
       y = fmaxf(y, __shfl_xor_sync(0xffffffffu, y, off));
       z += __shfl_xor_sync(0xffffffffu, z, off);
     }
-    gabs = x;
+    gnrm = x;
     gerr = y;
     gfro = z;
   };
-  // initial scaling: sigma_max^2 <= ||X^T X||_1
-  gram_stats(0.f, 1.f);
+  // Ab = d0 I + d1 A_blk
+  auto make_b = [&](float d0, float d1) {
+    for (int e = tid; e < NB * KP; e += blockDim.x) {
+      const int jb = e / KP, i = e % KP;
+      float* p = Ab + jb * XLD + i;
+      *p = fmaf(d1, *p, i == c0 + jb ? d0 : 0.f);
+    }
+    __syncthreads();
+  };
+  // initial scaling: sigma_max^2 <= ||X^T X||_F
+  gram_stats(no_wait);
   post_stats();
   cluster.sync();
   int it = 0;
   bool done = timed_out, last = false;
   if (!done) {
-    float gabs, gerr, gfro;
-    reduce_stats(red, 1, CL, gabs, gerr, gfro);
-    if (!(gerr == gerr) || !(gabs == gabs) || !(gfro == gfro)) {
+    float gnrm, gerr, gfro;
+    reduce_stats(red, 1, CL, gnrm, gerr, gfro);
+    if (!(gerr == gerr) || !(gnrm == gnrm) || !(gfro == gfro)) {
       if (tid == 0 && rank == 0) atomicOr(a.flags, kFlagNonFinite);
       done = true;
     } else if (gerr < a.ns_tol) {
       done = true;
-    } else if (gabs > 0.f) {
-      const float sc = rsqrtf(gabs);
+    } else if (gnrm > 0.f) {
+      const float sc = rsqrtf(sqrtf(gnrm));
       for (int e = tid; e < KP * XLD; e += blockDim.x) X[e] *= sc;
       __syncthreads();
     }
@@ -613,36 +649,58 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   // before the first broadcast of the loop)
   float lo = kNsLowerGuess;  // lower bound (guess at first) on sigma(X_t)
   float prev_err = 1e30f;    // max|A_{t-1} - I|
-  for (; !done && it < a.max_ns; ++it) {
-    const float al = prev_err < kNsPlainBelow ? 1.f : fminf(sqrtf(3.f / (1.f + lo + lo * lo)), kNsMaxScale);
-    // A_t, its statistics and the speculative B_t in one pass
-    gram_stats(1.5f * al, -0.5f * al * al * al);
-    if (!times_and_broadcast(1.f, 0.f, nullptr, 0.f)) {
+  float al_prev = 1.f;       // the scale of the step that made X_t
+  bool pending = false;      // blocks of X_t still arriving
+  // X_t (t = it) has arrived with the statistics of A_{t-1}: apply them.
+  // False once the loop stops, the result then being X_it.
+  auto receive = [&]() -> bool {
+    pending = false;
+    if (!wait_all()) {
       timed_out = true;
-      break;
+      return false;
     }
-    float gabs, gerr, gfro;
-    reduce_stats(dn + KP, NB * XLD, 1, gabs, gerr, gfro);  // A_t's statistics, from every rank
-    if (!(gerr == gerr) || !(gabs == gabs) || !(gfro == gfro)) {
+    float gnrm, gerr, gfro;
+    reduce_stats(X + KP, NB * XLD, 1, gnrm, gerr, gfro);
+    if (!(gerr == gerr) || !(gnrm == gnrm) || !(gfro == gfro)) {
       if (tid == 0 && rank == 0) atomicOr(a.flags, kFlagNonFinite);
       done = true;
-      break;
+      return false;
     }
-    if (gerr < a.ns_tol) {  // X_t was converged: keep it, drop X_{t+1}
+    if (gerr < a.ns_tol) {  // X_{t-1} was converged: keep it, drop X_t
+      if (!S::SB) {  // (a single buffer holds X_t only: keep that)
+        swap_buffers();
+        --it;
+      }
       done = true;
-      break;
+      return false;
     }
-    // bound for X_{t+1}: [lb, 1] -> [min(f(a lb), f(a)), 1]
+    // bound for X_t: [lb, 1] -> [min(f(a lb), f(a)), 1]
     const float lb = fmaxf(lo, sqrtf(fmaxf(0.f, 1.f - sqrtf(gfro))));
-    lo = al > 1.f ? fminf(ns_poly(al * lb), ns_poly(al)) : ns_poly(lb);
+    lo = al_prev > 1.f ? fminf(ns_poly(al_prev * lb), ns_poly(al_prev)) : ns_poly(lb);
     prev_err = gerr;
-    swap_buffers();
     if (last) {
       done = true;
-      ++it;
-      break;
+      return false;
     }
     if (gerr < 1e-3f) last = true;
+    return true;
+  };
+  while (!done) {
+    // when no further step will be taken, the statistics alone decide: no
+    // speculative Gram
+    const bool closing = pending && (last || it >= a.max_ns);
+    if (!closing) gram_stats([&](int tile) {
+      if (pending) wait_rows(tile);
+    });
+    if (pending && !receive()) break;
+    if (closing || it >= a.max_ns) break;
+    const float al = prev_err < kNsPlainBelow ? 1.f : fminf(sqrtf(3.f / (1.f + lo + lo * lo)), kNsMaxScale);
+    make_b(1.5f * al, -0.5f * al * al * al);
+    times_and_send(1.f, 0.f, nullptr, 0.f);
+    swap_buffers();
+    al_prev = al;
+    pending = true;
+    ++it;
   }
   if (timed_out) {
     if (tid == 0) atomicOr(a.flags, kFlagTimeout);
