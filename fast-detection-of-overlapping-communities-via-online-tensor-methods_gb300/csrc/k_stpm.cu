@@ -25,6 +25,7 @@
 
 #include <cstdlib>
 #include "k_stpm.cuh"
+#include "tc_util.cuh"
 
 #include <cooperative_groups.h>
 #include <cuda_bf16.h>
@@ -744,8 +745,54 @@ __global__ void __launch_bounds__(512, 1) stpm_step_batched(const StpmUpdateArgs
 // The FP32 form keeps FP32 accuracy through the 3xTF32 split; the BF16 form
 // reads y rounded to BF16, Phi as a BF16 pair (hi + lo: Z = hi^T y + lo^T y,
 // two MMAs), the coefficients C rounded to BF16, and accumulates in FP32.
+// Tensor-core form of the plain FP32 contraction (tcgen05.mma kind::tf32,
+// 3xTF32: D += Ahi Bhi + Ahi Blo + Alo Bhi), for KP in [64, 112].  Per tile
+// of TM = 32 nodes:
+//   [Z1 Z2] = Phi^T [y1 y2]      A = Phi  (M = i, K = j), B = y1 | y2 (N = 2 TM, K = j)
+//   C   = c0 Z1 Z2 + c2 (Z1 m2 + m1 Z2)   (TMEM -> registers -> shared)
+//   G  += y3^T C                 A = y3   (M = j, K = x), B = C   (N = i, K = x)
+// Z1, Z2 and G live in tensor memory (columns [0, TM), [TM, 2 TM),
+// [2 TM, 2 TM + KP)); G accumulates over the CTA's tiles.  Operands are
+// staged hi / lo in shared memory, K-major without swizzle; y3 is staged
+// transposed (node index along K).  An M = 128 operand of KP < 128 rows
+// reads its rows past KP from the buffer after it: their products land in
+// TMEM lanes that are never read.
+template <int KP>
+struct ContractTc {
+  static constexpr int TM = 32;
+  static constexpr uint32_t SBOJ = (KP / 4) * 128u;  // 8-row groups of a K = j operand
+  static constexpr uint32_t SBOX = (TM / 4) * 128u;  // 8-row groups of a K = x operand
+  static constexpr uint32_t PSZ = 4u * KP * KP, TSZ = 4u * TM * KP;
+  static constexpr uint32_t PH = 0, PL = PSZ;                                   // Phi, KP rows i
+  // y1 hi | y2 hi | y1 lo | y2 lo (TM rows x each): y1 and y2 stack into one
+  // operand of N = 2 TM rows, so one MMA makes Z1 and Z2 side by side
+  static constexpr uint32_t Y1H = 2 * PSZ, Y2H = Y1H + TSZ, Y1L = Y2H + TSZ, Y2L = Y1L + TSZ;
+  static constexpr uint32_t Y3H = Y2L + TSZ, Y3L = Y3H + TSZ;                   // KP rows j
+  static constexpr uint32_t CH = Y3L + TSZ, CLO = CH + TSZ;                     // KP rows i
+  static constexpr uint32_t END = CLO + TSZ;
+  static constexpr uint32_t READ_END =  // furthest byte read by an M = 128 operand
+      (Y3L + 16 * SBOX > PL + 16 * SBOJ) ? Y3L + 16 * SBOX : PL + 16 * SBOJ;
+  static constexpr uint32_t STAGE = 4u * (KP * KP + 3 * KP + 1);  // partial for the cluster sum
+  static constexpr uint32_t REGION0 = END > READ_END ? END : READ_END;
+  static constexpr uint32_t REGION = ((REGION0 > STAGE ? REGION0 : STAGE) + 127) / 128 * 128;
+  // alignment slack, m1 | m2, d-sums of the 4 node groups
+  static constexpr size_t smem = 1024 + REGION + sizeof(float) * (2 * KP + 4 * KP);
+  static constexpr uint32_t TMEM_COLS = 256;
+  static_assert(KP % 16 == 0 && KP >= 64 && KP <= 112, "tensor-core contraction: KP in [64, 112]");
+  static_assert(smem <= 227 * 1024, "tensor-core contraction shared memory");
+};
+
+template <int KP, bool TC>
+constexpr size_t contract_smem(size_t cuda_core_form) {
+  if constexpr (TC)
+    return ContractTc<KP>::smem;
+  else
+    return cuda_core_form;
+}
+
 template <int KP, int MODE, bool BF>
 struct Contract {
+  static constexpr bool TC = MODE == kModePlain && !BF && KP >= 64 && KP <= 112;
   using T = typename std::conditional<BF, __nv_bfloat16, float>::type;
   static constexpr int TM = BF ? 64 : 32;  // nodes per tile
   static constexpr int NZ = MODE == kModePlain ? 2 : 3;
@@ -770,7 +817,8 @@ struct Contract {
       sizeof(T) * ((size_t)NPHI * IB * PLD + (size_t)3 * TM * LDY + (size_t)NC * IB * LDC);
   static constexpr size_t stage_bytes = sizeof(float) * ((size_t)KP * IB + 3 * IB + 4);
   static constexpr size_t region = ((tile_bytes > stage_bytes ? tile_bytes : stage_bytes) + 15) / 16 * 16;
-  static constexpr size_t smem = region + sizeof(float) * (3 * IB + NW + NW * 3 * IB);
+  static constexpr size_t smem_mma = region + sizeof(float) * (3 * IB + NW + NW * 3 * IB);
+  static constexpr size_t smem = contract_smem<KP, TC>(smem_mma);
   static_assert(NBC <= 4, "one loss slot per column block");
 };
 
@@ -808,6 +856,330 @@ __device__ __forceinline__ void split_tf32(float v, uint32_t& hi, uint32_t& lo) 
   lo = __float_as_uint(v - __uint_as_float(hi));
 }
 
+// The cluster's CTAs staged their partials (column block cb: G block, 3
+// d-sums, loss) at the same shared-memory offset `stage`; CTA r sums a 1/CLP
+// slice over the cluster through DSMEM and writes it out.  Column block cb
+// writes loss slot cb of the 4 spare floats of the partial row (block 0 also
+// clears the unused slots).
+template <int KP, int IB, int NBC, int MODE>
+__device__ __forceinline__ void partial_cluster_sum(const StpmPartialArgs& a, float* stage, int cb,
+                                                    int i0) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int crank = (int)cluster.block_rank(), tid = threadIdx.x, NT = blockDim.x, k = a.k;
+  constexpr int CLP = kPartialCluster;
+  constexpr int STAGE = KP * IB + 3 * IB + 1;
+  cluster.sync();
+  float* gp = a.gpart + (int64_t)(blockIdx.x / CLP) * a.part_stride;
+  const int slice = (STAGE + CLP - 1) / CLP;
+  for (int e = crank * slice + tid; e < min(STAGE, (crank + 1) * slice); e += NT) {
+    float v = 0.f;
+#pragma unroll
+    for (int q = 0; q < CLP; ++q) v += cluster.map_shared_rank(stage, q)[e];
+    if (e < KP * IB) {
+      const int i = i0 + e / KP, j = e % KP;
+      if (i < k && j < k && MODE != kModeLoss) gp[(int64_t)i * k + j] = v;
+    } else if (e < KP * IB + 3 * IB) {
+      const int q = (e - KP * IB) / IB, i = i0 + (e - KP * IB) % IB;
+      if (i < k) gp[(int64_t)k * k + q * k + i] = v;
+    } else {
+      gp[(int64_t)k * k + 3 * k + cb] = v;
+    }
+  }
+  if (cb == 0 && crank == 0 && tid < 4 && tid >= NBC) gp[(int64_t)k * k + 3 * k + tid] = 0.f;
+  cluster.sync();  // keep shared memory alive until every remote read is done
+}
+
+// The tensor-core contraction of one CTA (plain mode, FP32): stages this
+// CTA's partial -- G column-major (stage[i KP + j]), the d-sums d1 (then
+// d2 = d3 = 0) and a zero loss -- at `stage`, as the CUDA-core form does.
+template <int KP>
+__device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblocks,
+                                            unsigned char* smraw, float* stage) {
+  using C = ContractTc<KP>;
+  constexpr int TM = C::TM, NT = 512, NQ = KP / 4;
+  __shared__ __align__(8) uint64_t bars[2];  // Z products done | G products done
+  __shared__ uint32_t tmem_slot;
+  unsigned char* base = smraw + ((1024 - (tc::sm_addr(smraw) & 1023)) & 1023);
+  float* mv = reinterpret_cast<float*>(base + C::REGION);  // m1 | m2
+  float* dsum = mv + 2 * KP;                               // d1 per node group (4 x KP)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int k = a.k;
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, C::TMEM_COLS);
+  if (tid == 0) {
+    tc::mbar_init(&bars[0], 1);
+    tc::mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // Staging tasks are laid out so that the 8 lanes of a quarter-warp write
+  // one whole core matrix (8 consecutive rows x 16 bytes, 128 contiguous
+  // bytes: no bank conflicts), and the global loads of a warp still cover
+  // whole 32-byte sectors.  y1, y2 (row x, 16-byte chunks along j): lane l
+  // takes row 8 g + (l & 7) and chunk 4 h + (l >> 3) of warp-task (g, h); y3
+  // (transposed: row j, 4 nodes along K): lane = j, four scalar loads.
+  // A tile's loads go to registers one tile ahead.
+  constexpr int T12 = 2 * TM * NQ, S12 = (T12 + NT - 1) / NT;
+  constexpr int T3 = KP * (TM / 4), S3 = (T3 + NT - 1) / NT;
+  static_assert(NQ % 4 == 0 && TM % 8 == 0, "warp-task shape");
+  uint4 p12[S12];
+  float p3[S3][4];
+  auto task12 = [&](int e, int& q, int& x, int& jq) {
+    const int l = e & 31, w = e >> 5;
+    x = 8 * (w % (TM / 8)) + (l & 7);
+    jq = 4 * ((w / (TM / 8)) % (NQ / 4)) + (l >> 3);
+    q = w / ((TM / 8) * (NQ / 4));
+  };
+  auto tile_nodes = [&](int64_t tile, int64_t& x0) {
+    x0 = a.begin + tile * TM;
+    const int64_t left = a.begin + a.count - x0;
+    return left < TM ? (int)left : TM;
+  };
+  auto load_tile = [&](int64_t tile) {
+    int64_t x0;
+    const int nv = tile_nodes(tile, x0);
+#pragma unroll
+    for (int s = 0; s < S12; ++s) {
+      const int e = tid + NT * s;
+      p12[s] = make_uint4(0u, 0u, 0u, 0u);
+      if (e < T12) {
+        int q, x, jq;
+        task12(e, q, x, jq);
+        const float* Y = q == 0 ? a.y1 : a.y2;
+        if (x < nv && 4 * jq < a.ldy)
+          p12[s] = __ldg(reinterpret_cast<const uint4*>(Y + (x0 + x) * a.ldy + 4 * jq));
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < S3; ++s) {
+      const int e = tid + NT * s, j = e % KP, xq = e / KP;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int x = 4 * xq + u;
+        p3[s][u] = (e < T3 && x < nv && j < a.ldy) ? __ldg(a.y3 + (x0 + x) * a.ldy + j) : 0.f;
+      }
+    }
+  };
+  auto store_tile = [&]() {
+#pragma unroll
+    for (int s = 0; s < S12; ++s) {
+      const int e = tid + NT * s;
+      if (e < T12) {
+        int q, x, jq;
+        task12(e, q, x, jq);
+        const float v[4] = {__uint_as_float(p12[s].x), __uint_as_float(p12[s].y),
+                            __uint_as_float(p12[s].z), __uint_as_float(p12[s].w)};
+        uint4 h;
+        float4 l;
+        tc::split4(v, h, l);
+        const uint32_t off = tc::kmajor_off(x, 4 * jq, C::SBOJ);
+        *reinterpret_cast<uint4*>(base + (q == 0 ? C::Y1H : C::Y2H) + off) = h;
+        *reinterpret_cast<float4*>(base + (q == 0 ? C::Y1L : C::Y2L) + off) = l;
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < S3; ++s) {
+      const int e = tid + NT * s, j = e % KP, xq = e / KP;
+      if (e < T3) {
+        uint4 h;
+        float4 l;
+        tc::split4(p3[s], h, l);
+        const uint32_t off = tc::kmajor_off(j, 4 * xq, C::SBOX);
+        *reinterpret_cast<uint4*>(base + C::Y3H + off) = h;
+        *reinterpret_cast<float4*>(base + C::Y3L + off) = l;
+      }
+    }
+  };
+  const int64_t ntiles = ceil_div_dev(a.count, TM);
+  // the first tile's loads are in flight during the Phi prologue
+  if ((int64_t)blockIdx.x < ntiles) load_tile(blockIdx.x);
+  // Phi hi / lo (operand row i = column i of Phi, contiguous in j), all of
+  // a thread's loads issued together; the partial dot products of its
+  // chunks with mu_1, mu_2 go to part[] (in the y area, free until the first
+  // tile is stored) and are summed per column in a fixed order: m_q = Phi^T mu_q
+  constexpr int PT = (KP * NQ + NT - 1) / NT;
+  auto task_phi = [&](int e, int& i, int& jq) {  // 8 rows i x 4 chunks per warp
+    const int l = e & 31, w = e >> 5;
+    i = 8 * (w % (KP / 8)) + (l & 7);
+    jq = 4 * (w / (KP / 8)) + (l >> 3);
+  };
+  float* mus = mv;                                          // mu_1 | mu_2 staged in mv
+  float* part = reinterpret_cast<float*>(base + C::Y1H);    // [q][i][jq]
+  static_assert(2 * KP * NQ * 4 <= 6 * C::TSZ, "partials fit the y area");
+  {
+    float v[PT][4];
+#pragma unroll
+    for (int t = 0; t < PT; ++t) {
+      int i, jq;
+      task_phi(tid + NT * t, i, jq);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int j = 4 * jq + u;
+        v[t][u] = (tid + NT * t < KP * NQ && i < k && j < k) ? __ldg(a.phi + (int64_t)i * k + j) : 0.f;
+      }
+    }
+    for (int e = tid; e < 2 * KP; e += NT) {
+      const float* mu = e < KP ? a.mu1 : a.mu2;
+      const int j = e % KP;
+      mus[e] = (mu && j < k) ? mu[j] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < PT; ++t) {
+      const int e = tid + NT * t;
+      int i, jq;
+      task_phi(e, i, jq);
+      if (e < KP * NQ) {
+        uint4 h;
+        float4 l;
+        tc::split4(v[t], h, l);
+        const uint32_t off = tc::kmajor_off(i, 4 * jq, C::SBOJ);
+        *reinterpret_cast<uint4*>(base + C::PH + off) = h;
+        *reinterpret_cast<float4*>(base + C::PL + off) = l;
+        float p1 = 0.f, p2 = 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          p1 = fmaf(v[t][u], mus[4 * jq + u], p1);
+          p2 = fmaf(v[t][u], mus[KP + 4 * jq + u], p2);
+        }
+        part[i * NQ + jq] = p1;
+        part[KP * NQ + i * NQ + jq] = p2;
+      }
+    }
+    __syncthreads();
+    float m = 0.f;
+    if (tid < 2 * KP) {
+      const float* pp = part + (tid / KP) * KP * NQ + (tid % KP) * NQ;
+#pragma unroll 4
+      for (int jq = 0; jq < NQ; ++jq) m += pp[jq];
+    }
+    __syncthreads();  // every read of mus done
+    if (tid < 2 * KP) mv[tid] = m;
+  }
+  for (int e = tid; e < 4 * KP; e += NT) dsum[e] = 0.f;
+
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_slot, sbase = tc::sm_addr(base);
+  const float cc0 = a.c0, cc2 = a.c2;
+  uint32_t ph_z = 0u, ph_g = 0u;
+  bool g_pending = false, timed_out = false, any = false;
+  int64_t tile = blockIdx.x;
+  for (; tile < ntiles; tile += nblocks) {
+    // the G products of the previous tile read y3 and C
+    if (g_pending) {
+      if (!tc::mbar_wait(&bars[1], ph_g)) timed_out = true;
+      ph_g ^= 1u;
+      g_pending = false;
+    }
+    if (__syncthreads_or(timed_out)) {
+      timed_out = true;
+      break;
+    }
+    store_tile();
+    int64_t x0;
+    const int nv = tile_nodes(tile, x0);
+    if (tile + nblocks < ntiles) load_tile(tile + nblocks);  // in flight during the MMAs
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+      // K-step ks starts 256 B further: + 16 in the descriptor's address field
+      constexpr uint32_t iz = tc::tf32_idesc(128, 2 * TM);
+      const uint64_t dph = tc::smem_desc(sbase + C::PH, 128, C::SBOJ);
+      const uint64_t dpl = tc::smem_desc(sbase + C::PL, 128, C::SBOJ);
+      const uint64_t dyh = tc::smem_desc(sbase + C::Y1H, 128, C::SBOJ);
+      const uint64_t dyl = tc::smem_desc(sbase + C::Y1L, 128, C::SBOJ);
+#pragma unroll
+      for (int ks = 0; ks < KP / 8; ++ks) {
+        const uint64_t ko = 16u * ks;
+        tc::mma_tf32(tmem, dph + ko, dyh + ko, iz, ks > 0 ? 1u : 0u);
+        tc::mma_tf32(tmem, dph + ko, dyl + ko, iz, 1u);
+        tc::mma_tf32(tmem, dpl + ko, dyh + ko, iz, 1u);
+      }
+      tc::commit(&bars[0]);
+    }
+    if (!tc::mbar_wait(&bars[0], ph_z)) timed_out = true;
+    ph_z ^= 1u;
+    tc::fence_after_sync();
+    {
+      // warp w: TMEM lanes (rows i) 32 (w % 4) .., nodes 8 (w / 4) .. + 7
+      const int sub = warp & 3, xg = warp >> 2, i = 32 * sub + lane;
+      const uint32_t lb = tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)(8 * xg);
+      float z1[8], z2[8];
+      tc::tmem_ld8(lb, z1);
+      tc::tmem_ld8(lb + TM, z2);
+      if (i < KP) {
+        const float m1 = mv[i], m2 = mv[KP + i];
+        float cv[8], d = 0.f;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const bool valid = 8 * xg + u < nv && i < k;
+          cv[u] = valid ? cc0 * z1[u] * z2[u] + cc2 * (z1[u] * m2 + m1 * z2[u]) : 0.f;
+          if (valid) d = fmaf(z1[u], z2[u], d);
+        }
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const float v[4] = {cv[4 * h2], cv[4 * h2 + 1], cv[4 * h2 + 2], cv[4 * h2 + 3]};
+          uint4 h;
+          float4 l;
+          tc::split4(v, h, l);
+          const uint32_t off = tc::kmajor_off(i, 8 * xg + 4 * h2, C::SBOX);
+          *reinterpret_cast<uint4*>(base + C::CH + off) = h;
+          *reinterpret_cast<float4*>(base + C::CLO + off) = l;
+        }
+        dsum[xg * KP + i] += d;
+      }
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+      constexpr uint32_t ig = tc::tf32_idesc(128, KP);
+      const uint32_t d = tmem + (uint32_t)(2 * TM);
+      const uint64_t dah = tc::smem_desc(sbase + C::Y3H, 128, C::SBOX);
+      const uint64_t dal = tc::smem_desc(sbase + C::Y3L, 128, C::SBOX);
+      const uint64_t dbh = tc::smem_desc(sbase + C::CH, 128, C::SBOX);
+      const uint64_t dbl = tc::smem_desc(sbase + C::CLO, 128, C::SBOX);
+#pragma unroll
+      for (int ks = 0; ks < TM / 8; ++ks) {
+        const uint64_t ko = 16u * ks;
+        tc::mma_tf32(d, dah + ko, dbh + ko, ig, (any || ks > 0) ? 1u : 0u);
+        tc::mma_tf32(d, dah + ko, dbl + ko, ig, 1u);
+        tc::mma_tf32(d, dal + ko, dbh + ko, ig, 1u);
+      }
+      tc::commit(&bars[1]);
+    }
+    g_pending = true;
+    any = true;
+  }
+  if (g_pending) {
+    if (!tc::mbar_wait(&bars[1], ph_g)) timed_out = true;
+    ph_g ^= 1u;
+  }
+  tc::fence_after_sync();
+  const bool ok = !__syncthreads_or(timed_out);
+  // the tiles are dead: stage the partial over them (stage <= base)
+  {
+    const int sub = warp & 3, cg4 = warp >> 2, j = 32 * sub + lane;
+    for (int c4 = 0; c4 < NQ; c4 += 4) {
+      const int ic = cg4 * NQ + c4;
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      if (ok && any) tc::tmem_ld4(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)(2 * TM + ic), v);
+      if (j < KP)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) stage[(ic + u) * KP + j] = v[u];
+    }
+  }
+  for (int e = tid; e < 3 * KP + 1; e += NT)
+    stage[KP * KP + e] = e < KP ? ((dsum[e] + dsum[KP + e]) + (dsum[2 * KP + e] + dsum[3 * KP + e])) : 0.f;
+  if (!ok && tid == 0 && a.flags) atomicOr(a.flags, kFlagTimeout);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, C::TMEM_COLS);
+}
+
 template <int KP, int MODE, bool BF>
 __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblocks) {
   using Cfg = Contract<KP, MODE, BF>;
@@ -821,6 +1193,13 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   extern __shared__ __align__(16) unsigned char smraw[];
+  if constexpr (Cfg::TC) {
+    static_assert(Cfg::NT == 512 && Cfg::NBC == 1, "tensor-core contraction launch shape");
+    float* stage = reinterpret_cast<float*>(smraw);
+    contract_tc<KP>(a, nblocks, smraw, stage);
+    partial_cluster_sum<KP, IB, Cfg::NBC, MODE>(a, stage, 0, 0);
+    return;
+  }
   // this CTA's columns of Phi: i0 + ii, ii < IB (i local below)
   const int cb = (Cfg::NBC > 1) ? (int)blockIdx.y : 0, i0 = cb * IB;
   T* Phis = reinterpret_cast<T*>(smraw);  // Phis[ii PLD + j] = Phi_j,i0+ii (column i0+ii of Phi)
@@ -1116,29 +1495,7 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
       for (int w = 0; w < NW; ++w) t += tred[w];
     stage[KP * IB + 3 * IB] = t;
   }
-  cg::cluster_group cluster = cg::this_cluster();
-  const int crank = (int)cluster.block_rank();
-  constexpr int CLP = kPartialCluster;
-  constexpr int STAGE = KP * IB + 3 * IB + 1;
-  cluster.sync();
-  float* gp = a.gpart + (int64_t)(blockIdx.x / CLP) * a.part_stride;
-  const int slice = (STAGE + CLP - 1) / CLP;
-  for (int e = crank * slice + tid; e < min(STAGE, (crank + 1) * slice); e += NT) {
-    float v = 0.f;
-#pragma unroll
-    for (int q = 0; q < CLP; ++q) v += cluster.map_shared_rank(stage, q)[e];
-    if (e < KP * IB) {
-      const int i = i0 + e / KP, j = e % KP;
-      if (i < k && j < k && MODE != kModeLoss) gp[(int64_t)i * k + j] = v;
-    } else if (e < KP * IB + 3 * IB) {
-      const int q = (e - KP * IB) / IB, i = i0 + (e - KP * IB) % IB;
-      if (i < k) gp[(int64_t)k * k + q * k + i] = v;
-    } else {
-      gp[(int64_t)k * k + 3 * k + cb] = v;
-    }
-  }
-  if (cb == 0 && crank == 0 && tid < 4 && tid >= Cfg::NBC) gp[(int64_t)k * k + 3 * k + tid] = 0.f;
-  cluster.sync();  // keep shared memory alive until every remote read is done
+  partial_cluster_sum<KP, IB, Cfg::NBC, MODE>(a, stage, cb, i0);
 }
 
 template <int KP, int MODE, bool BF>

@@ -35,6 +35,7 @@ struct StpmPartialArgs {
   float* gpart;          // [grid][part_stride]: k*k partial G, then 3k d-sums (+1 loss)
   int64_t part_stride;
   int nblocks;           // batched launches: CTAs of this graph (multiple of the cluster size)
+  unsigned* flags;       // device flag word (MMSB_ERR_TIMEOUT of a bounded wait), may be null
 };
 
 struct StpmReduceArgs {

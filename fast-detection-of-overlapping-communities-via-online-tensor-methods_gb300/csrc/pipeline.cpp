@@ -596,6 +596,7 @@ StpmPartialArgs stpm_partial_args(mmsb_ctx* c, int q1, int q2, int q3, int64_t b
   a.gpart = gpart;
   a.part_stride = stride;
   a.nblocks = nblocks;
+  a.flags = c->flags;
   return a;
 }
 
