@@ -631,6 +631,8 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   cluster.sync();
   int it = 0;
   bool done = timed_out, last = false;
+  bool gram_ready = false;  // Ab and s_* already hold the Gram of X (scaled first iterate)
+  __shared__ float wred[3][16];
   if (!done) {
     float gnrm, gerr, gfro;
     reduce_stats(red, 1, CL, gnrm, gerr, gfro);
@@ -640,9 +642,52 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     } else if (gerr < a.ns_tol) {
       done = true;
     } else if (gnrm > 0.f) {
-      const float sc = rsqrtf(sqrtf(gnrm));
+      const float sc = rsqrtf(sqrtf(gnrm)), sc2 = sc * sc;
       for (int e = tid; e < KP * XLD; e += blockDim.x) X[e] *= sc;
+      // the Gram of the scaled iterate is sc^2 A: its block and statistics
+      // without a second product
+      float er = 0.f, fr = 0.f, na = 0.f;
+      for (int e = tid; e < NB * KP; e += blockDim.x) {
+        const int jb = e / KP, i = e % KP, col = c0 + jb;
+        float* pa = Ab + jb * XLD + i;
+        const float v = *pa * sc2;
+        *pa = v;
+        if (i < k && col < k) {
+          const float d = v - (i == col ? 1.f : 0.f);
+          er = fmaxf(er, fabsf(d));
+          fr = fmaf(d, d, fr);
+          na = fmaf(v, v, na);
+        }
+      }
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        er = fmaxf(er, __shfl_xor_sync(0xffffffffu, er, off));
+        fr += __shfl_xor_sync(0xffffffffu, fr, off);
+        na += __shfl_xor_sync(0xffffffffu, na, off);
+      }
+      if (lane == 0) {
+        wred[0][tid >> 5] = na;
+        wred[1][tid >> 5] = er;
+        wred[2][tid >> 5] = fr;
+      }
       __syncthreads();
+      if (tid < 32) {
+        float m = lane < 16 ? wred[0][lane] : 0.f, e = lane < 16 ? wred[1][lane] : 0.f,
+              f = lane < 16 ? wred[2][lane] : 0.f;
+#pragma unroll
+        for (int off = 16; off; off >>= 1) {
+          m += __shfl_xor_sync(0xffffffffu, m, off);
+          e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, off));
+          f += __shfl_xor_sync(0xffffffffu, f, off);
+        }
+        if (lane == 0) {
+          s_nrm = m;
+          s_err = e;
+          s_fro = f;
+        }
+      }
+      __syncthreads();
+      gram_ready = true;
     }
   }
   // (red[] is written only by post_stats above, and every CTA finished its
@@ -690,9 +735,10 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     // when no further step will be taken, the statistics alone decide: no
     // speculative Gram
     const bool closing = pending && (last || it >= a.max_ns);
-    if (!closing) gram_stats([&](int tile) {
+    if (!closing && !gram_ready) gram_stats([&](int tile) {
       if (pending) wait_rows(tile);
     });
+    gram_ready = false;
     if (pending && !receive()) break;
     if (closing || it >= a.max_ns) break;
     const float al = prev_err < kNsPlainBelow ? 1.f : fminf(sqrtf(3.f / (1.f + lo + lo * lo)), kNsMaxScale);
@@ -1773,7 +1819,13 @@ int stpm_partial_grid(int64_t count, bool bf16) {
   // 4,096-node minibatches at k = 100, 64 CTAs beat 128 (44 vs 53 us in FP32;
   // staging Phi and the cluster reduction are per-CTA costs)
   (void)bf16;
-  const int64_t tiles = ceil_div(count, 64);
+  // MMSB_CONTRACT_NODES overrides the 64 nodes per CTA (a tuning override)
+  static const int64_t per_cta = []() {
+    const char* e = std::getenv("MMSB_CONTRACT_NODES");
+    const long v = e ? std::strtol(e, nullptr, 10) : 0;
+    return v >= 16 ? (int64_t)v : (int64_t)64;
+  }();
+  const int64_t tiles = ceil_div(count, per_cta);
   // MMSB_CONTRACT_CTAS caps the contraction CTAs of single-graph runs (a
   // tuning override; default 2 per SM)
   static const int64_t cap = []() {
