@@ -173,9 +173,9 @@ def peaks():
 
 
 # DRAM bytes (read + write) per launch of the STPM kernels, from the ncu
-# capture summarised in profiles/stpm_kernels_tensor_n20k_full.md (k = 100,
-# 4,096-node minibatches: the same per-launch shapes as the full workload)
-NCU_TRAFFIC_PER_LAUNCH = {"stpm_step_kernel": 270592, "stpm_contract_kernel": 5031424}
+# capture summarised in profiles/stpm_kernels_n200k_k100_full.md (this
+# workload: k = 100, 4,096-node minibatches)
+NCU_TRAFFIC_PER_LAUNCH = {"stpm_step_kernel": 436480, "stpm_contract_kernel": 5014784}
 
 
 # ---------------------------------------------------------------------------
@@ -369,7 +369,8 @@ def run_ours(args, wl, ws, rank, local):
                            "3xTF32 mma.sync on a KP/8-CTA cluster)", kern["step_ms"],
                            kern["step_flops"], kern["step_launches"])
     contract_rf = tensor_entry("stpm_contract_kernel (Z = Phi^T y, alpha0 terms, G += y^T C; "
-                               "3xTF32 mma.sync)", kern["contract_ms"], kern["contract_flops"],
+                               "3xTF32 tcgen05 kind::tf32, accumulators in tensor memory)",
+                               kern["contract_ms"], kern["contract_flops"],
                                kern["contract_launches"])
     spmm_achieved = (spmm_bytes / max(spmm_ms, 1e-9) / 1e6) if spmm_ms > 0 else None
     spmm_rf = {"kernel": "spmm_rows_kernel (whitening CSR SpMM)", "bound": "hbm",
