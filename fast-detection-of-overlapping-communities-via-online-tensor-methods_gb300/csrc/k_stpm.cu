@@ -531,7 +531,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   // exchanged numbers.  The exchange is bandwidth-bound, so the Gram of
   // X_{t+1} starts while its blocks arrive: a warp waits only for the blocks
   // holding its tile's columns, and the statistics are applied after the
-  // products (Ab holds A_blk until then).
+  // products.
   //
   // gram_stats: A_blk = X^T X[:, blk] into Ab with its statistics
   // (||A||_F^2, max |A - I|, ||A - I||_F^2 over the block) in s_nrm, s_err,
@@ -615,15 +615,6 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     gnrm = x;
     gerr = y;
     gfro = z;
-  };
-  // Ab = d0 I + d1 A_blk
-  auto make_b = [&](float d0, float d1) {
-    for (int e = tid; e < NB * KP; e += blockDim.x) {
-      const int jb = e / KP, i = e % KP;
-      float* p = Ab + jb * XLD + i;
-      *p = fmaf(d1, *p, i == c0 + jb ? d0 : 0.f);
-    }
-    __syncthreads();
   };
   // initial scaling: sigma_max^2 <= ||X^T X||_F
   gram_stats(no_wait);
@@ -742,8 +733,8 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     if (pending && !receive()) break;
     if (closing || it >= a.max_ns) break;
     const float al = prev_err < kNsPlainBelow ? 1.f : fminf(sqrtf(3.f / (1.f + lo + lo * lo)), kNsMaxScale);
-    make_b(1.5f * al, -0.5f * al * al * al);
-    times_and_send(1.f, 0.f, nullptr, 0.f);
+    // X (d0 I + d1 A)[:, blk] = d1 (X A_blk) + d0 X[:, blk], d0 = 3a/2, d1 = -a^3/2
+    times_and_send(-0.5f * al * al * al, 1.5f * al, nullptr, 0.f);
     swap_buffers();
     al_prev = al;
     pending = true;

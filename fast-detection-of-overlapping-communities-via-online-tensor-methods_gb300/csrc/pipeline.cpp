@@ -127,8 +127,9 @@ void check_device_flags(mmsb_ctx* c, const char* stage) { check_flags(c, stage);
 
 // Symmetric positive semi-definite eigen-decomposition (n <= 512), eigenvalues
 // descending: FP32 one-sided Jacobi on the Cholesky factor (run to
-// convergence), then four FP64 Ogita-Aishima refinement steps (quadratic
-// convergence to FP64 accuracy from a converged FP32 start).
+// convergence), then three FP64 Ogita-Aishima refinement steps (quadratic
+// convergence from a converged FP32 start: 1e-7 -> 1e-14 -> FP64 round-off,
+// the third a margin).
 void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A, double* evals,
                      double* V, const double* factor, cudaStream_t stream) {
   cudaStream_t s = stream ? stream : c->s;
@@ -151,7 +152,7 @@ void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A
   ck(eig_from_factor(n, Y, lam, X, work, c->flags, s), "jacobi");
   double* dstate = c->tbuf<double>(tag + ".edelta", 4);  // delta + three maxima
   ck(cudaMemsetAsync(dstate, 0, 4 * sizeof(double), s), "delta");
-  for (int step = 0; step < 4; ++step) {
+  for (int step = 0; step < 3; ++step) {
     ck(dgemm_small(true, false, n, n, n, 1.0, X, n, X, n, 0.0, G, n, s), "X^T X");
     ck(dgemm_small(false, false, n, n, n, 1.0, A, n, X, n, 0.0, AX, n, s), "A X");
     ck(dgemm_small(true, false, n, n, n, 1.0, X, n, AX, n, 0.0, S, n, s), "X^T A X");

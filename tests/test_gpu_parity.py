@@ -64,7 +64,7 @@ def test_spmm_weighted_and_empty(mm):
 @pytest.mark.parametrize("kind", ["wishart", "graded"])
 @pytest.mark.parametrize("n", [6, 20, 64, 200])
 def test_symeig_vs_numpy(mm, n, kind):
-    """FP32 one-sided Jacobi run to convergence + four FP64 Ogita-Aishima
+    """FP32 one-sided Jacobi run to convergence + three FP64 Ogita-Aishima
     refinement steps: FP64-level eigen-pairs on a Wishart spectrum and on a
     graded one spanning five decades."""
     rng = np.random.default_rng(n)
