@@ -123,8 +123,10 @@ cudaError_t fill_f64(double* p, int64_t n, double v, cudaStream_t s);
 cudaError_t axpy_f64(int64_t n, double a, const double* x, double* y, cudaStream_t s);
 
 // ---- small element-wise helpers (k_misc.cu) -----------------------------------
-// *out = ||phi - snap||_F (FP64; out may be null), then snap = phi (n floats).
-cudaError_t phi_delta(int64_t n, const float* phi, float* snap, double* out, cudaStream_t s);
+// conv[i] = sqrt of the sum of parts[i * stride + 0 .. used - 1] (the step
+// kernel's per-CTA trace partials), for i < count
+cudaError_t conv_sum(const double* parts, int count, int stride, int used, double* conv,
+                     cudaStream_t s);
 
 cudaError_t sig_from_evals(int k, const double* ev, double* sig, cudaStream_t s);
 cudaError_t scale_cols_pinv(int rows, int k, double* F, int ldf, const double* sig, double tol,

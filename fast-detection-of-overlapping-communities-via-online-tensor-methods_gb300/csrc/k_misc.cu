@@ -160,31 +160,22 @@ unsigned blocks(int64_t n, int T = 256) {
 
 // ||Phi - snap||_F (FP64) into *out, then snap = Phi (one CTA): the
 // convergence trace of the online methods, one value per sweep
-__global__ void __launch_bounds__(256) phi_delta_kernel(int64_t n, const float* __restrict__ phi,
-                                                        float* __restrict__ snap,
-                                                        double* __restrict__ out) {
-  __shared__ double red[8];
-  double s = 0.0;
-  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
-    const double d = (double)phi[e] - (double)snap[e];
-    s = fma(d, d, s);
-    snap[e] = phi[e];
-  }
-#pragma unroll
-  for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < 8; ++w) t += red[w];
-    if (out) *out = sqrt(t);
-  }
+// conv[i] = sqrt(sum_q parts[i * stride + q]), q < used (fixed order)
+__global__ void conv_sum_kernel(const double* __restrict__ parts, int count, int stride, int used,
+                                double* __restrict__ conv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  double t = 0.0;
+  for (int q = 0; q < used; ++q) t += parts[(int64_t)i * stride + q];
+  conv[i] = sqrt(t);
 }
 
 }  // namespace
 
-cudaError_t phi_delta(int64_t n, const float* phi, float* snap, double* out, cudaStream_t s) {
-  phi_delta_kernel<<<1, 256, 0, s>>>(n, phi, snap, out);
+cudaError_t conv_sum(const double* parts, int count, int stride, int used, double* conv,
+                     cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  conv_sum_kernel<<<(unsigned)ceil_div((int64_t)count, 128), 128, 0, s>>>(parts, count, stride, used, conv);
   ++g_launch_count;
   return cudaGetLastError();
 }

@@ -750,6 +750,28 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     const int r = e % KP, col = c0 + e / KP;
     if (r < k && col < k) a.phi[(int64_t)col * k + r] = X[col * XLD + r];
   }
+  if (a.trace_out) {  // ||Phi_new - snapshot||_F^2 over this CTA's columns, fixed order
+    double d2 = 0.0;
+    for (int e = tid; e < KP * NB; e += blockDim.x) {
+      const int r = e % KP, col = c0 + e / KP;
+      if (r < k && col < k) {
+        const float v = X[col * XLD + r];
+        const double d = (double)v - (double)a.trace_snap[(int64_t)col * k + r];
+        d2 = fma(d, d, d2);
+        a.trace_snap[(int64_t)col * k + r] = v;
+      }
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) d2 += __shfl_xor_sync(0xffffffffu, d2, off);
+    __shared__ double tpart[16];
+    if (lane == 0) tpart[tid >> 5] = d2;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += tpart[w];
+      a.trace_out[rank] = t;
+    }
+  }
   cluster.sync();  // keep shared memory alive until remote writers are done
   if (timed_out) __nanosleep(100000);  // let copies a stalled exchange left in flight land
 }

@@ -78,6 +78,10 @@ struct StpmUpdateArgs {
   unsigned* flags;
   int* ns_iters;         // accumulates Newton-Schulz iterations
   int active;            // batched launches: 0 = no update for this graph in this round
+  // convergence trace (may be null): CTA q writes sum over its columns of
+  // (Phi_new - trace_snap)^2 to trace_out[q] and sets trace_snap = Phi_new there
+  float* trace_snap;
+  double* trace_out;
 };
 
 int stpm_kp(int k);

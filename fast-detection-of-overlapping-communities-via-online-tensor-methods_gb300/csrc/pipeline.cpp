@@ -721,10 +721,13 @@ int64_t stpm_online_rounds(const mmsb_ctx* c) {
 
 // one minibatch update: partial contractions, then the fused reduction +
 // Phi - beta (3 theta O - gscale G) + polar orthonormalisation on one cluster
-static void stpm_step(mmsb_ctx* c, const OnlineRound& rd, bool timed = true) {
+static void stpm_step(mmsb_ctx* c, const OnlineRound& rd, bool timed = true,
+                      float* trace_snap = nullptr, double* trace_out = nullptr) {
   c->ksample = timed;
   PartialOut po = stpm_partials(c, rd.mode, 0, 1, 2, rd.x0, rd.cnt, rd.c0, rd.c2, rd.bf16);
   StpmUpdateArgs u = stpm_online_update_args(c, rd, po.gpart, po.stride, po.grid);
+  u.trace_snap = trace_snap;
+  u.trace_out = trace_out;
   timed_launch(c, 1, [&]() { ck(stpm_update(u, c->s), "stpm_step"); });
 }
 
@@ -835,19 +838,28 @@ void pipeline_stpm(mmsb_ctx* c, const double* phi0) {
   }
   const int64_t rounds = stpm_online_rounds(c);
   const int64_t per = std::max<int64_t>(1, rounds / std::max(1, c->cfg.sweeps));
-  // ||Phi - Phi at the previous sweep's end||_F after every sweep
+  // ||Phi - Phi at the previous sweep's end||_F after every sweep: the step
+  // kernel that ends a sweep writes one partial per CTA (at most 16), summed
+  // once after the loop
+  constexpr int kTraceStride = 16;
+  const int64_t ntrace = rounds / per;
   float* snap = c->tbuf<float>("phi_snap", (size_t)k * k);
-  c->conv = c->tbuf<double>("conv", (size_t)std::max(1, c->cfg.sweeps));
+  double* tparts = c->tbuf<double>("conv_parts", (size_t)std::max<int64_t>(1, ntrace) * kTraceStride);
+  c->conv = c->tbuf<double>("conv", (size_t)std::max<int64_t>(1, ntrace));
   c->conv_count = 0;
-  ck(phi_delta((int64_t)k * k, c->phi, snap, nullptr, s), "trace");
+  ck(cudaMemcpyAsync(snap, c->phi, sizeof(float) * k * k, cudaMemcpyDeviceToDevice, s), "trace");
+  ck(cudaMemsetAsync(tparts, 0, sizeof(double) * std::max<int64_t>(1, ntrace) * kTraceStride, s),
+     "trace");
   OnlineRound rd;
   for (int64_t r = 0; r < rounds; ++r) {
     if (c->stop.load()) throw MmsbError(MMSB_ERR_STOPPED, "stop requested");
     stpm_online_round(c, r, &rd);
-    stpm_step(c, rd, r % 8 == 0);
-    if ((r + 1) % per == 0)
-      ck(phi_delta((int64_t)k * k, c->phi, snap, c->conv + c->conv_count++, s), "trace");
+    const bool ends_sweep = (r + 1) % per == 0 && c->conv_count < ntrace;
+    stpm_step(c, rd, r % 8 == 0, ends_sweep ? snap : nullptr,
+              ends_sweep ? tparts + c->conv_count * kTraceStride : nullptr);
+    if (ends_sweep) ++c->conv_count;
   }
+  ck(conv_sum(tparts, (int)c->conv_count, kTraceStride, kTraceStride, c->conv, s), "trace");
   stpm_finish_online(c, rounds);
 }
 

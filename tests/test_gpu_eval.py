@@ -51,6 +51,25 @@ def test_convergence_traces(mm, solved):
         assert abs(tb[-1] - q.stats()["stpm_last_error"]) <= 1e-12 * max(1.0, tb[-1])
 
 
+def test_online_trace_matches_sweep_snapshots(mm, solved):
+    """Entry s of the online trace is ||Phi after sweep s+1 - Phi after sweep s||_F:
+    the same runs stopped after 4 and 5 sweeps give those two iterates (the
+    schedule does not depend on the sweep count; columns aligned for the final
+    lambda sign fix)."""
+    g, p = solved
+    tr = p.convergence()
+    snaps = []
+    for sweeps in (4, 5):
+        with mm.Pipeline(k=10, alpha0=1.0, stpm_method=mm.STPM_ONLINE, sweeps=sweeps,
+                         minibatch=100, tau=0.3) as q:
+            q.upload(g).whiten().stpm()
+            snaps.append(q.phi())
+    a, b = snaps
+    b = b * np.where(np.sum(a * b, axis=0) < 0, -1.0, 1.0)
+    d = float(np.linalg.norm(b - a))
+    assert abs(tr[4] - d) <= 1e-4 * d + 1e-6, (tr[4], d)
+
+
 def test_gpu_tree_output_files(solved, tmp_path):
     g, p = solved
     p.write_gpu_outputs(tmp_path)
