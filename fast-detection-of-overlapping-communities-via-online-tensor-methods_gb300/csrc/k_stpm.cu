@@ -1048,21 +1048,33 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
     }
   };
   const int64_t ntiles = ceil_div_dev(a.count, TM);
-  // the first tile's loads are in flight during the Phi prologue
-  if ((int64_t)blockIdx.x < ntiles) load_tile(blockIdx.x);
+  float* mus = mv;  // mu_1 | mu_2 staged in mv
+  // Launched as a programmatic dependent of the step that writes Phi: all
+  // that does not read Phi -- TMEM, barriers, mu and the whole first node
+  // tile -- is done before the wait and overlaps that kernel's tail.
+  const bool first_staged = (int64_t)blockIdx.x < ntiles;
+  if (first_staged) load_tile(blockIdx.x);
+  for (int e = tid; e < 2 * KP; e += NT) {
+    const float* mu = e < KP ? a.mu1 : a.mu2;
+    const int j = e % KP;
+    mus[e] = (mu && j < k) ? mu[j] : 0.f;
+  }
+  for (int e = tid; e < 4 * KP; e += NT) dsum[e] = 0.f;
+  if (first_staged) store_tile();
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   // Phi hi / lo (operand row i = column i of Phi, contiguous in j), all of
   // a thread's loads issued together; the partial dot products of its
-  // chunks with mu_1, mu_2 go to part[] (in the y area, free until the first
-  // tile is stored) and are summed per column in a fixed order: m_q = Phi^T mu_q
+  // chunks with mu_1, mu_2 go to part[] (in the C area, free until the first
+  // epilogue) and are summed per column in a fixed order: m_q = Phi^T mu_q
   constexpr int PT = (KP * NQ + NT - 1) / NT;
   auto task_phi = [&](int e, int& i, int& jq) {  // 8 rows i x 4 chunks per warp
     const int l = e & 31, w = e >> 5;
     i = 8 * (w % (KP / 8)) + (l & 7);
     jq = 4 * (w / (KP / 8)) + (l >> 3);
   };
-  float* mus = mv;                                          // mu_1 | mu_2 staged in mv
-  float* part = reinterpret_cast<float*>(base + C::Y1H);    // [q][i][jq]
-  static_assert(2 * KP * NQ * 4 <= 6 * C::TSZ, "partials fit the y area");
+  float* part = reinterpret_cast<float*>(base + C::CH);  // [q][i][jq]
+  static_assert(2 * KP * NQ * 4 <= 2 * C::TSZ, "partials fit the C area");
   {
     float v[PT][4];
 #pragma unroll
@@ -1075,12 +1087,7 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
         v[t][u] = (tid + NT * t < KP * NQ && i < k && j < k) ? __ldg(a.phi + (int64_t)i * k + j) : 0.f;
       }
     }
-    for (int e = tid; e < 2 * KP; e += NT) {
-      const float* mu = e < KP ? a.mu1 : a.mu2;
-      const int j = e % KP;
-      mus[e] = (mu && j < k) ? mu[j] : 0.f;
-    }
-    __syncthreads();
+    __syncthreads();  // mus staged
 #pragma unroll
     for (int t = 0; t < PT; ++t) {
       const int e = tid + NT * t;
@@ -1113,7 +1120,6 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
     __syncthreads();  // every read of mus done
     if (tid < 2 * KP) mv[tid] = m;
   }
-  for (int e = tid; e < 4 * KP; e += NT) dsum[e] = 0.f;
 
   tc::fence_before_sync();
   __syncthreads();
@@ -1134,7 +1140,7 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
       timed_out = true;
       break;
     }
-    store_tile();
+    if (tile != (int64_t)blockIdx.x) store_tile();  // the first tile was staged before the wait
     int64_t x0;
     const int nv = tile_nodes(tile, x0);
     if (tile + nblocks < ntiles) load_tile(tile + nblocks);  // in flight during the MMAs
@@ -1247,18 +1253,18 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
                 LDC = Cfg::LDC;
   constexpr int IB = Cfg::IB;
   static_assert(KP % 16 == 0 && KP <= 256, "KP");
-  // programmatic serialization: wait for the previous kernel (the step that
-  // wrote Phi), then let the next one be scheduled early
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   extern __shared__ __align__(16) unsigned char smraw[];
-  if constexpr (Cfg::TC) {
+  if constexpr (Cfg::TC) {  // waits for the previous kernel itself, after its own prologue
     static_assert(Cfg::NT == 512 && Cfg::NBC == 1, "tensor-core contraction launch shape");
     float* stage = reinterpret_cast<float*>(smraw);
     contract_tc<KP>(a, nblocks, smraw, stage);
     partial_cluster_sum<KP, IB, Cfg::NBC, MODE>(a, stage, 0, 0);
     return;
   }
+  // programmatic serialization: wait for the previous kernel (the step that
+  // wrote Phi), then let the next one be scheduled early
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   // this CTA's columns of Phi: i0 + ii, ii < IB (i local below)
   const int cb = (Cfg::NBC > 1) ? (int)blockIdx.y : 0, i0 = cb * IB;
   T* Phis = reinterpret_cast<T*>(smraw);  // Phis[ii PLD + j] = Phi_j,i0+ii (column i0+ii of Phi)
