@@ -841,10 +841,46 @@ struct ContractTc {
   static_assert(smem <= 227 * 1024, "tensor-core contraction shared memory");
 };
 
-template <int KP, bool TC>
+// BF16 tensor-core form of the adjoint contraction (tcgen05.mma kind::f16,
+// BF16 operands, FP32 accumulation), for KP in [64, 112]: per tile of TM = 64
+// nodes
+//   [Z1 Z2 Z3] = Phi^T [y1 y2 y3]  A = Phi as a BF16 hi / lo pair (M = i, K = j),
+//                                  B = y1 | y2 | y3 (N = 3 TM, K = j)
+//   C_1..3 (alpha0 terms of the Z pairs, BF16)       TMEM -> registers -> shared
+//   G += sum_c y_c^T C_c           A = y_c staged transposed (M = j, K = x),
+//                                  B = C_c (N = i, K = x)
+// Z in TMEM columns [0, 3 TM), G in [3 TM, 3 TM + KP).  16-bit operands: a
+// core matrix is 8 rows x 8 elements, one MMA consumes K = 16.
+template <int KP>
+struct ContractTcBf {
+  static constexpr int TM = 64;
+  static constexpr uint32_t SBOJ = (KP / 8) * 128u;  // 8-row groups of a K = j operand
+  static constexpr uint32_t SBOX = (TM / 8) * 128u;  // 8-row groups of a K = x operand
+  static constexpr uint32_t PSZ = 2u * KP * KP, TSZ = 2u * TM * KP;
+  static constexpr uint32_t PH = 0, PL = PSZ;   // Phi hi / lo, KP rows i
+  static constexpr uint32_t YB = 2 * PSZ;       // y1 | y2 | y3, TM rows x each
+  static constexpr uint32_t YT = YB + 3 * TSZ;  // y_c transposed, KP rows j each
+  static constexpr uint32_t CB = YT + 3 * TSZ;  // C_c, KP rows i each
+  static constexpr uint32_t END = CB + 3 * TSZ;
+  static constexpr uint32_t READ_END =  // furthest byte an M = 128 operand reads (Phi lo, y3^T)
+      (YT + 2 * TSZ + 16 * SBOX > PL + 16 * SBOJ) ? YT + 2 * TSZ + 16 * SBOX : PL + 16 * SBOJ;
+  static constexpr uint32_t STAGE = 4u * (KP * KP + 3 * KP + 1);
+  static constexpr uint32_t REGION0 = END > READ_END ? END : READ_END;
+  static constexpr uint32_t REGION = ((REGION0 > STAGE ? REGION0 : STAGE) + 127) / 128 * 128;
+  // alignment slack, m1 | m2 | m3, d-sums (3 pairs x 4 node groups)
+  static constexpr size_t smem = 1024 + REGION + sizeof(float) * (3 * KP + 12 * KP);
+  static constexpr uint32_t TMEM_COLS = 512;
+  static_assert(KP % 16 == 0 && KP >= 64 && KP <= 112, "BF16 tensor-core contraction: KP in [64, 112]");
+  static_assert(3 * TM + KP <= 512, "tensor memory columns");
+  static_assert(smem <= 227 * 1024, "BF16 tensor-core contraction shared memory");
+};
+
+template <int KP, bool TC, bool TCBF>
 constexpr size_t contract_smem(size_t cuda_core_form) {
   if constexpr (TC)
     return ContractTc<KP>::smem;
+  else if constexpr (TCBF)
+    return ContractTcBf<KP>::smem;
   else
     return cuda_core_form;
 }
@@ -852,6 +888,7 @@ constexpr size_t contract_smem(size_t cuda_core_form) {
 template <int KP, int MODE, bool BF>
 struct Contract {
   static constexpr bool TC = MODE == kModePlain && !BF && KP >= 64 && KP <= 112;
+  static constexpr bool TCBF = MODE == kModeAdjoint && BF && KP >= 64 && KP <= 112;
   using T = typename std::conditional<BF, __nv_bfloat16, float>::type;
   static constexpr int TM = BF ? 64 : 32;  // nodes per tile
   static constexpr int NZ = MODE == kModePlain ? 2 : 3;
@@ -877,7 +914,7 @@ struct Contract {
   static constexpr size_t stage_bytes = sizeof(float) * ((size_t)KP * IB + 3 * IB + 4);
   static constexpr size_t region = ((tile_bytes > stage_bytes ? tile_bytes : stage_bytes) + 15) / 16 * 16;
   static constexpr size_t smem_mma = region + sizeof(float) * (3 * IB + NW + NW * 3 * IB);
-  static constexpr size_t smem = contract_smem<KP, TC>(smem_mma);
+  static constexpr size_t smem = contract_smem<KP, TC, TCBF>(smem_mma);
   static_assert(NBC <= 4, "one loss slot per column block");
 };
 
@@ -1245,6 +1282,300 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
   if (warp == 0) tc::tmem_dealloc(tmem, C::TMEM_COLS);
 }
 
+// The BF16 tensor-core adjoint contraction of one CTA: stages this CTA's
+// partial (G column-major at stage[i KP + j], the three d-sums, a zero loss)
+// at `stage`, as the CUDA-core form does.
+template <int KP>
+__device__ __forceinline__ void contract_tc_bf(const StpmPartialArgs& a, int nblocks,
+                                               unsigned char* smraw, float* stage) {
+  using C = ContractTcBf<KP>;
+  constexpr int TM = C::TM, NT = 512, NJ = KP / 8;  // 16-byte chunks (8 elements) along j
+  __shared__ __align__(8) uint64_t bars[2];  // Z products done | G products done
+  __shared__ uint32_t tmem_slot;
+  unsigned char* base = smraw + ((1024 - (tc::sm_addr(smraw) & 1023)) & 1023);
+  float* mv = reinterpret_cast<float*>(base + C::REGION);  // m1 | m2 | m3
+  float* dsum = mv + 3 * KP;                               // [pair][node group][i]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int k = a.k;
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, C::TMEM_COLS);
+  if (tid == 0) {
+    tc::mbar_init(&bars[0], 1);
+    tc::mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // Node tiles, one tile ahead in registers.  Row form (B of the Z product):
+  // task (q, x, chunk) = one 16-byte load of y_q's row x; the 8 lanes of a
+  // quarter-warp take 8 consecutive rows, so they write one whole core matrix.
+  // Transposed form (A of the G product): task (c, j, node chunk) = 8 scalar
+  // loads of column j (lanes along j: coalesced) packed into one 16-byte row.
+  constexpr int TR = 3 * TM * NJ, SR = (TR + NT - 1) / NT;
+  constexpr int TT = 3 * KP * (TM / 8), ST = (TT + NT - 1) / NT;
+  uint4 pr[SR], pt[ST];
+  auto yh = [&](int q) {
+    return static_cast<const unsigned short*>(q == 0 ? a.yh1 : q == 1 ? a.yh2 : a.yh3);
+  };
+  auto task_row = [&](int e, int& q, int& x, int& jc) {
+    const int grp = e >> 3, rest = grp / (TM / 8);
+    x = 8 * (grp % (TM / 8)) + (e & 7);
+    jc = rest % NJ;
+    q = rest / NJ;
+  };
+  auto tile_nodes = [&](int64_t tile, int64_t& x0) {
+    x0 = a.begin + tile * TM;
+    const int64_t left = a.begin + a.count - x0;
+    return left < TM ? (int)left : TM;
+  };
+  auto load_tile = [&](int64_t tile) {
+    int64_t x0;
+    const int nv = tile_nodes(tile, x0);
+#pragma unroll
+    for (int s = 0; s < SR; ++s) {
+      const int e = tid + NT * s;
+      pr[s] = make_uint4(0u, 0u, 0u, 0u);
+      if (e < TR) {
+        int q, x, jc;
+        task_row(e, q, x, jc);
+        if (x < nv && 8 * jc < a.ldyh)
+          pr[s] = __ldg(reinterpret_cast<const uint4*>(yh(q) + (x0 + x) * a.ldyh + 8 * jc));
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < ST; ++s) {
+      const int e = tid + NT * s, j = e % KP, rest = e / KP, xc = rest % (TM / 8), c = rest / (TM / 8);
+      uint32_t w[4] = {0u, 0u, 0u, 0u};
+      if (e < TT && j < a.ldyh) {
+        const unsigned short* Yc = yh(c);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int x = 8 * xc + u;
+          const uint32_t v = x < nv ? (uint32_t)__ldg(Yc + (x0 + x) * a.ldyh + j) : 0u;
+          w[u >> 1] |= v << (16 * (u & 1));
+        }
+      }
+      pt[s] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  };
+  auto store_tile = [&]() {
+#pragma unroll
+    for (int s = 0; s < SR; ++s) {
+      const int e = tid + NT * s;
+      if (e < TR) {
+        int q, x, jc;
+        task_row(e, q, x, jc);
+        *reinterpret_cast<uint4*>(base + C::YB + q * C::TSZ + tc::kmajor16_off(x, 8 * jc, C::SBOJ)) = pr[s];
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < ST; ++s) {
+      const int e = tid + NT * s, j = e % KP, rest = e / KP, xc = rest % (TM / 8), c = rest / (TM / 8);
+      if (e < TT)
+        *reinterpret_cast<uint4*>(base + C::YT + c * C::TSZ + tc::kmajor16_off(j, 8 * xc, C::SBOX)) = pt[s];
+    }
+  };
+  const int64_t ntiles = ceil_div_dev(a.count, TM);
+  float* mus = mv;  // mu_1 | mu_2 | mu_3 staged in mv
+  // everything that does not read Phi happens before the dependency wait
+  const bool first_staged = (int64_t)blockIdx.x < ntiles;
+  if (first_staged) load_tile(blockIdx.x);
+  for (int e = tid; e < 3 * KP; e += NT) {
+    const float* mu = e < KP ? a.mu1 : e < 2 * KP ? a.mu2 : a.mu3;
+    const int j = e % KP;
+    mus[e] = (mu && j < k) ? mu[j] : 0.f;
+  }
+  for (int e = tid; e < 12 * KP; e += NT) dsum[e] = 0.f;
+  if (first_staged) store_tile();
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  // Phi as a BF16 pair (hi = bf16(Phi), lo = bf16(Phi - hi)); the partial dot
+  // products of each chunk with mu_1..3 (FP32 Phi) go to part[] in the C
+  // area and are summed per column in a fixed order: m_q = Phi^T mu_q
+  constexpr int PT = (KP * NJ + NT - 1) / NT;
+  float* part = reinterpret_cast<float*>(base + C::CB);  // [q][i][jc]
+  static_assert(3 * KP * NJ * 4 <= 3 * C::TSZ, "partials fit the C area");
+  {
+    float v[PT][8];
+#pragma unroll
+    for (int t = 0; t < PT; ++t) {
+      const int e = tid + NT * t, grp = e >> 3, i = 8 * (grp % (KP / 8)) + (e & 7), jc = grp / (KP / 8);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = 8 * jc + u;
+        v[t][u] = (e < KP * NJ && i < k && j < k) ? __ldg(a.phi + (int64_t)i * k + j) : 0.f;
+      }
+    }
+    __syncthreads();  // mus staged
+#pragma unroll
+    for (int t = 0; t < PT; ++t) {
+      const int e = tid + NT * t, grp = e >> 3, i = 8 * (grp % (KP / 8)) + (e & 7), jc = grp / (KP / 8);
+      if (e < KP * NJ) {
+        uint32_t h[4] = {0u, 0u, 0u, 0u}, l[4] = {0u, 0u, 0u, 0u};
+        float p1 = 0.f, p2 = 0.f, p3 = 0.f;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const __nv_bfloat16 hb = __float2bfloat16_rn(v[t][u]);
+          const __nv_bfloat16 lb = __float2bfloat16_rn(v[t][u] - __bfloat162float(hb));
+          h[u >> 1] |= (uint32_t)__bfloat16_as_ushort(hb) << (16 * (u & 1));
+          l[u >> 1] |= (uint32_t)__bfloat16_as_ushort(lb) << (16 * (u & 1));
+          p1 = fmaf(v[t][u], mus[8 * jc + u], p1);
+          p2 = fmaf(v[t][u], mus[KP + 8 * jc + u], p2);
+          p3 = fmaf(v[t][u], mus[2 * KP + 8 * jc + u], p3);
+        }
+        const uint32_t off = tc::kmajor16_off(i, 8 * jc, C::SBOJ);
+        *reinterpret_cast<uint4*>(base + C::PH + off) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4*>(base + C::PL + off) = make_uint4(l[0], l[1], l[2], l[3]);
+        part[i * NJ + jc] = p1;
+        part[KP * NJ + i * NJ + jc] = p2;
+        part[2 * KP * NJ + i * NJ + jc] = p3;
+      }
+    }
+    __syncthreads();
+    float m = 0.f;
+    if (tid < 3 * KP) {
+      const float* pp = part + (tid / KP) * KP * NJ + (tid % KP) * NJ;
+#pragma unroll 2
+      for (int jc = 0; jc < NJ; ++jc) m += pp[jc];
+    }
+    __syncthreads();  // every read of mus done
+    if (tid < 3 * KP) mv[tid] = m;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_slot, sbase = tc::sm_addr(base);
+  const float cc0 = a.c0, cc2 = a.c2;
+  uint32_t ph_z = 0u, ph_g = 0u;
+  bool g_pending = false, timed_out = false, any = false;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += nblocks) {
+    if (g_pending) {  // the G products of the previous tile read y^T and C
+      if (!tc::mbar_wait(&bars[1], ph_g)) timed_out = true;
+      ph_g ^= 1u;
+      g_pending = false;
+    }
+    if (__syncthreads_or(timed_out)) {
+      timed_out = true;
+      break;
+    }
+    if (tile != (int64_t)blockIdx.x) store_tile();
+    int64_t x0;
+    const int nv = tile_nodes(tile, x0);
+    if (tile + nblocks < ntiles) load_tile(tile + nblocks);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+      constexpr uint32_t iz = tc::bf16_idesc(128, 3 * TM);
+      const uint64_t dph = tc::smem_desc(sbase + C::PH, 128, C::SBOJ);
+      const uint64_t dpl = tc::smem_desc(sbase + C::PL, 128, C::SBOJ);
+      const uint64_t dy = tc::smem_desc(sbase + C::YB, 128, C::SBOJ);
+#pragma unroll
+      for (int ks = 0; ks < KP / 16; ++ks) {
+        const uint64_t ko = 16u * ks;  // 256 bytes: two core matrices along K
+        tc::mma_bf16(tmem, dph + ko, dy + ko, iz, ks > 0 ? 1u : 0u);
+        tc::mma_bf16(tmem, dpl + ko, dy + ko, iz, 1u);
+      }
+      tc::commit(&bars[0]);
+    }
+    if (!tc::mbar_wait(&bars[0], ph_z)) timed_out = true;
+    ph_z ^= 1u;
+    tc::fence_after_sync();
+    {
+      // warp w: TMEM lanes (rows i) 32 (w % 4) .., nodes 16 (w / 4) .. + 15
+      const int sub = warp & 3, xg = warp >> 2, i = 32 * sub + lane;
+      const uint32_t lb = tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)(16 * xg);
+      const float m1 = i < KP ? mv[i] : 0.f, m2 = i < KP ? mv[KP + i] : 0.f,
+                  m3 = i < KP ? mv[2 * KP + i] : 0.f;
+      float d0 = 0.f, d1 = 0.f, d2 = 0.f;
+#pragma unroll
+      for (int h2 = 0; h2 < 2; ++h2) {  // 8 nodes at a time (warp-wide TMEM loads)
+        float z1[8], z2[8], z3[8];
+        tc::tmem_ld8(lb + 8 * h2, z1);
+        tc::tmem_ld8(lb + TM + 8 * h2, z2);
+        tc::tmem_ld8(lb + 2 * TM + 8 * h2, z3);
+        if (i < KP) {
+          uint32_t w0[4] = {0u, 0u, 0u, 0u}, w1[4] = {0u, 0u, 0u, 0u}, w2[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const bool valid = 16 * xg + 8 * h2 + u < nv && i < k;
+            const float a1 = z1[u], a2 = z2[u], a3 = z3[u];
+            const float v0 = valid ? cc0 * a2 * a3 + cc2 * (a2 * m3 + m2 * a3) : 0.f;
+            const float v1 = valid ? cc0 * a1 * a3 + cc2 * (a1 * m3 + m1 * a3) : 0.f;
+            const float v2 = valid ? cc0 * a1 * a2 + cc2 * (a1 * m2 + m1 * a2) : 0.f;
+            if (valid) {
+              d0 = fmaf(a2, a3, d0);
+              d1 = fmaf(a1, a3, d1);
+              d2 = fmaf(a1, a2, d2);
+            }
+            const int sh = 16 * (u & 1);
+            w0[u >> 1] |= (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v0)) << sh;
+            w1[u >> 1] |= (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v1)) << sh;
+            w2[u >> 1] |= (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v2)) << sh;
+          }
+          const uint32_t off = tc::kmajor16_off(i, 16 * xg + 8 * h2, C::SBOX);
+          *reinterpret_cast<uint4*>(base + C::CB + off) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+          *reinterpret_cast<uint4*>(base + C::CB + C::TSZ + off) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+          *reinterpret_cast<uint4*>(base + C::CB + 2 * C::TSZ + off) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+        }
+      }
+      if (i < KP) {
+        dsum[(0 * 4 + xg) * KP + i] += d0;
+        dsum[(1 * 4 + xg) * KP + i] += d1;
+        dsum[(2 * 4 + xg) * KP + i] += d2;
+      }
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+      constexpr uint32_t ig = tc::bf16_idesc(128, KP);
+      const uint32_t d = tmem + (uint32_t)(3 * TM);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const uint64_t da = tc::smem_desc(sbase + C::YT + c * C::TSZ, 128, C::SBOX);
+        const uint64_t db = tc::smem_desc(sbase + C::CB + c * C::TSZ, 128, C::SBOX);
+#pragma unroll
+        for (int ks = 0; ks < TM / 16; ++ks)
+          tc::mma_bf16(d, da + 16u * ks, db + 16u * ks, ig, (any || c > 0 || ks > 0) ? 1u : 0u);
+      }
+      tc::commit(&bars[1]);
+    }
+    g_pending = true;
+    any = true;
+  }
+  if (g_pending) {
+    if (!tc::mbar_wait(&bars[1], ph_g)) timed_out = true;
+    ph_g ^= 1u;
+  }
+  tc::fence_after_sync();
+  const bool ok = !__syncthreads_or(timed_out);
+  {
+    const int sub = warp & 3, cg4 = warp >> 2, j = 32 * sub + lane;
+    constexpr int NQ = KP / 4;
+    for (int c4 = 0; c4 < NQ; c4 += 4) {
+      const int ic = cg4 * NQ + c4;
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      if (ok && any)
+        tc::tmem_ld4(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)(3 * TM + ic), v);
+      if (j < KP)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) stage[(ic + u) * KP + j] = v[u];
+    }
+  }
+  for (int e = tid; e < 3 * KP + 1; e += NT) {
+    float v = 0.f;
+    if (e < 3 * KP) {
+      const float* ds = dsum + (e / KP) * 4 * KP + e % KP;
+      v = (ds[0] + ds[KP]) + (ds[2 * KP] + ds[3 * KP]);
+    }
+    stage[KP * KP + e] = v;
+  }
+  if (!ok && tid == 0 && a.flags) atomicOr(a.flags, kFlagTimeout);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, C::TMEM_COLS);
+}
+
 template <int KP, int MODE, bool BF>
 __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblocks) {
   using Cfg = Contract<KP, MODE, BF>;
@@ -1258,6 +1589,12 @@ __device__ __forceinline__ void contract_body(const StpmPartialArgs& a, int nblo
     static_assert(Cfg::NT == 512 && Cfg::NBC == 1, "tensor-core contraction launch shape");
     float* stage = reinterpret_cast<float*>(smraw);
     contract_tc<KP>(a, nblocks, smraw, stage);
+    partial_cluster_sum<KP, IB, Cfg::NBC, MODE>(a, stage, 0, 0);
+    return;
+  } else if constexpr (Cfg::TCBF) {  // likewise
+    static_assert(Cfg::NT == 512 && Cfg::NBC == 1, "tensor-core contraction launch shape");
+    float* stage = reinterpret_cast<float*>(smraw);
+    contract_tc_bf<KP>(a, nblocks, smraw, stage);
     partial_cluster_sum<KP, IB, Cfg::NBC, MODE>(a, stage, 0, 0);
     return;
   }
