@@ -805,7 +805,7 @@ __global__ void __launch_bounds__(512, 1) stpm_step_batched(const StpmUpdateArgs
 // reads y rounded to BF16, Phi as a BF16 pair (hi + lo: Z = hi^T y + lo^T y,
 // two MMAs), the coefficients C rounded to BF16, and accumulates in FP32.
 // Tensor-core form of the plain FP32 contraction (tcgen05.mma kind::tf32,
-// 3xTF32: D += Ahi Bhi + Ahi Blo + Alo Bhi), for KP in [64, 112].  Per tile
+// 3xTF32: D += Ahi Bhi + Ahi Blo + Alo Bhi), for KP in [32, 112].  Per tile
 // of TM = 32 nodes:
 //   [Z1 Z2] = Phi^T [y1 y2]      A = Phi  (M = i, K = j), B = y1 | y2 (N = 2 TM, K = j)
 //   C   = c0 Z1 Z2 + c2 (Z1 m2 + m1 Z2)   (TMEM -> registers -> shared)
@@ -837,12 +837,12 @@ struct ContractTc {
   // alignment slack, m1 | m2, d-sums of the 4 node groups
   static constexpr size_t smem = 1024 + REGION + sizeof(float) * (2 * KP + 4 * KP);
   static constexpr uint32_t TMEM_COLS = 256;
-  static_assert(KP % 16 == 0 && KP >= 64 && KP <= 112, "tensor-core contraction: KP in [64, 112]");
+  static_assert(KP % 16 == 0 && KP >= 32 && KP <= 112, "tensor-core contraction: KP in [32, 112]");
   static_assert(smem <= 227 * 1024, "tensor-core contraction shared memory");
 };
 
 // BF16 tensor-core form of the adjoint contraction (tcgen05.mma kind::f16,
-// BF16 operands, FP32 accumulation), for KP in [64, 112]: per tile of TM = 64
+// BF16 operands, FP32 accumulation), for KP in [32, 112]: per tile of TM = 64
 // nodes
 //   [Z1 Z2 Z3] = Phi^T [y1 y2 y3]  A = Phi as a BF16 hi / lo pair (M = i, K = j),
 //                                  B = y1 | y2 | y3 (N = 3 TM, K = j)
@@ -870,7 +870,7 @@ struct ContractTcBf {
   // alignment slack, m1 | m2 | m3, d-sums (3 pairs x 4 node groups)
   static constexpr size_t smem = 1024 + REGION + sizeof(float) * (3 * KP + 12 * KP);
   static constexpr uint32_t TMEM_COLS = 512;
-  static_assert(KP % 16 == 0 && KP >= 64 && KP <= 112, "BF16 tensor-core contraction: KP in [64, 112]");
+  static_assert(KP % 16 == 0 && KP >= 32 && KP <= 112, "BF16 tensor-core contraction: KP in [32, 112]");
   static_assert(3 * TM + KP <= 512, "tensor memory columns");
   static_assert(smem <= 227 * 1024, "BF16 tensor-core contraction shared memory");
 };
@@ -887,8 +887,8 @@ constexpr size_t contract_smem(size_t cuda_core_form) {
 
 template <int KP, int MODE, bool BF>
 struct Contract {
-  static constexpr bool TC = MODE == kModePlain && !BF && KP >= 64 && KP <= 112;
-  static constexpr bool TCBF = MODE == kModeAdjoint && BF && KP >= 64 && KP <= 112;
+  static constexpr bool TC = MODE == kModePlain && !BF && KP <= 112;
+  static constexpr bool TCBF = MODE == kModeAdjoint && BF && KP <= 112;
   using T = typename std::conditional<BF, __nv_bfloat16, float>::type;
   static constexpr int TM = BF ? 64 : 32;  // nodes per tile
   static constexpr int NZ = MODE == kModePlain ? 2 : 3;
