@@ -20,7 +20,7 @@ namespace mmsb {
 namespace {
 
 constexpr int kTcM = 128, kTcN = 128, kTcK = 32;  // tile edge, rows per stage
-constexpr int kTcThreads = 256;
+constexpr int kTcThreads = 512;  // 16 warps: the staging is issue-bound
 constexpr uint32_t kStageBytes = 4u * (2 * kTcM * kTcK + 2 * kTcN * kTcK);  // Ahi Alo Bhi Blo
 constexpr uint32_t kTcSmem = 2 * kStageBytes + 1024;  // + alignment slack
 
@@ -109,7 +109,7 @@ gram_tc_kernel(const float* __restrict__ A, int lda, int pa, const float* __rest
   // (lanes along m), then one 16-byte store each of hi and lo into the core
   // matrix row (m, 4 kq .. 4 kq + 3).  The next chunk's loads are issued
   // before this chunk's barrier and MMAs, so their latency overlaps them.
-  constexpr int kTasks = 2 * kTcM * (kTcK / 4) / kTcThreads;  // 8
+  constexpr int kTasks = 2 * kTcM * (kTcK / 4) / kTcThreads;  // 4
   float v[kTasks][4];
   auto load_chunk = [&](int c) {
     const int64_t rb = r0 + (int64_t)c * kTcK;
@@ -210,13 +210,14 @@ gram_tc_kernel(const float* __restrict__ A, int lda, int pa, const float* __rest
     }
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (rows m), columns
-  // [64 (w / 4), +64) (n), 16 at a time
+  // [kCols (w / 4), +kCols) (n), 16 at a time
   if (!timed_out && nchunks > 0) {
+    constexpr int kGroups = kTcThreads / 128, kCols = kTcN / kGroups;  // column groups of warps
     const int q = warp & 3, half = warp >> 2;
     const int m = m0 + 32 * q + lane;
     double* out = partials + (int64_t)blockIdx.z * pa * pb;
-    for (int cb = 0; cb < 64; cb += 16) {
-      const int col = 64 * half + cb;
+    for (int cb = 0; cb < kCols; cb += 16) {
+      const int col = kCols * half + cb;
       uint32_t v[16];
       const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)col;
       asm volatile(
