@@ -175,7 +175,7 @@ def peaks():
 # DRAM bytes (read + write) per launch of the STPM kernels, from the ncu
 # capture summarised in profiles/stpm_kernels_n200k_k100_full.md (this
 # workload: k = 100, 4,096-node minibatches)
-NCU_TRAFFIC_PER_LAUNCH = {"stpm_step_kernel": 436480, "stpm_contract_kernel": 5014784}
+NCU_TRAFFIC_PER_LAUNCH = {"stpm_step_kernel": 436480, "stpm_contract_kernel": 5017344}
 
 
 # ---------------------------------------------------------------------------
