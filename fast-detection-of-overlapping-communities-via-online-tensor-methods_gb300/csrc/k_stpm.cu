@@ -583,8 +583,11 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
         s_err = e;
         s_fro = f;
       }
+      __syncwarp();
     }
-    __syncthreads();
+    // no barrier: s_* are read only by warp 0 (post_stats, the staging of
+    // the next broadcast); the block barrier above published A_blk, and
+    // nrm/err/fropart are next written after several more barriers
   };
   // initial statistics: rank q's [||A_blk||_F^2 | max error | Frobenius^2]
   // go to red[q], red[CL + q], red[2 CL + q] of every rank
