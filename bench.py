@@ -275,8 +275,7 @@ def run_ours(args, wl, ws, rank, local):
         p.run()
     p.synchronize()
     dist.barrier()
-    clocks = ClockSampler(local, ROOT / "gpurun_out" / "clocks.csv"
-                          if (ROOT / "gpurun_out").is_dir() else None)
+    clocks = ClockSampler(local, Path(args.clocks_csv) if args.clocks_csv else None)
     clocks.start()
     dev_ms, spmm_ms, spmm_bytes, spmm_launch, launches = [], 0.0, 0.0, 0, 0
     ns_iters, stpm_steps = 0, 0
@@ -686,6 +685,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--clocks-csv", default=None,
+                    help="also write the SM clock samples of the timed region to this CSV file")
     ap.add_argument("--n", type=int, default=None, help="override node count (testing)")
     ap.add_argument("--batch", action="store_true",
                     help="the batching configuration (256 graphs) instead of the default")

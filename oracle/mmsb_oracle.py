@@ -1,8 +1,8 @@
 """FP64 CPU restatement of the reference's MMSB tensor-method path -- the ORACLE.
 
 This module is test infrastructure: only tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline leg use it, always as the checker, never as the thing
-measured or shipped.  The GPU library never calls it.
+bench.py's CPU-baseline leg use it, always as the oracle results are compared
+with, never as the thing measured or shipped.  The GPU library never calls it.
 
 Parity is pinned by tests/golden/: fixtures produced by the reference's own CPU
 implementation (CommunityDetectionSoftware_CPU, compiled unmodified by

@@ -1,6 +1,6 @@
 // Test-infrastructure harness around the reference's own CPU implementation.
 //
-// This file is part of the ORACLE (checker), never of the product.  It links
+// This file is part of the ORACLE (test infrastructure), never of the product.  It links
 // the unmodified reference sources CommunityDetectionSoftware_CPU/CommunityDetection/
 // {IOfn,Probability,Spectral,Util}.cpp (vendored Eigen 3.2.1) and replaces only
 // the reference's `main` (CommunityDetection.cpp:16-149) so that every stage's
