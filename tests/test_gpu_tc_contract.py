@@ -1,4 +1,4 @@
-"""k in (48, 112] (padded to 64 ... 112): the online STPM's contraction runs on
+"""k up to 112 (padded to 64, 80 and 112 here): the online STPM's contraction runs on
 the tensor cores (tcgen05, 3xTF32, Z and G in tensor memory).  Online sweeps
 against the FP64 oracle on the device's own whitened data, with tolerances
 set by the oracle's own response to a 1e-6 relative perturbation of y."""
@@ -14,7 +14,7 @@ def rel(a, b):
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("k,minibatch", [(64, 500), (100, 700), (100, 64)])
+@pytest.mark.parametrize("k,minibatch", [(64, 500), (75, 500), (100, 700), (100, 64)])
 def test_tensor_core_contraction_online_vs_oracle(mm, oracle, k, minibatch):
     a0 = 0.5
     g = mm.generate(8000, k, a0, 0.2, 0.002, seed=k + 1)
@@ -47,7 +47,7 @@ def _bf16(v):
     return r.view(np.float32).astype(np.float64)
 
 
-@pytest.mark.parametrize("k", [64, 100])
+@pytest.mark.parametrize("k", [64, 75, 100])
 def test_bf16_adjoint_tensor_core_vs_oracle(mm, oracle, k):
     """BF16 form of the adjoint method (tcgen05 kind::f16 contraction for all
     sweeps but the last, which refines in FP32) against the FP64 oracle; the
