@@ -687,7 +687,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--clocks-csv", default=None,
                     help="also write the SM clock samples of the timed region to this CSV file")
-    ap.add_argument("--n", type=int, default=None, help="override node count (testing)")
+    # --nodes, not --n alone, under torchrun: its argument parser rejects "--n" as an
+    # ambiguous abbreviation of its own options even after the script name
+    ap.add_argument("--nodes", "--n", dest="n", type=int, default=None,
+                    help="override node count (testing)")
     ap.add_argument("--batch", action="store_true",
                     help="the batching configuration (256 graphs) instead of the default")
     ap.add_argument("--precision", action="store_true",
