@@ -56,3 +56,32 @@ def test_reference_arm_under_torchrun_prints_once():
     assert len(lines) == 1
     _check(lines[0])
     assert lines[0]["n_gpus"] == 2
+
+
+def _dist_rank(rank, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE="2", LOCAL_RANK=str(rank))
+    sys.path.insert(0, str(ROOT))
+    import bench
+    d = bench.Dist(2)
+    d.barrier()
+    q.put((rank, d.max(1.5 + rank), d.max(-rank)))
+    d.close()
+
+
+def test_dist_barrier_and_max_over_two_gloo_ranks():
+    """The replicas' timing is the max over ranks (host-side gloo)."""
+    import multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_dist_rank, args=(r, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res == [(0, 2.5, 0.0), (1, 2.5, 0.0)]
