@@ -203,7 +203,7 @@ class CpuPort:
         self.wh = O.second_whiten(Gxa, Gxb, Gxc, k, a0, sk)
         self.y = O.whitened_data(Gxa, Gxb, Gxc, self.wh)
         self.t_whiten = time.perf_counter() - t0
-        self.phi = O.polar(rng.standard_normal((k, k)))
+        self.phi = O.qr_pos(rng.standard_normal((k, k)))
         self.t = 0
         self.batches = O.stpm_minibatches(nX, wl["minibatch"])
         t0 = time.perf_counter()
@@ -220,7 +220,7 @@ class CpuPort:
             S = self.phi.T @ self.phi
             step = 3.0 * (self.phi @ (S * S)) - 3.0 * O.online_grad_terms(self.phi, self.y,
                                                                            nodes, a0)
-            self.phi = O.polar(self.phi - beta * step)
+            self.phi = O.qr_pos(self.phi - beta * step)
             self.t += 1
         dt = time.perf_counter() - t0
         self.sweeps.append(dt)
@@ -278,7 +278,7 @@ def run_ours(args, wl, ws, rank, local):
     clocks = ClockSampler(local, Path(args.clocks_csv) if args.clocks_csv else None)
     clocks.start()
     dev_ms, spmm_ms, spmm_bytes, spmm_launch, launches = [], 0.0, 0.0, 0, 0
-    ns_iters, stpm_steps = 0, 0
+    orth_passes, orth_err, stpm_steps = 0, 0.0, 0
     kern = {"contract_ms": 0.0, "contract_flops": 0.0, "contract_launches": 0,
             "step_ms": 0.0, "step_flops": 0.0, "step_launches": 0}
     stage = {"whiten_ms": 0.0, "stpm_ms": 0.0, "post_ms": 0.0}
@@ -295,7 +295,8 @@ def run_ours(args, wl, ws, rank, local):
         spmm_bytes += st["spmm_bytes"]
         spmm_launch += st["spmm_launches"]
         launches += st["kernel_launches"]
-        ns_iters += st["polar_iterations"]
+        orth_passes += st["orth_passes"]
+        orth_err = max(orth_err, st["orth_err_max"])
         stpm_steps += st["stpm_steps"]
         for key in kern:
             kern[key] += st[key]
@@ -364,7 +365,7 @@ def run_ours(args, wl, ws, rank, local):
                 "launches_per_step": launches / args.steps, "ms_per_step": ms / args.steps,
                 "algorithmic_flops_per_launch": flops / launches, "peak_source": pk["source"]}
 
-    step_rf = tensor_entry("stpm_step_kernel (k x k update + scaled Newton-Schulz polar, "
+    step_rf = tensor_entry("stpm_step_kernel (k x k update + Cholesky QR re-orthonormalisation, "
                            "3xTF32 mma.sync on a KP/8-CTA cluster)", kern["step_ms"],
                            kern["step_flops"], kern["step_launches"])
     contract_rf = tensor_entry("stpm_contract_kernel (Z = Phi^T y, alpha0 terms, G += y^T C; "
@@ -395,7 +396,8 @@ def run_ours(args, wl, ws, rank, local):
                    "parallelism": f"replicas{ws}"},
         "stages_ms_per_step": {k_: v / args.steps for k_, v in stage.items()},
         "host_wall_ms_per_step": t_host * 1e3 / args.steps,
-        "polar_iterations_per_stpm_step": ns_iters / max(stpm_steps, 1),
+        "cholesky_qr_passes_per_stpm_step": orth_passes / max(stpm_steps, 1),
+        "orth_err_before_first_order_pass_max": orth_err,
         "e2e": {"value": e2e_value, "unit": "node-updates/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_step},
         "gpu_launches": launches,
@@ -533,7 +535,7 @@ def run_precision(args, ws, rank, local):
     t_gen = time.perf_counter() - t0
     k, a0, nX = wl["k"], wl["alpha0"], graph.parts[0]
     rng = np.random.default_rng(wl["seed"])
-    phi0 = O.polar(rng.standard_normal((k, k)))
+    phi0 = O.qr_pos(rng.standard_normal((k, k)))
     forms, res = {}, {}
     y64 = wh = None
     for name, prec in (("fp32", mm.PREC_FP32), ("bf16", mm.PREC_BF16)):

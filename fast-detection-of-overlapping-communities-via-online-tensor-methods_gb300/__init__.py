@@ -78,10 +78,10 @@ class Stats(ctypes.Structure):
                 ("spmm_bytes", ctypes.c_double), ("spmm_launches", ctypes.c_int64),
                 ("stpm_steps", ctypes.c_int64), ("node_updates", ctypes.c_int64),
                 ("stpm_last_error", ctypes.c_double), ("kernel_launches", ctypes.c_int64),
-                ("polar_iterations", ctypes.c_int64), ("contract_ms", ctypes.c_double),
+                ("orth_passes", ctypes.c_int64), ("contract_ms", ctypes.c_double),
                 ("contract_flops", ctypes.c_double), ("contract_launches", ctypes.c_int64),
                 ("step_ms", ctypes.c_double), ("step_flops", ctypes.c_double),
-                ("step_launches", ctypes.c_int64)]
+                ("step_launches", ctypes.c_int64), ("orth_err_max", ctypes.c_double)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

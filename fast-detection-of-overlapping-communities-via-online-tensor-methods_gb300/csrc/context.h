@@ -68,6 +68,9 @@ struct mmsb_ctx {
   size_t kused[2] = {0, 0};
   int64_t klaunched[2] = {0, 0};  // launches since the last collect (timed or not)
   bool ksample = true;             // time the next STPM launches with events
+  // clock64 cycles a bounded device wait of the STPM kernels may take
+  // (0: about one second); mmsb_set_wait_limit
+  long long wait_limit = 0;
 
   ~mmsb_ctx();
   // grow-only named workspace buffer of at least `bytes` bytes

@@ -92,45 +92,70 @@ __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
 
 // ---- k x k step on one thread-block cluster -------------------------------------
 //
-// Every CTA of the cluster holds the whole current matrix X (column-major,
-// leading dimension KP + 4) and owns NB = 8 or 16 of its columns.  The
-// products X^T X[:, blk] and X B[:, blk] run on the tensor cores as warp-level
-// m16n8k8 TF32 MMAs with the 3xTF32 split (a = a_hi + a_lo; hi*hi + hi*lo +
-// lo*hi accumulated in FP32, relative error ~1e-6 per product), one warp per
-// 16 x 8 output tile.  The new column block is staged in shared memory and
-// sent to every CTA's next buffer by bulk asynchronous copies
-// (cp.async.bulk shared::cta -> shared::cluster), which complete on the
-// receiver's mbarrier; a CTA proceeds once all CL blocks of the next
-// iterate have arrived, so the data exchange itself is the per-iteration
-// synchronisation.  A block sent at broadcast n is rewritten only at
-// broadcast n + 2, after every receiver has finished waiting for broadcast
-// n (two staging buffers alternate).
+// The update of one minibatch step (Diff_Loss, CPU/Util.cpp:257-284, as the
+// GPU tree applies it at GPU/stpm.c:649-691, then its re-orthonormalisation
+// by culaDeviceDgeqrfp + culaDeviceDorgqr, GPU/stpm.c:783-784):
+//
+//   X   = Phi - beta (3 theta Phi (Phi^T Phi)^.2 - gscale G)
+//   Phi = Q  of  X = Q R  with R upper triangular, diag(R) > 0
+//
+// Q is computed by Cholesky QR: A = X^T X = R1^T R1 (Cholesky), Q1 = X R1^-1,
+// then E = Q1^T Q1 - I and Q = Q1 (I - F) with F upper triangular,
+// F + F^T = E (F = strict upper part of E plus half its diagonal), which is
+// the second Cholesky QR pass to first order in E.  Every factor applied to X
+// from the right is upper triangular with a positive diagonal, so Q is the
+// Q of the QR factorisation with diag(R) > 0 (it is unique), the factor the
+// reference forms.  When a pivot of the Cholesky shows that X's columns are
+// far from independent (R_jj^2 / A_jj below kQrExactBelow; the loss of
+// orthogonality of one pass grows like eps / that ratio), further exact
+// Cholesky QR passes run on Q1 before the first-order step.  Every CTA of
+// the cluster computes the same Cholesky from the same data, so the pass
+// count needs no vote.
+//
+// Layout: every CTA holds whole k x k matrices (column-major, leading
+// dimension KP + 4) and owns NB = 8 or 16 columns.  The products
+// X^T Y[:, blk] (Gram) and X B_blk (times) run on the tensor cores as
+// warp-level m16n8k8 TF32 MMAs with the 3xTF32 split (a = a_hi + a_lo;
+// hi*hi + hi*lo + lo*hi accumulated in FP32, relative error ~1e-6 per
+// product), one warp per 16 x 8 output tile.  A CTA's new column block is
+// staged in shared memory and sent to every CTA by bulk asynchronous copies
+// (cp.async.bulk shared::cta -> shared::cluster) that complete on the
+// receiver's per-block mbarrier; a CTA proceeds once all CL blocks have
+// arrived.  A staging tile used for broadcast n is rewritten at broadcast
+// n + 2 only, after every receiver has waited for broadcast n + 1 (sent by
+// each rank after it received all of broadcast n).
 
-// scaled Newton-Schulz: first guess of the smallest singular value after
-// the initial scaling, the error below which the plain step is used, and a
-// cap on the scale that keeps f(a sigma) > 0 for sigma slightly above 1
-constexpr float kNsLowerGuess = 1e-2f;
-constexpr float kNsPlainBelow = 0.1f;
-constexpr float kNsMaxScale = 1.7f;
-__device__ __forceinline__ float ns_poly(float y) { return y * (1.5f - 0.5f * y * y); }
+// pivot ratio R_jj^2 / A_jj below which one more exact Cholesky QR pass runs,
+// the floor a non-positive pivot is raised to (relative to A_jj), and the
+// largest number of exact passes per step
+constexpr float kQrExactBelow = 1e-3f;
+constexpr float kPivotFloor = 1e-12f;
+constexpr int kQrMaxPasses = 4;
 
-// column stride of X, B and the output tile: KP + 4 (== 4 mod 8 for KP a
-// multiple of 16) makes the fragment loads of the Gram product conflict-free
+// column stride of the k x k matrices: KP + 4 (== 4 mod 8 for KP a multiple
+// of 16) makes the fragment loads of the Gram product conflict-free
 __host__ __device__ constexpr int step_xld(int KP) { return KP + 4; }
 
 // NB = 8 (one n-tile) when the cluster has KP / 8 CTAs, else 16.  Above
-// KP = 128 two FP32 copies of Phi no longer fit one SM (SB: a single buffer,
-// refilled in place after a cluster barrier, and the G block kept in the
-// second staging tile, which the online update leaves unused).
+// KP = 128 two FP32 copies of a k x k matrix no longer fit one SM (SB: a
+// single buffer, refilled after a cluster barrier, one staging tile, the
+// second tile holding the G block and then the inverse diagonal blocks of
+// the Cholesky factor; a matrix still needed after the buffer is refilled
+// is kept in global memory, StpmUpdateArgs::xstash).
 template <int KP, int CL>
 struct StepSmem {
   static constexpr int NB = KP / CL, XLD = step_xld(KP), MT = KP / 16, NT = NB / 8;
   static constexpr int TILES = MT * NT, KS = TILES <= 8 ? 2 : 1;  // K split over warps
   static constexpr bool SB = KP > 128;
-  static constexpr size_t floats = (size_t)(SB ? 1 : 2) * KP * XLD    // X (and next X)
-                                   + (size_t)(SB ? 3 : 4) * NB * XLD  // B, 2 output tiles (+ G block)
-                                   + (size_t)(KS == 2 ? TILES * 128 : 0)  // K-split partial tiles
-                                   + 4 * KP + 3 * CL + 3 * NB + 2 * NB + 8;
+  static constexpr int NBK = KP / 16;  // 16-column blocks of the Cholesky factor
+  static constexpr size_t full = (size_t)(SB ? 1 : 2) * KP * XLD;
+  static constexpr size_t tiles = (size_t)4 * NB * XLD;  // B block, 2 staging tiles, G block
+  static constexpr size_t kpart = KS == 2 ? (size_t)TILES * 128 : 0;
+  static constexpr size_t small = 3 * KP + 3 * NB + 16 * NB + 8;  // mean terms, d-sums, tmp
+  static constexpr size_t tinv = SB ? 0 : (size_t)256 * NBK;      // SB: in the G block's tile
+  static constexpr size_t floats = full + tiles - (SB ? NB * XLD : 0) + kpart + small + tinv +
+                                   2 * KP;  // original diagonal, 1 / R_jj
+  static_assert(!SB || (size_t)256 * NBK <= (size_t)NB * XLD, "inverse blocks in the G tile");
   static_assert(floats * sizeof(float) <= 227 * 1024 - 2048, "step kernel shared memory");
 };
 
@@ -164,9 +189,10 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                : "memory");
 }
 
-// waits for the phase with the given parity to complete; false after about
-// one second (then the caller reports kFlagTimeout instead of hanging)
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// waits for the phase with the given parity to complete; false after `limit`
+// clock64 cycles (then the caller reports kFlagTimeout instead of hanging)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  long long limit) {
   const long long start = clock64();
   while (true) {
     uint32_t ok;
@@ -177,7 +203,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
         : "r"(smem_addr(bar)), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (clock64() - start > 2000000000LL) return false;
+    if (clock64() - start > limit) return false;
   }
 }
 
@@ -232,22 +258,22 @@ __device__ __forceinline__ void warp_tile_3xtf32(const float* __restrict__ pa,
 }
 
 // Tile products of the step.  Warp w < TILES * KS owns tile w % TILES and
-// half w / TILES of the K range (KS = 2); the halves meet in `part`.  A warp
-// calls pre(tile) before it reads the tile's operands.
-// kProdGram:  A_blk = X^T X[:, c0 .. c0+NB)   (A(m=i, k=r) = X[i XLD + r])
-// kProdTimes: P_blk = X B_blk                 (A(m=r, k=i) = X[i XLD + r])
+// half w / TILES of the K range (KS = 2); the halves meet in `part`.
+// kProdGram:  C_blk = X^T Y[:, c0 .. c0+NB)   (A(m=i, k=r) = X[i XLD + r], B = Y block)
+// kProdTimes: C_blk = X B_blk                 (A(m=r, k=i) = X[i XLD + r])
+// epi(acc, m0, n0) receives each finished 16 x 8 tile.
 enum StepProd : int { kProdGram = 0, kProdTimes = 1 };
 
-template <int KP, int CL, int PROD, typename Pre, typename Epi>
+template <int KP, int CL, int PROD, typename Epi>
 __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const float* __restrict__ Bm,
-                                           int c0, float* __restrict__ part, Pre&& pre, Epi&& epi) {
+                                           float* __restrict__ part, Epi&& epi) {
   using S = StepSmem<KP, CL>;
   constexpr int XLD = S::XLD;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   auto product = [&](int tile, int kb, int ke, float (&acc)[4]) {
     const int m0 = (tile % S::MT) * 16, n0 = (tile / S::MT) * 8;
     if (PROD == kProdGram)
-      warp_tile_3xtf32<XLD, 1, 1, XLD>(X + m0 * XLD, X + (c0 + n0) * XLD, kb, ke, acc);
+      warp_tile_3xtf32<XLD, 1, 1, XLD>(X + m0 * XLD, Bm + n0 * XLD, kb, ke, acc);
     else
       warp_tile_3xtf32<1, XLD, 1, XLD>(X + m0, Bm + n0 * XLD, kb, ke, acc);
   };
@@ -256,7 +282,6 @@ __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const fl
     const bool active = warp < S::TILES * S::KS;
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     if (active) {
-      pre(tile);
       product(tile, ks * (KP / 2), ks * (KP / 2) + KP / 2, acc);
       if (ks == 1) {
 #pragma unroll
@@ -267,14 +292,209 @@ __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const fl
     if (!active || ks != 0) return;
 #pragma unroll
     for (int q = 0; q < 4; ++q) acc[q] += part[tile * 128 + q * 32 + lane];
-    epi(acc, (tile % S::MT) * 16, (tile / S::MT) * 8, tile);
+    epi(acc, (tile % S::MT) * 16, (tile / S::MT) * 8);
   } else {
     for (int tile = warp; tile < S::TILES; tile += nw) {
       float acc[4] = {0.f, 0.f, 0.f, 0.f};
-      pre(tile);
       product(tile, 0, KP, acc);
-      epi(acc, (tile % S::MT) * 16, (tile / S::MT) * 8, tile);
+      epi(acc, (tile % S::MT) * 16, (tile / S::MT) * 8);
     }
+  }
+}
+
+// ---- Cholesky factor and its inverse on one CTA ----------------------------------
+//
+// A (KP x KP symmetric, column-major, leading dimension XLD, upper triangle
+// read) = R^T R with R upper triangular, blocked by 16 columns (right-looking):
+// a warp factors the diagonal block and inverts it, the block row of R right
+// of it is T_JJ^T A_J,K (T_JJ = R_JJ^-1), and the trailing upper triangle is
+// updated by 3xTF32 tensor-core tiles.  R overwrites A's upper triangle; the
+// inverse diagonal blocks go to tinv (16 x 16 column-major each), 1 / R_jj to
+// rd.  Rows and columns >= k must hold the identity (the caller sets their
+// diagonal to 1; X's padding columns are zero).
+
+// One warp: the 16 x 16 diagonal block at (j0, j0) (already updated by the
+// blocks above it).  Lane l < 16 holds column l (a[i] = A(j0+i, j0+l)); a
+// pivot that is not above kPivotFloor * dg (breakdown, or NaN) is raised to
+// it and counted as ratio 0.  Returns, in every lane, the smallest ratio
+// R_jj^2 / dg[j] over the live columns j0 + j < k.
+template <int XLD>
+__device__ __forceinline__ float factor_diag16(float* __restrict__ A, int j0, int k,
+                                               float* __restrict__ tb, float* __restrict__ rd,
+                                               const float* __restrict__ dg) {
+  const int lane = threadIdx.x & 31, l = lane & 15;
+  float a[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) a[i] = A[(j0 + i) + (j0 + l) * XLD];
+  float rv[16];
+  float rmin = 1.f;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    float d = __shfl_sync(0xffffffffu, a[j], j);
+    const float d0 = dg[j0 + j];
+    float ratio = d / d0;
+    if (!(d > kPivotFloor * d0)) {
+      d = kPivotFloor * d0;
+      ratio = 0.f;
+    }
+    if (j0 + j < k) rmin = fminf(rmin, ratio);
+    const float ri = rsqrtf(d);
+    rv[j] = ri;
+    const float u = (l == j) ? d * ri : a[j] * ri;  // R(j, l); lane j: sqrt(d)
+    a[j] = u;
+#pragma unroll
+    for (int i = j + 1; i < 16; ++i) {
+      const float rji = __shfl_sync(0xffffffffu, u, i);  // R(j, i)
+      a[i] = fmaf(-rji, u, a[i]);
+    }
+  }
+  // T = R^-1 by rows: lane m < 16 holds t[j] = T(m, j); T(m, j) =
+  // (delta_mj - sum_{i<j} T(m, i) R(i, j)) / R(j, j), zero for j < m
+  float t[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    float s = (l == j) ? 1.f : 0.f;
+#pragma unroll
+    for (int i = 0; i < j; ++i) s = fmaf(-t[i], __shfl_sync(0xffffffffu, a[i], j), s);
+    t[j] = s * rv[j];
+  }
+  if (lane < 16) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      if (i <= l) A[(j0 + i) + (j0 + l) * XLD] = a[i];
+      tb[l + 16 * i] = t[i];
+      if (l == i) rd[j0 + i] = rv[i];
+    }
+  }
+  return rmin;
+}
+
+// Whole CTA.  Returns the smallest pivot ratio (the same value in every
+// thread: every CTA of a cluster factors the same matrix the same way).
+template <int KP>
+__device__ float chol_blocked(float* __restrict__ A, int k, float* __restrict__ tinv,
+                              float* __restrict__ rd, float* __restrict__ dg,
+                              float* __restrict__ s_ratio) {
+  constexpr int XLD = step_xld(KP), NBK = KP / 16;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
+  const int nw = blockDim.x >> 5;
+  for (int i = tid; i < KP; i += blockDim.x) {
+    float d = A[i + i * XLD];
+    if (i >= k) {
+      d = 1.f;
+      A[i + i * XLD] = 1.f;
+    }
+    dg[i] = fmaxf(d, 1e-30f);
+  }
+  __syncthreads();
+  float rmin = 1.f;
+  for (int J = 0; J < NBK; ++J) {
+    const int j0 = 16 * J;
+    if (warp == 0) rmin = fminf(rmin, factor_diag16<XLD>(A, j0, k, tinv + 256 * J, rd, dg));
+    __syncthreads();
+    const int rest = KP - j0 - 16;
+    if (rest <= 0) break;
+    // block row: R(j0 + a, c) = sum_{b <= a} T(b, a) A(j0 + b, c), c >= j0 + 16
+    // (a thread per column)
+    const float* tb = tinv + 256 * J;
+    for (int e = tid; e < rest; e += blockDim.x) {
+      const int c = j0 + 16 + e;
+      float x[16];
+#pragma unroll
+      for (int b = 0; b < 16; ++b) x[b] = A[(j0 + b) + c * XLD];
+#pragma unroll
+      for (int aa = 15; aa >= 0; --aa) {
+        float s = 0.f;
+#pragma unroll
+        for (int b = 0; b <= aa; ++b) s = fmaf(tb[b + 16 * aa], x[b], s);
+        x[aa] = s;  // rows below aa are still the inputs
+      }
+#pragma unroll
+      for (int b = 0; b < 16; ++b) A[(j0 + b) + c * XLD] = x[b];
+    }
+    __syncthreads();
+    // trailing update of the upper triangle: A(c, c') -= sum_b R(j0+b, c) R(j0+b, c')
+    const int nm = rest / 16, nn = rest / 8;
+    for (int tl = warp; tl < nm * nn; tl += nw) {
+      const int m0 = j0 + 16 + (tl % nm) * 16, n0 = j0 + 16 + (tl / nm) * 8;
+      if (m0 > n0 + 7) continue;  // entirely below the diagonal
+      float acc[4];
+      warp_tile_3xtf32<XLD, 1, 1, XLD>(A + j0 + m0 * XLD, A + j0 + n0 * XLD, 0, 16, acc);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = m0 + g + ((q & 2) ? 8 : 0), c = n0 + 2 * t4 + (q & 1);
+        A[r + c * XLD] -= acc[q];
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) *s_ratio = rmin;
+  __syncthreads();
+  return *s_ratio;
+}
+
+// Columns c0 .. c0+NB of W = R^-1 (NB = 8 or 16, inside the 16-block K =
+// c0 / 16) into Wb (column jb at Wb + jb * XLD, rows >= 16 K + 16 zero), by
+// block back substitution: W_KK = T_KK, W_JK = -T_JJ sum_{L=J+1..K} R_JL W_LK.
+// tmp: 16 * NB floats.  Whole CTA; ends with a barrier.
+template <int KP, int NB>
+__device__ void inverse_columns(const float* __restrict__ R, const float* __restrict__ tinv, int c0,
+                                float* __restrict__ Wb, float* __restrict__ tmp) {
+  constexpr int XLD = step_xld(KP);
+  const int tid = threadIdx.x;
+  const int K = c0 / 16, co = c0 % 16;
+  for (int e = tid; e < NB * KP; e += blockDim.x) {
+    const int r = e % KP, jb = e / KP;
+    Wb[r + jb * XLD] = 0.f;
+  }
+  for (int e = tid; e < 16 * NB; e += blockDim.x) {
+    const int aa = e % 16, jb = e / 16;
+    tmp[e] = tinv[256 * K + aa + 16 * (co + jb)];  // W_KK
+  }
+  __syncthreads();
+  for (int L = K;; --L) {
+    // W_LK (in tmp) into place; rows above block L accumulate -R_JL W_LK
+    for (int e = tid; e < 16 * NB; e += blockDim.x) {
+      const int aa = e % 16, jb = e / 16;
+      Wb[16 * L + aa + jb * XLD] = tmp[e];
+    }
+    for (int e = tid; e < 16 * L * NB; e += blockDim.x) {
+      const int r = e % (16 * L), jb = e / (16 * L);
+      float s = 0.f;
+#pragma unroll
+      for (int b = 0; b < 16; ++b) s = fmaf(R[r + (16 * L + b) * XLD], tmp[b + 16 * jb], s);
+      Wb[r + jb * XLD] -= s;
+    }
+    __syncthreads();
+    if (L == 0) break;
+    // W_(L-1)K = T_(L-1) (the accumulated rows of block L-1)
+    const float* tb = tinv + 256 * (L - 1);
+    for (int e = tid; e < 16 * NB; e += blockDim.x) {
+      const int aa = e % 16, jb = e / 16;
+      const float* src = Wb + 16 * (L - 1) + jb * XLD;
+      float s = 0.f;
+#pragma unroll
+      for (int b = 0; b < 16; ++b)
+        if (b >= aa) s = fmaf(tb[aa + 16 * b], src[b], s);
+      tmp[e] = s;
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ bool mbar_wait_cluster_bounded(uint64_t* bar, uint32_t parity,
+                                                          long long limit) {
+  const long long start = clock64();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - start > limit) return false;
   }
 }
 
@@ -283,26 +503,31 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   using S = StepSmem<KP, CL>;
   constexpr int NB = S::NB, XLD = S::XLD;
   static_assert(NB == 8 || NB == 16, "column block of 8 or 16");
-  // one warp of the 512 threads issues the copy to each rank; the statistics
-  // of the tiles and of the ranks are reduced across the lanes of a warp
+  // one warp of the 512 threads issues the copy to each rank
   static_assert(CL <= 16 && S::TILES <= 32, "cluster or tile count");
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   extern __shared__ __align__(16) float sm[];
   float* Xa = sm;
-  float* Xb = S::SB ? Xa : Xa + KP * XLD;         // SB: one buffer, refilled in place
-  float* Ab = Xa + (S::SB ? 1 : 2) * KP * XLD;    // B (or A) block, column jb at Ab + jb * XLD
-  float* Ot = Ab + NB * XLD;                      // 2 staging tiles of the cluster broadcast
-  float* Gb = Ot + (S::SB ? 1 : 2) * NB * XLD;    // G block (online step; SB: staging tile 2)
-  float* part = Ot + (S::SB ? 2 : 3) * NB * XLD;  // K-split partial tiles
-  float* mv = part + (S::KS == 2 ? S::TILES * 128 : 0);  // m1, m2, m3 (+ pad) for this block
-  float* red = mv + 4 * KP;       // initial statistics of the CL ranks (3 x CL)
-  float* dcol = red + 3 * CL;     // 3 * NB d-sums (online step)
-  __shared__ float s_nrm, s_err, s_fro;
+  float* Xb = S::SB ? Xa : Xa + KP * XLD;
+  float* Ab = Xa + S::full;                       // B block of the products, column jb at Ab + jb * XLD
+  float* Ot = Ab + NB * XLD;                      // staging tile(s) of the broadcasts
+  float* Gb = Ot + (S::SB ? 1 : 2) * NB * XLD;    // G block (online step)
+  float* part = Gb + NB * XLD;                    // K-split partial tiles
+  float* mv = part + S::kpart;                    // m1, m2, m3 of this block
+  float* dcol = mv + 3 * KP;                      // 3 * NB d-sums
+  float* tmp = dcol + 3 * NB;                     // 16 * NB (inverse columns)
+  float* tinv = S::SB ? Gb : tmp + 16 * NB + 8;   // 16 x 16 inverse diagonal blocks
+  float* dg = (S::SB ? tmp + 16 * NB + 8 : tinv + 256 * S::NBK);  // original diagonal
+  float* rd = dg + KP;                            // 1 / R_jj
+  __shared__ float s_ratio;
+  __shared__ float s_emax[16];
   __shared__ __align__(8) uint64_t s_blk[2][16];  // block q of Xa / Xb arrived
+  __shared__ __align__(8) uint64_t s_csync;       // bounded cluster barrier
   const int k = a.k;
   const int c0 = rank * NB;
   const int tid = threadIdx.x, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
+  const long long wl = a.wait_limit > 0 ? a.wait_limit : 2000000000LL;
   {
     // Phi: loads issued in batches of 8 per thread so that their latencies overlap
     constexpr int N = KP * XLD, B = 8;
@@ -321,11 +546,10 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
         }
     }
   }
-  for (int e = tid; e < 2 * NB * XLD; e += blockDim.x) Ot[e] = 0.f;
-  if (tid < 2 * CL) {
-    mbar_init(&s_blk[tid / CL][tid % CL], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
+  for (int e = tid; e < (S::SB ? 1 : 2) * NB * XLD; e += blockDim.x) Ot[e] = 0.f;
+  if (tid < 2 * CL) mbar_init(&s_blk[tid / CL][tid % CL], 1);
+  if (tid == 2 * CL) mbar_init(&s_csync, CL);
+  if (tid <= 2 * CL) asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   __syncthreads();
   if (a.step_mode == kStepOnline) {
     // the mean terms phi_i . mu of this block's columns (a warp per dot
@@ -350,83 +574,82 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   uint32_t parity = 0u;  // bit b: phase parity awaited on the barriers of buffer b
+  uint32_t csync_parity = 0u;
   int nbcast = 0;
   bool timed_out = false;
-  bool wait_failed = false;  // a per-block wait of this thread gave up
   constexpr uint32_t kBlockBytes = sizeof(float) * NB * XLD;
-
-  float* X = Xa;   // current iterate
-  float* dn = Xb;  // next iterate (the same offset in every CTA of the cluster)
-  auto swap_buffers = [&]() {
-    float* tt = X;
-    X = dn;
-    dn = tt;
-  };
   auto buf_of = [&](const float* b) { return b == Xa ? 0 : 1; };
-  auto no_wait = [](int) {};
-  // P = alpha X B_blk + beta_self X[:, blk] + gamma Gb, zero outside k x k,
-  // with this CTA's statistics s_nrm, s_err, s_fro in the padding rows KP..
-  // of its first column: written into this CTA's block of the next buffer
-  // and, staged, sent to every other rank's.  Returns without waiting: block
-  // q of a buffer completes on that buffer's barrier s_blk[.][q].
-  auto times_and_send = [&](float alpha, float beta_self, const float* Gsrc, float gamma) {
-    float* Otc = Ot + (nbcast & 1) * NB * XLD;
+  // staging tile of the next broadcast (or of the final block)
+  auto stage_next = [&]() -> float* {
+    float* p = S::SB ? Ot : Ot + (nbcast & 1) * NB * XLD;
     ++nbcast;
-    float* own = dn + c0 * XLD;
-    step_tiles<KP, CL, kProdTimes>(X, Ab, c0, part, no_wait, [&](const float (&acc)[4], int m0, int n0, int) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int r = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
-        float v = alpha * acc[q] + beta_self * X[col * XLD + r];
-        if (Gsrc) v += gamma * Gsrc[jb * XLD + r];
-        v = (r < k && col < k) ? v : 0.f;
-        Otc[jb * XLD + r] = v;
-        if (!S::SB) own[jb * XLD + r] = v;  // the other buffer: nobody reads it now
-      }
-    });
-    if (tid == 0) {
-      Otc[KP] = s_nrm;
-      Otc[KP + 1] = s_err;
-      Otc[KP + 2] = s_fro;
-      if (!S::SB) {
-        own[KP] = s_nrm;
-        own[KP + 1] = s_err;
-        own[KP + 2] = s_fro;
-      }
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // staging -> async proxy
+    return p;
+  };
+  // bounded cluster barrier: every thread of every CTA has passed the
+  // __syncthreads before its rank's arrival (remote mbarrier arrives with
+  // release semantics, waited for with acquire); false after a timeout
+  auto csync = [&]() -> bool {
     __syncthreads();
-    if (S::SB) {
-      // single buffer: every CTA has finished reading the current iterate
-      // before any copy, or this CTA's own block, overwrites it
-      cluster.sync();
-      for (int e = tid; e < NB * XLD; e += blockDim.x) own[e] = Otc[e];
+    if (tid < CL) {
+      uint32_t remote;
+      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(smem_addr(&s_csync)), "r"(tid));
+      asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(remote) : "memory");
+    }
+    bool ok = true;
+    if (tid == 0) ok = mbar_wait_cluster_bounded(&s_csync, csync_parity, wl);
+    csync_parity ^= 1u;
+    return !__syncthreads_or(!ok);
+  };
+  // the staged block Otc (this CTA's columns) into `dst` of every rank,
+  // own copy included; sync_first: a cluster barrier first, because some
+  // rank may still be reading its `dst`
+  auto broadcast = [&](float* Otc, float* dst, bool sync_first) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // staging -> async proxy
+    if (sync_first) {
+      if (!csync()) timed_out = true;
+    } else {
       __syncthreads();
     }
-    const int bi = buf_of(dn), w = tid >> 5;
+    float* own = dst + c0 * XLD;
+    for (int e = tid; e < NB * XLD; e += blockDim.x) own[e] = Otc[e];
+    const int bi = buf_of(dst), w = tid >> 5;
     // one issuing thread per warp (copies issued by lanes of one warp
-    // serialise); a CTA's copies leave about in warp order at the SM's
-    // outgoing bandwidth, so rank q sends to q+1, q+2, ... first: every rank
-    // then receives its blocks spread over the exchange, not all at its end
+    // serialise); rank q sends to q+1, q+2, ... first, so every rank receives
+    // its blocks spread over the exchange
     if (lane == 0 && w < CL - 1)
       bulk_copy_to_rank(own, Otc, kBlockBytes, &s_blk[bi][rank], (uint32_t)((rank + 1 + w) % CL));
     if (tid < CL && tid != rank) mbar_arrive_expect_tx(&s_blk[bi][tid], kBlockBytes);
   };
-  // every block of X has arrived (false after a timeout of any thread's wait)
-  auto wait_all = [&]() -> bool {
-    const int bi = buf_of(X);
-    bool ok = !wait_failed;
-    if (tid < CL && tid != rank) ok = mbar_wait_bounded(&s_blk[bi][tid], (parity >> bi) & 1u) && ok;
+  // every block of `buf` has arrived (false after a timeout of any wait);
+  // SB: then a cluster barrier, after which every copy of the broadcast has
+  // landed everywhere (the single staging tile and the G tile are free)
+  auto wait_buf = [&](const float* buf) -> bool {
+    const int bi = buf_of(buf);
+    bool ok = true;
+    if (tid < CL && tid != rank) ok = mbar_wait_bounded(&s_blk[bi][tid], (parity >> bi) & 1u, wl);
     parity ^= 1u << bi;
-    wait_failed = false;
-    return !__syncthreads_or(!ok);
+    ok = !__syncthreads_or(!ok);
+    if (S::SB) ok = csync() && ok;
+    return ok;
   };
-  // the blocks of X holding the columns that are rows m0 .. m0+15 of a Gram tile
-  auto wait_rows = [&](int tile) {
-    const int bi = buf_of(X), m0 = (tile % S::MT) * 16;
-    for (int q = m0 / NB; q <= (m0 + 15) / NB; ++q)
-      if (q != rank && !mbar_wait_bounded(&s_blk[bi][q], (parity >> bi) & 1u)) wait_failed = true;
+  // Gram block C = P^T P[:, c0 .. c0+NB) into the staging tile, zero outside
+  // k x k; a non-finite entry raises kFlagNonFinite
+  auto gram_stage = [&](const float* P, float* Otc) {
+    bool bad = false;
+    step_tiles<KP, CL, kProdGram>(P, P + c0 * XLD, part, [&](const float (&acc)[4], int m0, int n0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
+        const float v = acc[q];
+        if (!isfinite(v)) bad = true;
+        Otc[jb * XLD + i] = (i < k && col < k) ? v : 0.f;
+      }
+    });
+    if (bad) atomicOr(a.flags, kFlagNonFinite);
   };
+
+  float* M = Xa;               // the matrix to orthonormalise (full in every CTA)
+  float* F = S::SB ? Xa : Xb;  // the other buffer
   if (a.step_mode == kStepOnline) {
     // G block (columns c0 .. c0+NB) from the per-CTA partials.  The first 8
     // partials of this thread's (up to) two G entries are loaded together
@@ -499,8 +722,8 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       }
       Gb[jb * XLD + j] = gval;
     }
-    // Phi' = Phi - beta (3 theta Phi (Phi^T Phi)^.2 - gscale G)   (Util.cpp:259-272)
-    step_tiles<KP, CL, kProdGram>(X, nullptr, c0, part, no_wait, [&](const float (&acc)[4], int m0, int n0, int) {
+    // X = Phi - beta (3 theta Phi (Phi^T Phi)^.2 - gscale G)   (Util.cpp:259-272)
+    step_tiles<KP, CL, kProdGram>(M, M + c0 * XLD, part, [&](const float (&acc)[4], int m0, int n0) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int i = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1);
@@ -508,275 +731,146 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       }
     });
     __syncthreads();
-    times_and_send(-a.beta * a.theta3, 1.f, Gb, a.beta * a.gscale);
-    swap_buffers();
-    if (!wait_all()) timed_out = true;
+    float* Otc = stage_next();
+    const float alpha = -a.beta * a.theta3, gamma = a.beta * a.gscale;
+    step_tiles<KP, CL, kProdTimes>(M, Ab, part, [&](const float (&acc)[4], int m0, int n0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
+        const float v = alpha * acc[q] + M[col * XLD + r] + gamma * Gb[jb * XLD + r];
+        Otc[jb * XLD + r] = (r < k && col < k) ? v : 0.f;
+      }
+    });
+    broadcast(Otc, F, S::SB);
+    if (!wait_buf(F)) timed_out = true;
+    float* t = M;
+    M = F;
+    F = t;
   }
-  // Scaled Newton-Schulz polar iteration X <- X (3 a I - a^3 X^T X) / 2.
-  // After the first scaling (by ||X^T X||_F^(-1/2): sigma_max^2 <= ||X^T X||_F,
-  // nearly equal when one singular value dominates, as the gradient term
-  // makes it) every singular value of X lies in [l, 1]; with
-  // f(y) = 3y/2 - y^3/2 the step maps sigma to f(a sigma), and
-  // a = sqrt(3 / (1 + l + l^2)) makes f(a l) = f(a), so the lower end grows by
-  // up to sqrt(3) * 3/2 ~ 2.6x per iteration instead of 3/2 (the scaled
-  // Newton-Schulz iteration; l starts from the guess kNsLowerGuess and is
-  // tightened by sigma_min^2 >= 1 - ||X^T X - I||_F).  Once max|X^T X - I|
-  // < kNsPlainBelow the plain step (a = 1) takes over: with X^T X = I + E the
-  // next error is -3/4 E^2 + E^3/4, so after |E| < 1e-3 one more iteration
-  // reaches the FP32 floor and the loop stops there.
-  // One exchange per iteration: the statistics of A_t = X_t^T X_t travel
-  // with the broadcast of X_{t+1}; if they show X_t had already converged,
-  // X_{t+1} is discarded.  The scale of step t therefore uses
-  // the statistics of A_{t-1}; every CTA derives the same a from the same
-  // exchanged numbers.  The exchange is bandwidth-bound, so the Gram of
-  // X_{t+1} starts while its blocks arrive: a warp waits only for the blocks
-  // holding its tile's columns, and the statistics are applied after the
-  // products.
-  //
-  // gram_stats: A_blk = X^T X[:, blk] into Ab with its statistics
-  // (||A||_F^2, max |A - I|, ||A - I||_F^2 over the block) in s_nrm, s_err,
-  // s_fro; pre(tile) runs before a warp reads the tile's columns.
-  // (per-tile partial statistics are reduced in a fixed order, so the
-  // result does not depend on warp timing)
-  __shared__ float nrmpart[S::TILES], errpart[S::TILES], fropart[S::TILES];
-  auto gram_stats = [&](auto&& pre) {
-    step_tiles<KP, CL, kProdGram>(X, nullptr, c0, part, pre, [&](const float (&acc)[4], int m0, int n0, int tile) {
-      float er = 0.f, fr = 0.f, na = 0.f;
+  // Cholesky QR passes on M: A = M^T M gathered into F, R = chol(A) and the
+  // columns of R^-1 this CTA needs (computed by every CTA from the same A),
+  // M R^-1 gathered into F, which becomes M.  (SB: M is kept in global
+  // memory while its buffer holds A.)
+  int passes = 0;
+  while (!timed_out) {
+    float* Otc = stage_next();
+    gram_stage(M, Otc);
+    if (S::SB) {
+      // M's own columns to the stash (every rank's are read back below)
+      for (int e = tid; e < NB * KP; e += blockDim.x) {
+        const int r = e % KP, jb = e / KP;
+        a.xstash[(int64_t)(c0 + jb) * KP + r] = M[(c0 + jb) * XLD + r];
+      }
+    }
+    broadcast(Otc, F, S::SB);
+    if (!wait_buf(F)) {
+      timed_out = true;
+      break;
+    }
+    const float ratio = chol_blocked<KP>(F, k, tinv, rd, dg, &s_ratio);
+    inverse_columns<KP, NB>(F, tinv, c0, Ab, tmp);
+    ++passes;
+    if (S::SB) {
+      // the buffer (R, read by no one now) gets M back from the stash
+      // (written before the barrier of the last broadcast)
+      for (int e = tid; e < KP * KP; e += blockDim.x) {
+        const int r = e % KP, c = e / KP;
+        M[c * XLD + r] = __ldcg(a.xstash + (int64_t)c * KP + r);
+      }
+      __syncthreads();
+    }
+    Otc = stage_next();
+    step_tiles<KP, CL, kProdTimes>(M, Ab, part, [&](const float (&acc)[4], int m0, int n0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
+        Otc[jb * XLD + r] = (r < k && col < k) ? acc[q] : 0.f;
+      }
+    });
+    // every rank has finished its Cholesky in F (and, SB, its product on M)
+    // before any block of M R^-1 is written there
+    broadcast(Otc, F, true);
+    if (!wait_buf(F)) {
+      timed_out = true;
+      break;
+    }
+    float* t = M;
+    M = F;
+    F = S::SB ? M : t;
+    if (ratio >= kQrExactBelow || passes >= a.max_passes) {
+      if (ratio < kQrExactBelow && rank == 0 && tid == 0) atomicOr(a.flags, kFlagNoConvergence);
+      break;
+    }
+  }
+  // first-order second pass: E = M^T M - I, F = strict upper part of E plus
+  // half its diagonal (this CTA's columns, in Ab), Phi = M (I - F)
+  float emax = 0.f;
+  if (!timed_out) {
+    step_tiles<KP, CL, kProdGram>(M, M + c0 * XLD, part, [&](const float (&acc)[4], int m0, int n0) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int i = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
-        const float v = acc[q];
-        const bool diag = i == col;
-        if (i < k && col < k) {
-          const float d = v - (diag ? 1.f : 0.f);
-          er = fmaxf(er, fabsf(d));
-          fr = fmaf(d, d, fr);
-          na = fmaf(v, v, na);
-        }
-        Ab[jb * XLD + i] = v;
+        const bool live = i < k && col < k;
+        const float e = live ? acc[q] - (i == col ? 1.f : 0.f) : 0.f;
+        emax = fmaxf(emax, fabsf(e));
+        Ab[jb * XLD + i] = i < col ? e : i == col ? 0.5f * e : 0.f;
       }
+    });
 #pragma unroll
-      for (int off = 16; off; off >>= 1) {
-        er = fmaxf(er, __shfl_xor_sync(0xffffffffu, er, off));
-        fr += __shfl_xor_sync(0xffffffffu, fr, off);
-        na += __shfl_xor_sync(0xffffffffu, na, off);
-      }
-      if (lane == 0) {
-        nrmpart[tile] = na;
-        errpart[tile] = er;
-        fropart[tile] = fr;
+    for (int off = 16; off; off >>= 1) emax = fmaxf(emax, __shfl_xor_sync(0xffffffffu, emax, off));
+    if (lane == 0) s_emax[tid >> 5] = emax;
+    __syncthreads();
+    float* Otc = stage_next();
+    step_tiles<KP, CL, kProdTimes>(M, Ab, part, [&](const float (&acc)[4], int m0, int n0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
+        Otc[jb * XLD + r] = (r < k && col < k) ? M[col * XLD + r] - acc[q] : 0.f;
       }
     });
     __syncthreads();
-    if (tid < 32) {  // warp 0: lane t takes tile t
-      float m = lane < S::TILES ? nrmpart[lane] : 0.f;
-      float e = lane < S::TILES ? errpart[lane] : 0.f;
-      float f = lane < S::TILES ? fropart[lane] : 0.f;
-#pragma unroll
-      for (int off = 16; off; off >>= 1) {
-        m += __shfl_xor_sync(0xffffffffu, m, off);
-        e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, off));
-        f += __shfl_xor_sync(0xffffffffu, f, off);
-      }
-      if (lane == 0) {
-        s_nrm = m;
-        s_err = e;
-        s_fro = f;
-      }
-      __syncwarp();
+    if (tid == 0) {
+      float m = 0.f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, s_emax[w]);
+      if (a.orth_err) atomicMax(reinterpret_cast<int*>(a.orth_err), __float_as_int(m));
     }
-    // no barrier: s_* are read only by warp 0 (post_stats, the staging of
-    // the next broadcast); the block barrier above published A_blk, and
-    // nrm/err/fropart are next written after several more barriers
-  };
-  // initial statistics: rank q's [||A_blk||_F^2 | max error | Frobenius^2]
-  // go to red[q], red[CL + q], red[2 CL + q] of every rank
-  auto post_stats = [&]() {
-    if (tid < CL) {
-      float* r = cluster.map_shared_rank(red, tid);
-      r[rank] = s_nrm;
-      r[CL + rank] = s_err;
-      r[2 * CL + rank] = s_fro;
+    for (int e = tid; e < KP * NB; e += blockDim.x) {
+      const int r = e % KP, jb = e / KP, col = c0 + jb;
+      if (r < k && col < k) a.phi[(int64_t)col * k + r] = Otc[jb * XLD + r];
     }
-  };
-  // rank q's statistics at src[q * qs + {0, fs, 2 fs}], reduced by every
-  // warp across its lanes (the xor butterfly gives every lane, and so every
-  // warp and every CTA, the same bits: IEEE addition is commutative)
-  auto reduce_stats = [&](const float* src, int qs, int fs, float& gnrm, float& gerr, float& gfro) {
-    float x = 0.f, y = 0.f, z = 0.f;
-    if (lane < CL) {
-      x = src[lane * qs];
-      y = src[lane * qs + fs];
-      z = src[lane * qs + 2 * fs];
-    }
-#pragma unroll
-    for (int off = 16; off; off >>= 1) {
-      x += __shfl_xor_sync(0xffffffffu, x, off);
-      y = fmaxf(y, __shfl_xor_sync(0xffffffffu, y, off));
-      z += __shfl_xor_sync(0xffffffffu, z, off);
-    }
-    gnrm = x;
-    gerr = y;
-    gfro = z;
-  };
-  // initial scaling: sigma_max^2 <= ||X^T X||_F
-  gram_stats(no_wait);
-  post_stats();
-  cluster.sync();
-  int it = 0;
-  bool done = timed_out, last = false;
-  bool gram_ready = false;  // Ab and s_* already hold the Gram of X (scaled first iterate)
-  __shared__ float wred[3][16];
-  if (!done) {
-    float gnrm, gerr, gfro;
-    reduce_stats(red, 1, CL, gnrm, gerr, gfro);
-    if (!(gerr == gerr) || !(gnrm == gnrm) || !(gfro == gfro)) {
-      if (tid == 0 && rank == 0) atomicOr(a.flags, kFlagNonFinite);
-      done = true;
-    } else if (gerr < a.ns_tol) {
-      done = true;
-    } else if (gnrm > 0.f) {
-      const float sc = rsqrtf(sqrtf(gnrm)), sc2 = sc * sc;
-      for (int e = tid; e < KP * XLD; e += blockDim.x) X[e] *= sc;
-      // the Gram of the scaled iterate is sc^2 A: its block and statistics
-      // without a second product
-      float er = 0.f, fr = 0.f, na = 0.f;
-      for (int e = tid; e < NB * KP; e += blockDim.x) {
-        const int jb = e / KP, i = e % KP, col = c0 + jb;
-        float* pa = Ab + jb * XLD + i;
-        const float v = *pa * sc2;
-        *pa = v;
-        if (i < k && col < k) {
-          const float d = v - (i == col ? 1.f : 0.f);
-          er = fmaxf(er, fabsf(d));
-          fr = fmaf(d, d, fr);
-          na = fmaf(v, v, na);
+    if (a.trace_out) {  // ||Phi_new - snapshot||_F^2 over this CTA's columns, fixed order
+      double d2 = 0.0;
+      for (int e = tid; e < KP * NB; e += blockDim.x) {
+        const int r = e % KP, jb = e / KP, col = c0 + jb;
+        if (r < k && col < k) {
+          const float v = Otc[jb * XLD + r];
+          const double d = (double)v - (double)a.trace_snap[(int64_t)col * k + r];
+          d2 = fma(d, d, d2);
+          a.trace_snap[(int64_t)col * k + r] = v;
         }
       }
 #pragma unroll
-      for (int off = 16; off; off >>= 1) {
-        er = fmaxf(er, __shfl_xor_sync(0xffffffffu, er, off));
-        fr += __shfl_xor_sync(0xffffffffu, fr, off);
-        na += __shfl_xor_sync(0xffffffffu, na, off);
-      }
-      if (lane == 0) {
-        wred[0][tid >> 5] = na;
-        wred[1][tid >> 5] = er;
-        wred[2][tid >> 5] = fr;
-      }
+      for (int off = 16; off; off >>= 1) d2 += __shfl_xor_sync(0xffffffffu, d2, off);
+      __shared__ double tpart[16];
+      if (lane == 0) tpart[tid >> 5] = d2;
       __syncthreads();
-      if (tid < 32) {
-        float m = lane < 16 ? wred[0][lane] : 0.f, e = lane < 16 ? wred[1][lane] : 0.f,
-              f = lane < 16 ? wred[2][lane] : 0.f;
-#pragma unroll
-        for (int off = 16; off; off >>= 1) {
-          m += __shfl_xor_sync(0xffffffffu, m, off);
-          e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, off));
-          f += __shfl_xor_sync(0xffffffffu, f, off);
-        }
-        if (lane == 0) {
-          s_nrm = m;
-          s_err = e;
-          s_fro = f;
-        }
+      if (tid == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += tpart[w];
+        a.trace_out[rank] = t;
       }
-      __syncthreads();
-      gram_ready = true;
     }
-  }
-  // (red[] is written only by post_stats above, and every CTA finished its
-  // update before the first cluster barrier: no second barrier is needed
-  // before the first broadcast of the loop)
-  float lo = kNsLowerGuess;  // lower bound (guess at first) on sigma(X_t)
-  float prev_err = 1e30f;    // max|A_{t-1} - I|
-  float al_prev = 1.f;       // the scale of the step that made X_t
-  bool pending = false;      // blocks of X_t still arriving
-  // X_t (t = it) has arrived with the statistics of A_{t-1}: apply them.
-  // False once the loop stops, the result then being X_it.
-  auto receive = [&]() -> bool {
-    pending = false;
-    if (!wait_all()) {
-      timed_out = true;
-      return false;
-    }
-    float gnrm, gerr, gfro;
-    reduce_stats(X + KP, NB * XLD, 1, gnrm, gerr, gfro);
-    if (!(gerr == gerr) || !(gnrm == gnrm) || !(gfro == gfro)) {
-      if (tid == 0 && rank == 0) atomicOr(a.flags, kFlagNonFinite);
-      done = true;
-      return false;
-    }
-    if (gerr < a.ns_tol) {  // X_{t-1} was converged: keep it, drop X_t
-      if (!S::SB) {  // (a single buffer holds X_t only: keep that)
-        swap_buffers();
-        --it;
-      }
-      done = true;
-      return false;
-    }
-    // bound for X_t: [lb, 1] -> [min(f(a lb), f(a)), 1]
-    const float lb = fmaxf(lo, sqrtf(fmaxf(0.f, 1.f - sqrtf(gfro))));
-    lo = al_prev > 1.f ? fminf(ns_poly(al_prev * lb), ns_poly(al_prev)) : ns_poly(lb);
-    prev_err = gerr;
-    if (last) {
-      done = true;
-      return false;
-    }
-    if (gerr < 1e-3f) last = true;
-    return true;
-  };
-  while (!done) {
-    // when no further step will be taken, the statistics alone decide: no
-    // speculative Gram
-    const bool closing = pending && (last || it >= a.max_ns);
-    if (!closing && !gram_ready) gram_stats([&](int tile) {
-      if (pending) wait_rows(tile);
-    });
-    gram_ready = false;
-    if (pending && !receive()) break;
-    if (closing || it >= a.max_ns) break;
-    const float al = prev_err < kNsPlainBelow ? 1.f : fminf(sqrtf(3.f / (1.f + lo + lo * lo)), kNsMaxScale);
-    // X (d0 I + d1 A)[:, blk] = d1 (X A_blk) + d0 X[:, blk], d0 = 3a/2, d1 = -a^3/2
-    times_and_send(-0.5f * al * al * al, 1.5f * al, nullptr, 0.f);
-    swap_buffers();
-    al_prev = al;
-    pending = true;
-    ++it;
   }
   if (timed_out) {
     if (tid == 0) atomicOr(a.flags, kFlagTimeout);
-  } else if (!done && rank == 0 && tid == 0) {
-    atomicOr(a.flags, kFlagNoConvergence);
   }
-  if (rank == 0 && tid == 0 && a.ns_iters) atomicAdd(a.ns_iters, it);
-  for (int e = tid; e < KP * NB; e += blockDim.x) {
-    const int r = e % KP, col = c0 + e / KP;
-    if (r < k && col < k) a.phi[(int64_t)col * k + r] = X[col * XLD + r];
+  if (rank == 0 && tid == 0 && a.orth_passes) atomicAdd(a.orth_passes, passes);
+  // keep shared memory alive until remote writers are done (bounded: after a
+  // timeout the ranks may stand at different barriers)
+  if (!csync()) {
+    if (tid == 0) atomicOr(a.flags, kFlagTimeout);
+    __nanosleep(100000);  // let copies a stalled exchange left in flight land
   }
-  if (a.trace_out) {  // ||Phi_new - snapshot||_F^2 over this CTA's columns, fixed order
-    double d2 = 0.0;
-    for (int e = tid; e < KP * NB; e += blockDim.x) {
-      const int r = e % KP, col = c0 + e / KP;
-      if (r < k && col < k) {
-        const float v = X[col * XLD + r];
-        const double d = (double)v - (double)a.trace_snap[(int64_t)col * k + r];
-        d2 = fma(d, d, d2);
-        a.trace_snap[(int64_t)col * k + r] = v;
-      }
-    }
-#pragma unroll
-    for (int off = 16; off; off >>= 1) d2 += __shfl_xor_sync(0xffffffffu, d2, off);
-    __shared__ double tpart[16];
-    if (lane == 0) tpart[tid >> 5] = d2;
-    __syncthreads();
-    if (tid == 0) {
-      double t = 0.0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += tpart[w];
-      a.trace_out[rank] = t;
-    }
-  }
-  cluster.sync();  // keep shared memory alive until remote writers are done
-  if (timed_out) __nanosleep(100000);  // let copies a stalled exchange left in flight land
 }
 
 template <int KP, int CL>

@@ -12,8 +12,8 @@ enum StpmMode : int {
 };
 
 enum StpmStep : int {
-  kStepOnline = 0,  // Phi - beta (3 theta O - gscale G), then polar
-  kStepPolar = 1,   // polar factor of Phi only
+  kStepOnline = 0,  // Phi - beta (3 theta O - gscale G), then QR (diag(R) > 0)
+  kStepQR = 1,      // Q of the QR factorisation of Phi only
 };
 
 struct StpmPartialArgs {
@@ -73,10 +73,12 @@ struct StpmUpdateArgs {
   float beta;
   float theta3;         // 3 * theta
   float gscale;         // 3 (plain) or 1 (adjoint: G already holds dT)
-  int max_ns;
-  float ns_tol;
+  int max_passes;        // exact Cholesky QR passes per step at most
   unsigned* flags;
-  int* ns_iters;         // accumulates Newton-Schulz iterations
+  int* orth_passes;      // accumulates the exact Cholesky QR passes (may be null)
+  float* orth_err;       // max |Q1^T Q1 - I| before the first-order pass, max over steps (may be null)
+  float* xstash;         // KP x KP scratch in global memory (KP > 128 only)
+  long long wait_limit;  // clock64 cycles a bounded wait may take (0: about one second)
   int active;            // batched launches: 0 = no update for this graph in this round
   // convergence trace (may be null): CTA q writes sum over its columns of
   // (Phi_new - trace_snap)^2 to trace_out[q] and sets trace_snap = Phi_new there

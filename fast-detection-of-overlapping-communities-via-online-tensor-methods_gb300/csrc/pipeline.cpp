@@ -639,29 +639,35 @@ static void stpm_pass(mmsb_ctx* c, int mode, int q1, int q2, int q3, int64_t beg
   ck(stpm_reduce(r, c->s), "stpm_reduce");
 }
 
-static StpmUpdateArgs step_args(mmsb_ctx* c, int step_mode, int* ns_iters) {
+static StpmUpdateArgs step_args(mmsb_ctx* c, int step_mode, bool counted) {
   StpmUpdateArgs u{};
   u.k = c->k;
   u.step_mode = step_mode;
   u.phi = c->phi;
   u.theta3 = (float)(3.0 * c->cfg.theta);
-  u.max_ns = 80;
-  u.ns_tol = 2e-6f;  // early exit; the 1e-3 + one-iteration rule ends typical steps
+  u.max_passes = 4;
   u.flags = c->flags;
-  u.ns_iters = ns_iters;
+  if (counted) {
+    u.orth_passes = c->tbuf<int>("orth_passes", 4);
+    u.orth_err = c->tbuf<float>("orth_err", 4);
+  }
+  const int kp = stpm_step_kp(c->k);
+  if (kp > 128) u.xstash = c->tbuf<float>("xstash", (size_t)kp * kp);
+  u.wait_limit = c->wait_limit;
   u.active = 1;
   return u;
 }
 
-static void polar_only(mmsb_ctx* c, int* ns_iters) {
-  StpmUpdateArgs u = step_args(c, kStepPolar, ns_iters);
-  ck(stpm_update(u, c->s), "stpm_polar");
+// Q of the QR factorisation of Phi (diag(R) > 0), in place
+static void qr_only(mmsb_ctx* c) {
+  StpmUpdateArgs u = step_args(c, kStepQR, false);
+  ck(stpm_update(u, c->s), "stpm_qr");
 }
 
 StpmUpdateArgs stpm_online_update_args(mmsb_ctx* c, const OnlineRound& rd, float* gpart,
                                        int64_t stride, int nparts) {
   const int k = c->k;
-  StpmUpdateArgs u = step_args(c, kStepOnline, c->tbuf<int>("ns_iters", 4));
+  StpmUpdateArgs u = step_args(c, kStepOnline, true);
   u.mode = rd.mode;
   u.gpart = gpart;
   u.part_stride = stride;
@@ -720,7 +726,7 @@ int64_t stpm_online_rounds(const mmsb_ctx* c) {
 }
 
 // one minibatch update: partial contractions, then the fused reduction +
-// Phi - beta (3 theta O - gscale G) + polar orthonormalisation on one cluster
+// Phi - beta (3 theta O - gscale G) + QR re-orthonormalisation on one cluster
 static void stpm_step(mmsb_ctx* c, const OnlineRound& rd, bool timed = true,
                       float* trace_snap = nullptr, double* trace_out = nullptr) {
   c->ksample = timed;
@@ -731,23 +737,24 @@ static void stpm_step(mmsb_ctx* c, const OnlineRound& rd, bool timed = true,
   timed_launch(c, 1, [&]() { ck(stpm_update(u, c->s), "stpm_step"); });
 }
 
-// Phi0 (host FP64, or the polar factor of a seeded Gaussian matrix), counters
+// Phi0 (host FP64, or the Q factor of a seeded Gaussian matrix), counters
 // and, for the BF16 form, the BF16 copies of y
 void stpm_prepare(mmsb_ctx* c, const double* phi0) {
   if (!c->have_y) throw MmsbError(MMSB_ERR_STATE, "stpm before whitening");
   const int k = c->k;
   if (stpm_kp(k) < 0) throw MmsbError(MMSB_ERR_UNSUPPORTED, "STPM kernels support k <= 208");
   cudaStream_t s = c->s;
-  int* ns_it = c->tbuf<int>("ns_iters", 4);
-  ck(cudaMemsetAsync(ns_it, 0, sizeof(int), s), "ns counter");
+  ck(cudaMemsetAsync(c->tbuf<int>("orth_passes", 4), 0, sizeof(int), s), "orth counter");
+  ck(cudaMemsetAsync(c->tbuf<float>("orth_err", 4), 0, sizeof(float), s), "orth error");
   if (phi0) {
     double* tmp = c->tbuf<double>("phi64", (size_t)k * k);
     ck(cudaMemcpyAsync(tmp, phi0, sizeof(double) * k * k, cudaMemcpyHostToDevice, s), "H2D phi0");
     ck(f64_to_f32(tmp, c->phi, (int64_t)k * k, s), "phi0");
   } else {
-    // orthonormal start: polar factor of a seeded Gaussian matrix
+    // orthonormal start: Q of a seeded Gaussian matrix, as the GPU tree's
+    // random start (GPU/stpm.c:1041-1064)
     ck(gaussian_panel(c->phi, k, k, k, c->cfg.seed, 7, s), "phi0");
-    polar_only(c, nullptr);  // (not counted: the statistics cover the minibatch steps)
+    qr_only(c);  // (not counted: the statistics cover the minibatch steps)
   }
   c->stats.stpm_steps = 0;
   c->stats.contract_ms = c->stats.step_ms = c->stats.contract_flops = c->stats.step_flops = 0.0;
@@ -780,13 +787,21 @@ void stpm_online_stats(mmsb_ctx* c, int64_t steps) {
   const int k = c->k;
   c->stats.stpm_steps = steps;
   c->stats.node_updates = c->nX * c->cfg.sweeps;
-  int nsit = 0;
-  ck(cudaMemcpyAsync(&nsit, c->tbuf<int>("ns_iters", 4), sizeof(int), cudaMemcpyDeviceToHost,
-                     c->s), "ns counter");
+  int passes = 0;
+  float oerr = 0.f;
+  ck(cudaMemcpyAsync(&passes, c->tbuf<int>("orth_passes", 4), sizeof(int), cudaMemcpyDeviceToHost,
+                     c->s), "orth counter");
+  ck(cudaMemcpyAsync(&oerr, c->tbuf<float>("orth_err", 4), sizeof(float), cudaMemcpyDeviceToHost,
+                     c->s), "orth error");
   ck(cudaStreamSynchronize(c->s), "sync");
-  c->stats.polar_iterations = nsit;
-  // gram + product of every Newton-Schulz iteration and of every online update
-  c->stats.step_flops = 4.0 * (double)k * k * k * (double)(nsit + steps);
+  c->stats.orth_passes = passes;
+  c->stats.orth_err_max = oerr;
+  // per online update 4 k^3 (the Gram Phi^T Phi and the product with its
+  // square) and 3 k^3 for the first-order pass (Gram, triangular product);
+  // per exact Cholesky QR pass 2 k^3 (Gram) + k^3 (triangular product) +
+  // k^3 / 3 (Cholesky) + k^3 / 3 (triangular inverse)
+  const double kkk = (double)k * k * k;
+  c->stats.step_flops = kkk * (7.0 * (double)steps + 11.0 / 3.0 * (double)passes);
   check_flags(c, "stpm");
   collect_kernel_times(c);
   c->have_phi = true;

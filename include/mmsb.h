@@ -117,17 +117,22 @@ typedef struct mmsb_stats {
   int64_t node_updates;    /* n_X * sweeps (online/adjoint) or n_X * iterations */
   double stpm_last_error;  /* batch power: last ||Phi - Phi_old||_F */
   int64_t kernel_launches; /* launches of this library's kernels by the last call */
-  int64_t polar_iterations; /* Newton-Schulz iterations summed over the STPM steps */
+  int64_t orth_passes;     /* exact Cholesky QR passes summed over the STPM steps */
   /* STPM kernels of the last mmsb_stpm, timed with CUDA events around each
    * launch; flops are algorithmic (k, not the padded tile size):
-   * contraction 2 k^2 per node per Z and per G product, step 4 k^3 per
-   * Newton-Schulz iteration and per online update */
+   * contraction 2 k^2 per node per Z and per G product, step 7 k^3 per
+   * online update (its Grams and products, the first-order QR pass) plus
+   * 11/3 k^3 per exact Cholesky QR pass */
   double contract_ms;
   double contract_flops;
   int64_t contract_launches;
   double step_ms;
   double step_flops;
   int64_t step_launches;
+  /* largest max_ij |Q1^T Q1 - I| over the steps, Q1 the result of the exact
+   * Cholesky QR passes of a step before its first-order pass (the returned
+   * Phi is orthonormal to about the square of this, or FP32 round-off) */
+  double orth_err_max;
 } mmsb_stats;
 
 typedef struct mmsb_ctx mmsb_ctx;

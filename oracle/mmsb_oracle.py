@@ -196,8 +196,23 @@ def tensor_decomp_batch(y, alpha0, phi0, min_iter=100, max_iter=10000, tol=TOLER
     return lam, phi, it, err
 
 
+def qr_pos(M):
+    """Q of the QR factorisation M = Q R with R's diagonal non-negative: the
+    per-step re-orthonormalisation of the reference's GPU tree
+    (culaDeviceDgeqrfp + culaDeviceDorgqr, GPU/stpm.c:783-784, and the random
+    start at GPU/stpm.c:1041-1064).  Householder QR (numpy/LAPACK dgeqrf),
+    then the sign of each column of Q flipped where R's diagonal is negative,
+    which gives the same Q as dgeqrfp; a zero diagonal keeps its column."""
+    Q, R = np.linalg.qr(np.asarray(M, dtype=np.float64))
+    s = np.sign(np.diag(R))
+    s[s == 0] = 1.0
+    return Q * s
+
+
 def polar(M):
-    """Orthonormal polar factor U V^T of M (M = U S V^T)."""
+    """Orthonormal polar factor U V^T of M (M = U S V^T).  Not the
+    reference's operator; kept as a named alternative orthonormalisation
+    (stpm_online(..., orth="polar"))."""
     U, _, Vt = np.linalg.svd(M)
     return U @ Vt
 
@@ -265,12 +280,18 @@ def tensor_values(phi, y, alpha0):
     return np.einsum("ji,ji->i", phi, G)
 
 
-def stpm_online(y, alpha0, phi0, sweeps, minibatch, lr0=1.0, theta=1.0, adjoint=False):
-    """Minibatch STPM: per step Phi <- polar(Phi - beta_t (3 theta O - 3 G))
-    (Diff_Loss, Util.cpp:257-284, minibatch-averaged; re-orthonormalised every
-    step like GPU/stpm.c:774-786), beta_t = lr0/(1+t).  adjoint=True uses
-    half the exact gradient of loss_fwd instead of 3 theta O - 3 G.
+def stpm_online(y, alpha0, phi0, sweeps, minibatch, lr0=1.0, theta=1.0, adjoint=False,
+                orth="qr"):
+    """Minibatch STPM: per step Phi <- qr_pos(Phi - beta_t (3 theta O - 3 G))
+    with O = Phi (Phi^T Phi)^.2 (Diff_Loss, Util.cpp:257-284, averaged over
+    the minibatch; the same update as GPU/stpm.c:649-691 with the learning
+    rate of the BASELINE schedule), re-orthonormalised every step by QR with
+    a non-negative R diagonal as GPU/stpm.c:774-786 does; beta_t = lr0/(1+t).
+    adjoint=True uses half the exact gradient of loss_fwd instead of
+    3 theta O - 3 G.  orth="polar" replaces the QR by the polar factor (not
+    the reference's operator).
     Returns (lambda, phi, steps) with lambda_i = That(phi_i,phi_i,phi_i) > 0."""
+    orthonormalise = {"qr": qr_pos, "polar": polar}[orth]
     nx = y["Da"].shape[1]
     phi = np.array(phi0, dtype=np.float64, copy=True)
     t = 0
@@ -284,9 +305,10 @@ def stpm_online(y, alpha0, phi0, sweeps, minibatch, lr0=1.0, theta=1.0, adjoint=
                 S = phi.T @ phi
                 step = 3.0 * theta * (phi @ (S * S)) - 3.0 * online_grad_terms(phi, y, nodes,
                                                                                  alpha0)
-            phi = polar(phi - beta * step)
+            phi = orthonormalise(phi - beta * step)
             t += 1
-    phi = polar(phi)
+    if t == 0:
+        phi = orthonormalise(phi)
     lam = tensor_values(phi, y, alpha0)
     sgn = np.where(lam < 0, -1.0, 1.0)
     return lam * sgn, phi * sgn, t

@@ -1,8 +1,8 @@
 """Regenerates the golden fixtures in this directory from the reference itself.
 
-Run in a checkout where the reference is mounted (default /root/reference):
+Run in a checkout where the reference is mounted (its path given by --ref):
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout>
 
 Steps per case: generate a seeded MMSB graph with this library's generator,
 write it in the reference's COO text contract, run the reference's own CPU
@@ -93,7 +93,7 @@ def make_case(mm, name, params, ref):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="reference checkout")
     ap.add_argument("cases", nargs="*", default=list(CASES))
     args = ap.parse_args()
     subprocess.run(["make", "-C", str(ROOT / "oracle"), f"REF={args.ref}"], check=True)

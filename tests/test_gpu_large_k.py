@@ -18,7 +18,7 @@ def test_large_k_contraction_and_step(mm, oracle, k):
     a0 = 0.5
     g = mm.generate(8000, k, a0, 0.2, 0.002, seed=k)
     rng = np.random.default_rng(k)
-    phi0 = oracle.polar(rng.standard_normal((k, k)))
+    phi0 = oracle.qr_pos(rng.standard_normal((k, k)))
     with mm.Pipeline(k=k, alpha0=a0, stpm_method=mm.STPM_ONLINE, sweeps=2, minibatch=500) as p:
         p.upload(g).whiten()
         y = {n: np.asarray(v, dtype=np.float64) for n, v in p.whitened().items()}

@@ -19,7 +19,7 @@ def test_tensor_core_contraction_online_vs_oracle(mm, oracle, k, minibatch):
     a0 = 0.5
     g = mm.generate(8000, k, a0, 0.2, 0.002, seed=k + 1)
     rng = np.random.default_rng(k)
-    phi0 = oracle.polar(rng.standard_normal((k, k)))
+    phi0 = oracle.qr_pos(rng.standard_normal((k, k)))
     sweeps = 2 if minibatch > 100 else 1
     with mm.Pipeline(k=k, alpha0=a0, stpm_method=mm.STPM_ONLINE, sweeps=sweeps,
                      minibatch=minibatch) as p:
@@ -55,7 +55,7 @@ def test_bf16_adjoint_tensor_core_vs_oracle(mm, oracle, k):
     a0 = 0.5
     g = mm.generate(8000, k, a0, 0.2, 0.002, seed=k + 2)
     rng = np.random.default_rng(k)
-    phi0 = oracle.polar(rng.standard_normal((k, k)))
+    phi0 = oracle.qr_pos(rng.standard_normal((k, k)))
     out = {}
     for prec in (mm.PREC_BF16, mm.PREC_FP32):
         with mm.Pipeline(k=k, alpha0=a0, stpm_method=mm.STPM_ADJOINT, sweeps=3, minibatch=500,
