@@ -13,9 +13,8 @@ through the public C ABI with pinned host buffers: graph upload (H2D), run, Pi
 and lambda download (D2H) inside the timed region.
 
 --impl reference times the FP64 CPU restatement of the reference path
-(oracle/mmsb_oracle.py) on the host cores on a bounded sample of the same
-workload; its node-updates/s are extrapolated from measured whitening and
-per-sweep times.
+(oracle/mmsb_oracle.py) on all host threads, whole pipelines per step, on the
+same graph (generated by oracle/mmsb_gen.c without the GPU library).
 """
 from __future__ import annotations
 
@@ -180,82 +179,95 @@ NCU_TRAFFIC_PER_LAUNCH = {"stpm_step_kernel": 436480, "stpm_contract_kernel": 50
 
 # ---------------------------------------------------------------------------
 
+def oracle_module():
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import mmsb_oracle as O
+    O.FAST_GS = True  # blocked Gram-Schmidt (same result to round-off)
+    O.SPMM_THREADS = os.cpu_count() or 1  # sparse products over all host threads
+    return O
+
+
 class CpuPort:
     """The FP64 oracle port of the reference path on the host cores.
 
-    Whitening and unwhitening are timed once; the STPM is timed per sweep (one
-    pass of minibatch updates over X).  node_updates_per_s() extrapolates the
-    whole job: n_X * sweeps / (whiten + sweeps * sweep + post)."""
+    pipeline() runs and times one whole pipeline: whitening (Gaussian sketch
+    panels), whitened data, `sweeps` sweeps of minibatch STPM with the per-step
+    QR, lambda and unwhitening + normalisation.  Sparse products run row-split
+    over all host threads, dense ones in the BLAS threads."""
 
-    def __init__(self, mm, wl, graph=None):
-        sys.path.insert(0, str(ROOT / "oracle"))
-        import mmsb_oracle as O
-        O.FAST_GS = True  # vectorised Gram-Schmidt (same result to round-off)
-        self.O, self.wl = O, wl
-        self.graph = graph if graph is not None else make_graph(mm, wl)
-        Gxa, Gxb, Gxc, Gba, Gca = self.graph.scipy_blocks()
+    def __init__(self, wl, graph):
+        self.O, self.wl, self.graph = oracle_module(), wl, graph
+        self.blocks = graph.scipy_blocks()
+        self.times = []
+
+    def pipeline(self):
+        O, wl = self.O, self.wl
+        Gxa, Gxb, Gxc, Gba, Gca = self.blocks
         k, a0 = wl["k"], wl["alpha0"]
-        rng = np.random.default_rng(0)
+        rng = np.random.default_rng(wl["seed"])
         nX, nA, nB, nC = self.graph.parts
+        t0 = time.perf_counter()
         sk = (rng.standard_normal((nB, 2 * k)), rng.standard_normal((nC, 2 * k)),
               rng.standard_normal((nA, 2 * k)))
-        t0 = time.perf_counter()
-        self.wh = O.second_whiten(Gxa, Gxb, Gxc, k, a0, sk)
-        self.y = O.whitened_data(Gxa, Gxb, Gxc, self.wh)
-        self.t_whiten = time.perf_counter() - t0
-        self.phi = O.qr_pos(rng.standard_normal((k, k)))
-        self.t = 0
-        self.batches = O.stpm_minibatches(nX, wl["minibatch"])
-        t0 = time.perf_counter()
-        lam = O.tensor_values(self.phi, self.y, a0)
-        O.postprocess(Gxa, Gba, Gca, self.wh, lam, self.phi)
-        self.t_post = time.perf_counter() - t0
-        self.sweeps = []
+        wh = O.second_whiten(Gxa, Gxb, Gxc, k, a0, sk)
+        y = O.whitened_data(Gxa, Gxb, Gxc, wh)
+        t1 = time.perf_counter()
+        phi0 = O.qr_pos(rng.standard_normal((k, k)))
+        lam, phi, _ = O.stpm_online(y, a0, phi0, sweeps=wl["sweeps"], minibatch=wl["minibatch"])
+        t2 = time.perf_counter()
+        O.postprocess(Gxa, Gba, Gca, wh, lam, phi)
+        t3 = time.perf_counter()
+        self.times.append((t1 - t0, t2 - t1, t3 - t2))
+        return t3 - t0
 
-    def sweep(self):
-        O, a0 = self.O, self.wl["alpha0"]
-        t0 = time.perf_counter()
-        for nodes in self.batches:
-            beta = 1.0 / (1.0 + self.t)
-            S = self.phi.T @ self.phi
-            step = 3.0 * (self.phi @ (S * S)) - 3.0 * O.online_grad_terms(self.phi, self.y,
-                                                                           nodes, a0)
-            self.phi = O.qr_pos(self.phi - beta * step)
-            self.t += 1
-        dt = time.perf_counter() - t0
-        self.sweeps.append(dt)
-        return dt
+    def sample(self, n):
+        w, s_, p = (statistics.median(t[i] for t in self.times[-n:]) for i in range(3))
+        return (f"FP64 numpy/scipy port of the reference path on {os.cpu_count()} host threads, "
+                f"{n} whole pipeline(s) timed: whitening {w:.2f}s, {self.wl['sweeps']} STPM sweeps "
+                f"{s_:.2f}s, unwhitening {p:.2f}s (medians)")
 
-    def node_updates_per_s(self):
-        t_sweep = statistics.median(self.sweeps)
-        total = self.t_whiten + self.wl["sweeps"] * t_sweep + self.t_post
-        return self.graph.parts[0] * self.wl["sweeps"] / total, total
 
-    def sample(self):
-        _, total = self.node_updates_per_s()
-        return (f"FP64 numpy/scipy port of the reference path: whitening {self.t_whiten:.2f}s and "
-                f"unwhitening {self.t_post:.2f}s timed once, {len(self.sweeps)} STPM sweeps "
-                f"(median {statistics.median(self.sweeps):.3f}s, {len(self.batches)} minibatch "
-                f"steps each); extrapolated to {self.wl['sweeps']} sweeps = {total:.1f}s per step")
+def flush_host_cache():
+    """Writes a 256 MiB buffer (larger than the host's last-level cache)."""
+    np.ones(1 << 25, dtype=np.float64).sum()
+
+
+def config_of(wl, nnz_directed, ws):
+    return {"workload": wl["name"], "n": wl["n"], "k": wl["k"], "alpha0": wl["alpha0"],
+            "p_in": wl["p_in"], "p_out": wl["p_out"], "sweeps": wl["sweeps"],
+            "minibatch": wl["minibatch"], "seed": wl["seed"], "nnz_directed": int(nnz_directed),
+            "l2": "256 MiB buffer written between timed steps",
+            "parallelism": f"replicas{ws}"}
 
 
 def run_reference(args, wl, ws, rank):
+    """The reference path's CPU implementation (the oracle port; the
+    reference's own CPU tree is x86-only source that is not present on the GPU
+    host) on the same graph as the GPU arm (oracle/mmsb_gen.c restates the
+    library's generator bit for bit, so this process never loads the GPU
+    library), whole pipelines per step."""
     if rank != 0:
         return
-    mm = load_pkg()
-    port = CpuPort(mm, wl)
-    for i in range(args.warmup + args.steps):
-        port.sweep()
-        if i == args.warmup - 1:
-            port.sweeps.clear()
-    v, total = port.node_updates_per_s()
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import mmsb_gen
+    graph = mmsb_gen.generate(wl["n"], wl["k"], wl["alpha0"], wl["p_in"], wl["p_out"], wl["seed"])
+    port = CpuPort(wl, graph)
+    for _ in range(args.warmup):
+        port.pipeline()
+    ts = []
+    for _ in range(args.steps):
+        flush_host_cache()
+        ts.append(port.pipeline())
+    step = statistics.mean(ts)
+    nX = graph.parts[0]
+    v = nX * wl["sweeps"] / step
     line = {"impl": "reference", "metric": "stpm_node_updates_per_s", "value": v,
             "unit": "node-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": total * 1e3, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": wl["name"], **{k: wl[k] for k in wl if k != "name"}},
+            "config": config_of(wl, sum(b.nnz for b in graph.blocks[:3]) * 2, ws),
             "cpu_baseline": {"value": v, "unit": "node-updates/s", "cores": os.cpu_count(),
-                             "kind": "port", "sample": port.sample()},
+                             "kind": "port", "sample": port.sample(args.steps)},
             "e2e": {"value": v, "unit": "node-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -388,12 +400,7 @@ def run_ours(args, wl, ws, rank, local):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": wl["name"], "n": wl["n"], "k": wl["k"], "alpha0": wl["alpha0"],
-                   "p_in": wl["p_in"], "p_out": wl["p_out"], "sweeps": wl["sweeps"],
-                   "minibatch": wl["minibatch"], "seed": wl["seed"], "nnz_directed": sum(
-                       b.nnz for b in graph.blocks[:3]) * 2,
-                   "l2": "256 MiB buffer written between timed steps",
-                   "parallelism": f"replicas{ws}"},
+        "config": config_of(wl, sum(b.nnz for b in graph.blocks[:3]) * 2, ws),
         "stages_ms_per_step": {k_: v / args.steps for k_, v in stage.items()},
         "host_wall_ms_per_step": t_host * 1e3 / args.steps,
         "cholesky_qr_passes_per_stpm_step": orth_passes / max(stpm_steps, 1),
@@ -411,12 +418,10 @@ def run_ours(args, wl, ws, rank, local):
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        port = CpuPort(mm, wl, graph)
-        for _ in range(3):
-            port.sweep()
-        nu, _ = port.node_updates_per_s()
-        line["cpu_baseline"] = {"value": nu, "unit": "node-updates/s", "cores": os.cpu_count(),
-                                "kind": "port", "sample": port.sample()}
+        port = CpuPort(wl, graph)
+        t = port.pipeline()
+        line["cpu_baseline"] = {"value": nX * wl["sweeps"] / t, "unit": "node-updates/s",
+                                "cores": os.cpu_count(), "kind": "port", "sample": port.sample(1)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     p.close()

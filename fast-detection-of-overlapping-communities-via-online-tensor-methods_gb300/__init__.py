@@ -148,6 +148,8 @@ _SIGS = {
     "mmsb_op_spmm": (ctypes.c_int, [ctypes.POINTER(Csr), ctypes.c_int, _F, ctypes.c_int64,
                                     ctypes.c_float, _F]),
     "mmsb_op_symeig": (ctypes.c_int, [_D, ctypes.c_int32, _D, _D]),
+    "mmsb_set_wait_limit": (ctypes.c_int, [_P, ctypes.c_int64]),
+    "mmsb_diag_wait_timeout": (ctypes.c_int, [_P, ctypes.c_int64]),
     "mmsb_op_spmm_t_noalloc": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_int64,
                                               ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_float,
                                               _P, _P]),
@@ -485,6 +487,16 @@ class Pipeline:
 
     def flush_l2(self):
         self._ck(lib().mmsb_flush_l2(self._h))
+
+    def set_wait_limit(self, cycles):
+        """clock64 cycles a bounded device wait may take (0 = about one second)."""
+        self._ck(lib().mmsb_set_wait_limit(self._h, int(cycles)))
+        return self
+
+    def diag_wait_timeout(self, cycles):
+        """One bounded wait on a barrier nothing arrives at; returns the status
+        (MMSB_ERR_TIMEOUT = 8 when the give-up path works)."""
+        return lib().mmsb_diag_wait_timeout(self._h, int(cycles))
 
     def request_stop(self):
         lib().mmsb_request_stop(self._h)

@@ -554,6 +554,20 @@ mmsb_status mmsb_flush_l2(mmsb_ctx* c) {
   });
 }
 
+mmsb_status mmsb_set_wait_limit(mmsb_ctx* c, int64_t cycles) {
+  if (!c || cycles < 0) return MMSB_ERR_INVALID_ARG;
+  c->wait_limit = (long long)cycles;
+  return MMSB_OK;
+}
+
+mmsb_status mmsb_diag_wait_timeout(mmsb_ctx* c, int64_t cycles) {
+  if (!c || cycles < 1 || cycles > 2000000000LL) return MMSB_ERR_INVALID_ARG;
+  return guard(c, [&]() {
+    ck(wait_probe(c->flags, (long long)cycles, c->s), "wait probe");
+    check_device_flags(c, "wait probe");
+  });
+}
+
 mmsb_status mmsb_synchronize(mmsb_ctx* c) {
   if (!c) return MMSB_ERR_INVALID_ARG;
   return guard(c, [&]() { ck(cudaStreamSynchronize(c->s), "sync"); });

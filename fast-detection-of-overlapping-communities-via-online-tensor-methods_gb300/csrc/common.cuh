@@ -25,6 +25,10 @@ enum DeviceFlag : unsigned {
   kFlagTimeout = 8u,
 };
 
+// A bounded device wait on a barrier nothing arrives at: sets kFlagTimeout
+// after `limit` clock64 cycles (the failure path of every bounded wait).
+cudaError_t wait_probe(unsigned* flags, long long limit, cudaStream_t s);
+
 // Counts launches of this library's kernels (reported in mmsb_stats).
 extern thread_local int64_t g_launch_count;
 
@@ -64,12 +68,12 @@ cudaError_t unwhiten_normprob(const int64_t* rp, const int32_t* ci, const float*
 // waits)
 cudaError_t gram_tsk(const float* A, int lda, int pa, const float* B, int ldb, int pb, int64_t n,
                      double alpha, double* S, double* partials, int64_t partials_cap,
-                     cudaStream_t s, unsigned* flags = nullptr);
+                     cudaStream_t s, unsigned* flags = nullptr, long long wait_limit = 0);
 inline bool gram_use_tc(int64_t n, int pa, int pb) { return pa >= 64 && pb >= 64 && n >= 4096; }
 int gram_tc_nsplit(int64_t n, int pa, int pb);
 cudaError_t gram_tc_partial(const float* A, int lda, int pa, const float* B, int ldb, int pb,
                             int64_t n, double* partials, int nsplit, unsigned* flags,
-                            cudaStream_t s);
+                            cudaStream_t s, long long wait_limit = 0);
 size_t gram_tsk_partials(int64_t n, int pa, int pb);
 // Y[n x ldy] (row-major FP32) = M[n x ldm] (first p cols) * F (p x q, column-major FP64, ldf);
 // columns q..ldy-1 of Y are zeroed.

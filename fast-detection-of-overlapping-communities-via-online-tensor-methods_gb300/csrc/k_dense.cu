@@ -1197,12 +1197,13 @@ size_t gram_tsk_partials(int64_t n, int pa, int pb) {
 
 cudaError_t gram_tsk(const float* A, int lda, int pa, const float* B, int ldb, int pb, int64_t n,
                      double alpha, double* S, double* partials, int64_t partials_cap,
-                     cudaStream_t s, unsigned* flags) {
+                     cudaStream_t s, unsigned* flags, long long wait_limit) {
   if (gram_use_tc(n, pa, pb)) {
     // tcgen05 (kind::tf32, 3xTF32) partials over row splits, then the FP64 sum
     const int nsplit = gram_tc_nsplit(n, pa, pb);
     if ((int64_t)nsplit * pa * pb > partials_cap) return cudaErrorInvalidValue;
-    MMSB_CUDA_TRY(gram_tc_partial(A, lda, pa, B, ldb, pb, n, partials, nsplit, flags, s));
+    MMSB_CUDA_TRY(gram_tc_partial(A, lda, pa, B, ldb, pb, n, partials, nsplit, flags, s,
+                                  wait_limit));
     gram_reduce_kernel<<<grid_for((int64_t)pa * pb), 256, 0, s>>>(partials, nsplit,
                                                                    (int64_t)pa * pb, alpha, S);
     ++g_launch_count;

@@ -4,6 +4,8 @@
 
 #include <cuda_bf16.h>
 
+#include "tc_util.cuh"
+
 #include <algorithm>
 
 namespace mmsb {
@@ -274,6 +276,31 @@ cudaError_t set_row_scaled(int rows, int cols, double* B, int ldb, int row, doub
 
 cudaError_t eye_mask(int m, int p, const double* R, int ldr, double* Q, int ldq, cudaStream_t s) {
   eye_mask_kernel<<<(unsigned)ceil_div((int64_t)m * p, 256), 256, 0, s>>>(m, p, R, ldr, Q, ldq);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+// One CTA waits, through the bounded mbarrier wait of the tensor-core
+// kernels (tc::mbar_wait), on a barrier that nothing ever arrives at; the
+// wait gives up after `limit` clock64 cycles and reports kFlagTimeout, the
+// same path a stalled wait of a real kernel takes.  No copy or MMA is in
+// flight, so the kernel leaves cleanly.
+__global__ void wait_probe_kernel(unsigned* __restrict__ flags, long long limit) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(&bar)), "r"(1)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  bool ok = true;
+  if (threadIdx.x == 0) ok = tc::mbar_wait(&bar, 0u, limit);
+  if (!ok) atomicOr(flags, kFlagTimeout);
+}
+
+cudaError_t wait_probe(unsigned* flags, long long limit, cudaStream_t s) {
+  wait_probe_kernel<<<1, 32, 0, s>>>(flags, limit);
   ++g_launch_count;
   return cudaGetLastError();
 }

@@ -94,11 +94,16 @@ cudaError_t launch_spmm(const int64_t* rp, const int32_t* ci, const float* val, 
 
 // ---- transpose -----------------------------------------------------------
 
-__global__ void count_cols_kernel(const int32_t* __restrict__ ci, int64_t nnz,
+// (entries with a column index outside [0, n_cols) are skipped here and in
+// scatter_kernel, and row ranges are clipped to [0, nnz): a malformed block
+// gives a wrong transpose but no access outside the buffers)
+__global__ void count_cols_kernel(const int32_t* __restrict__ ci, int64_t nnz, int64_t n_cols,
                                   unsigned long long* __restrict__ cnt) {
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nnz;
-       j += (int64_t)gridDim.x * blockDim.x)
-    atomicAdd(&cnt[ci[j] + 1], 1ull);
+       j += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = ci[j];
+    if (c >= 0 && (int64_t)c < n_cols) atomicAdd(&cnt[c + 1], 1ull);
+  }
 }
 
 // Exclusive scan in place over n+1 entries (entry 0 == 0 on input), one CTA.
@@ -125,13 +130,17 @@ __global__ void __launch_bounds__(1024) scan_kernel(unsigned long long* __restri
 }
 
 __global__ void scatter_kernel(const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                               const float* __restrict__ val, int64_t n_rows,
-                               unsigned long long* __restrict__ cursor, int32_t* __restrict__ ciT,
-                               float* __restrict__ valT) {
+                               const float* __restrict__ val, int64_t n_rows, int64_t n_cols,
+                               int64_t nnz, unsigned long long* __restrict__ cursor,
+                               int32_t* __restrict__ ciT, float* __restrict__ valT) {
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_rows;
        r += (int64_t)gridDim.x * blockDim.x) {
-    for (int64_t j = rp[r]; j < rp[r + 1]; ++j) {
-      unsigned long long pos = atomicAdd(&cursor[ci[j]], 1ull);
+    const int64_t b = rp[r] > 0 ? rp[r] : 0, e = rp[r + 1] < nnz ? rp[r + 1] : nnz;
+    for (int64_t j = b; j < e; ++j) {
+      const int32_t c = ci[j];
+      if (c < 0 || (int64_t)c >= n_cols) continue;
+      unsigned long long pos = atomicAdd(&cursor[c], 1ull);
+      if (pos >= (unsigned long long)nnz) continue;
       ciT[pos] = (int32_t)r;
       if (valT) valT[pos] = val[j];
     }
@@ -325,7 +334,7 @@ cudaError_t csr_transpose(const int64_t* rp, const int32_t* ci, const float* val
   const int T = 256;
   const unsigned G = (unsigned)std::min<int64_t>(4 * kNumSMs * 8, std::max<int64_t>(1, ceil_div(nnz, T)));
   if (nnz > 0) {
-    count_cols_kernel<<<G, T, 0, s>>>(ci, nnz, cnt);
+    count_cols_kernel<<<G, T, 0, s>>>(ci, nnz, n_cols, cnt);
     ++g_launch_count;
   }
   scan_kernel<<<1, 1024, 0, s>>>(cnt, n_cols + 1);
@@ -334,7 +343,10 @@ cudaError_t csr_transpose(const int64_t* rp, const int32_t* ci, const float* val
   ++g_launch_count;
   if (nnz > 0) {
     const unsigned GR = (unsigned)std::max<int64_t>(1, std::min<int64_t>(4096, ceil_div(n_rows, T)));
-    scatter_kernel<<<GR, T, 0, s>>>(rp, ci, val, n_rows, cnt, tmp_c, tmp_v);
+    // row 0 in every slot first: a malformed block (row ranges that overlap
+    // or skip entries) then leaves valid row indices, never stale words
+    MMSB_CUDA_TRY(cudaMemsetAsync(tmp_c, 0, sizeof(int32_t) * nnz, s));
+    scatter_kernel<<<GR, T, 0, s>>>(rp, ci, val, n_rows, n_cols, nnz, cnt, tmp_c, tmp_v);
     ++g_launch_count;
     segment_sort_kernel<<<(unsigned)ceil_div(n_cols * 32, T), T, 0, s>>>(rpT, n_cols, tmp_c, tmp_v,
                                                                           ciT, valT);

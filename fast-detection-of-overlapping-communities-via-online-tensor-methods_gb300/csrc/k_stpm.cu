@@ -527,7 +527,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   const int k = a.k;
   const int c0 = rank * NB;
   const int tid = threadIdx.x, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
-  const long long wl = a.wait_limit > 0 ? a.wait_limit : 2000000000LL;
+  const long long wl = tc::wait_limit_or_default(a.wait_limit);
   {
     // Phi: loads issued in batches of 8 per thread so that their latencies overlap
     constexpr int N = KP * XLD, B = 8;
@@ -1266,7 +1266,7 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
   for (; tile < ntiles; tile += nblocks) {
     // the G products of the previous tile read y3 and C
     if (g_pending) {
-      if (!tc::mbar_wait(&bars[1], ph_g)) timed_out = true;
+      if (!tc::mbar_wait(&bars[1], ph_g, tc::wait_limit_or_default(a.wait_limit))) timed_out = true;
       ph_g ^= 1u;
       g_pending = false;
     }
@@ -1298,7 +1298,7 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
       }
       tc::commit(&bars[0]);
     }
-    if (!tc::mbar_wait(&bars[0], ph_z)) timed_out = true;
+    if (!tc::mbar_wait(&bars[0], ph_z, tc::wait_limit_or_default(a.wait_limit))) timed_out = true;
     ph_z ^= 1u;
     tc::fence_after_sync();
     {
@@ -1354,7 +1354,7 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
     any = true;
   }
   if (g_pending) {
-    if (!tc::mbar_wait(&bars[1], ph_g)) timed_out = true;
+    if (!tc::mbar_wait(&bars[1], ph_g, tc::wait_limit_or_default(a.wait_limit))) timed_out = true;
     ph_g ^= 1u;
   }
   tc::fence_after_sync();
@@ -1544,7 +1544,7 @@ __device__ __forceinline__ void contract_tc_bf(const StpmPartialArgs& a, int nbl
   bool g_pending = false, timed_out = false, any = false;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += nblocks) {
     if (g_pending) {  // the G products of the previous tile read y^T and C
-      if (!tc::mbar_wait(&bars[1], ph_g)) timed_out = true;
+      if (!tc::mbar_wait(&bars[1], ph_g, tc::wait_limit_or_default(a.wait_limit))) timed_out = true;
       ph_g ^= 1u;
       g_pending = false;
     }
@@ -1573,7 +1573,7 @@ __device__ __forceinline__ void contract_tc_bf(const StpmPartialArgs& a, int nbl
       }
       tc::commit(&bars[0]);
     }
-    if (!tc::mbar_wait(&bars[0], ph_z)) timed_out = true;
+    if (!tc::mbar_wait(&bars[0], ph_z, tc::wait_limit_or_default(a.wait_limit))) timed_out = true;
     ph_z ^= 1u;
     tc::fence_after_sync();
     {
@@ -1641,7 +1641,7 @@ __device__ __forceinline__ void contract_tc_bf(const StpmPartialArgs& a, int nbl
     any = true;
   }
   if (g_pending) {
-    if (!tc::mbar_wait(&bars[1], ph_g)) timed_out = true;
+    if (!tc::mbar_wait(&bars[1], ph_g, tc::wait_limit_or_default(a.wait_limit))) timed_out = true;
     ph_g ^= 1u;
   }
   tc::fence_after_sync();

@@ -36,6 +36,7 @@ struct StpmPartialArgs {
   int64_t part_stride;
   int nblocks;           // batched launches: CTAs of this graph (multiple of the cluster size)
   unsigned* flags;       // device flag word (MMSB_ERR_TIMEOUT of a bounded wait), may be null
+  long long wait_limit;  // clock64 cycles a bounded wait may take (0: about one second)
 };
 
 struct StpmReduceArgs {

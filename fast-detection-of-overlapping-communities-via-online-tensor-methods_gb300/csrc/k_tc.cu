@@ -28,7 +28,7 @@ __device__ __forceinline__ uint32_t sm_addr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ bool mbar_wait_limited(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait_limited(uint32_t bar, uint32_t parity, long long limit) {
   const long long start = clock64();
   while (true) {
     uint32_t ok;
@@ -39,7 +39,7 @@ __device__ __forceinline__ bool mbar_wait_limited(uint32_t bar, uint32_t parity)
         : "r"(bar), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (clock64() - start > 2000000000LL) return false;
+    if (clock64() - start > limit) return false;
   }
 }
 
@@ -70,7 +70,8 @@ __device__ __forceinline__ uint32_t tile_off(int r, int k) {
 __global__ void __launch_bounds__(kTcThreads, 1)
 gram_tc_kernel(const float* __restrict__ A, int lda, int pa, const float* __restrict__ B, int ldb,
                int pb, int64_t n, int64_t rows_per_split, double* __restrict__ partials,
-               unsigned* flags) {
+               unsigned* flags, long long wait_limit) {
+  const long long wl = wait_limit > 0 ? wait_limit : 2000000000LL;
   extern __shared__ __align__(1024) unsigned char tc_raw[];
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ uint32_t tmem_slot;
@@ -136,7 +137,7 @@ gram_tc_kernel(const float* __restrict__ A, int lda, int pa, const float* __rest
     unsigned char* stage = base + st * kStageBytes;
     // the MMAs that last read this stage (chunk c - 2) must be done
     if (issued[st]) {
-      if (!mbar_wait_limited(sm_addr(&bars[st]), phase[st])) timed_out = true;
+      if (!mbar_wait_limited(sm_addr(&bars[st]), phase[st], wl)) timed_out = true;
       phase[st] ^= 1u;
       issued[st] = 0;
     }
@@ -205,7 +206,7 @@ gram_tc_kernel(const float* __restrict__ A, int lda, int pa, const float* __rest
   // wait for every outstanding commit (also after a timeout, bounded)
   for (int st = 0; st < 2; ++st)
     if (issued[st]) {
-      if (!mbar_wait_limited(sm_addr(&bars[st]), phase[st])) timed_out = true;
+      if (!mbar_wait_limited(sm_addr(&bars[st]), phase[st], wl)) timed_out = true;
       phase[st] ^= 1u;
     }
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -261,7 +262,7 @@ int gram_tc_nsplit(int64_t n, int pa, int pb) {
 
 cudaError_t gram_tc_partial(const float* A, int lda, int pa, const float* B, int ldb, int pb,
                             int64_t n, double* partials, int nsplit, unsigned* flags,
-                            cudaStream_t s) {
+                            cudaStream_t s, long long wait_limit) {
   static bool set = false;
   if (!set) {
     MMSB_CUDA_TRY(cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -270,7 +271,8 @@ cudaError_t gram_tc_partial(const float* A, int lda, int pa, const float* B, int
   }
   const int64_t rows = round_up(ceil_div(n, nsplit), kTcK);
   dim3 grid((unsigned)ceil_div(pa, kTcM), (unsigned)ceil_div(pb, kTcN), (unsigned)nsplit);
-  gram_tc_kernel<<<grid, kTcThreads, kTcSmem, s>>>(A, lda, pa, B, ldb, pb, n, rows, partials, flags);
+  gram_tc_kernel<<<grid, kTcThreads, kTcSmem, s>>>(A, lda, pa, B, ldb, pb, n, rows, partials, flags,
+                                                   wait_limit);
   ++g_launch_count;
   return cudaGetLastError();
 }

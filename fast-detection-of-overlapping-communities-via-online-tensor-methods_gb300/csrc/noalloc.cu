@@ -13,10 +13,12 @@
 // calls that overlap on the GPU (different streams, or different host threads)
 // race on it and must be serialised by the caller.  Each call clears the part
 // that must start at zero (the per-column counters) itself.  The first call
-// on a device looks the array's device address up once (see below); make that
+// in a CUDA context looks the array's device address up (see below); make that
 // first call before any stream capture.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 
 #include "common.cuh"
@@ -28,28 +30,48 @@ constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
-
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
-// Device address of the scratch array for the current device.  The first
-// call on a device looks the symbol up (this may load the module); later
-// calls reuse the cached address.
-cudaError_t scratch_for_current_device(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+// Device address of the scratch array in the current context.  The address
+// is looked up once per context and cached under the context's unique ID
+// (cuCtxGetId, reached through the runtime's driver entry point, so no link
+// to the driver library is needed): a device reset or a framework that
+// destroys and recreates the primary context gets a new ID and so a fresh
+// lookup instead of a stale pointer.
+cudaError_t scratch_for_current_context(void** out) {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static std::mutex mu;
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static unsigned long long cached_id = ~0ull;
+  static void* cached_addr = nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  cudaError_t e = cudaFree(nullptr);  // makes the device's primary context current (no allocation)
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[dev]) {
+  if (!get_current || !get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+    if (e != cudaSuccess || q1 != cudaDriverEntryPointSuccess) return cudaErrorNotSupported;
+    e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e != cudaSuccess || q2 != cudaDriverEntryPointSuccess) return cudaErrorNotSupported;
+    get_current = reinterpret_cast<GetCurrent>(f1);
+    get_id = reinterpret_cast<GetId>(f2);
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+    return cudaErrorContextIsDestroyed;
+  if (id != cached_id || !cached_addr) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = p;
+    cached_addr = p;
+    cached_id = id;
   }
-  *out = g_scratch_addr[dev];
+  *out = cached_addr;
   return cudaSuccess;
 }
 
@@ -60,8 +82,14 @@ extern "C" mmsb_status mmsb_op_spmm_t_noalloc(const int64_t* d_row_ptr, const in
                                               int64_t nnz, const float* d_P, int64_t p, float alpha,
                                               float* d_Y, void* stream) {
   if (!d_row_ptr || (nnz > 0 && !d_col_idx) || !d_P || !d_Y || n_rows < 0 || n_cols < 0 ||
-      nnz < 0 || p < 4 || p % 4 != 0 || n_cols > INT32_MAX || n_rows > INT32_MAX)
+      nnz < 0 || p < 4 || p % 4 != 0 || n_cols > INT32_MAX || n_rows > INT32_MAX ||
+      (n_rows == 0 && nnz > 0))
     return MMSB_ERR_INVALID_ARG;
+  // the panels are read and written as 16-byte vectors
+  if (((uintptr_t)d_P | (uintptr_t)d_Y) & 15u) return MMSB_ERR_INVALID_ARG;
+  // sizes beyond the array are refused before any product that could wrap
+  if ((size_t)nnz > kNoAllocScratchBytes / 8 || (size_t)n_cols > kNoAllocScratchBytes / 16)
+    return MMSB_ERR_UNSUPPORTED;
   // scratch layout: column counters (u64, n_cols+1) | transposed row offsets
   // (i64, n_cols+1) | staging columns (i32, nnz) [+ staging values (f32, nnz)]
   // | transposed columns (i32, nnz) [+ transposed values (f32, nnz)]
@@ -74,7 +102,7 @@ extern "C" mmsb_status mmsb_op_spmm_t_noalloc(const int64_t* d_row_ptr, const in
   const size_t need = counters + staging + rpT + ciT + valT;
   if (need > kNoAllocScratchBytes) return MMSB_ERR_UNSUPPORTED;  // block too large for the array
   void* base = nullptr;
-  cudaError_t e = scratch_for_current_device(&base);
+  cudaError_t e = scratch_for_current_context(&base);
   if (e != cudaSuccess) return MMSB_ERR_CUDA;
   unsigned char* s = static_cast<unsigned char*>(base);
   int32_t* work = reinterpret_cast<int32_t*>(s);  // counters, then staging (csr_transpose layout)

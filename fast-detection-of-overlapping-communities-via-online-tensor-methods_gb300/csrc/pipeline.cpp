@@ -94,7 +94,12 @@ void check_flags(mmsb_ctx* c, const char* stage) {
     ck(cudaMemsetAsync(c->flags, 0, sizeof(unsigned), c->s), "flags");
     throw MmsbError(MMSB_ERR_NUMERICAL, std::string(stage) + ": non-finite values");
   }
-  if (f & kFlagTimeout) throw MmsbError(MMSB_ERR_TIMEOUT, std::string(stage) + ": device wait timed out");
+  if (f & kFlagTimeout) {
+    // cleared like the numerical flags: the waits that gave up have returned,
+    // and the context stays usable for the next call
+    ck(cudaMemsetAsync(c->flags, 0, sizeof(unsigned), c->s), "flags");
+    throw MmsbError(MMSB_ERR_TIMEOUT, std::string(stage) + ": device wait timed out");
+  }
 }
 
 // SpMM with timing bookkeeping (algorithmic bytes: CSR + one panel-row
@@ -198,11 +203,11 @@ Nys svd_sym_nystrom(mmsb_ctx* c, const std::string& tag, const float* A, int lda
   float* Q1 = c->tbuf<float>(tag + ".Q1", (size_t)n * round_up(m, 4));
   const int ldq = (int)round_up(m, 4);
   // CholQR2: A = Q_A R_A
-  ck(gram_tsk(A, lda, m, A, lda, m, n, 1.0, S1, part, cap, s, c->flags), "gram1");
+  ck(gram_tsk(A, lda, m, A, lda, m, n, 1.0, S1, part, cap, s, c->flags, c->wait_limit), "gram1");
   ck(chol_upper_drop(m, S1, m, R1, 1e-300, c->flags, s), "chol1");
   ck(trinv_upper(m, R1, T1, s), "trinv1");
   ck(panel_times_small(A, lda, m, n, T1, m, m, Q1, ldq, s), "Q1");
-  ck(gram_tsk(Q1, ldq, m, Q1, ldq, m, n, 1.0, S2, part, cap, s, c->flags), "gram2");
+  ck(gram_tsk(Q1, ldq, m, Q1, ldq, m, n, 1.0, S2, part, cap, s, c->flags, c->wait_limit), "gram2");
   // S2 = Q1^T Q1 is close to I: its factor needs no more than FP32 (Q1 itself is FP32)
   ck(chol_upper_drop_f32(m, S2, m, R2, c->flags, s), "chol2");
   ck(dgemm_small(false, false, m, m, m, 1.0, R2, m, R1, m, 0.0, RA, m, s), "R_A");
@@ -598,6 +603,7 @@ StpmPartialArgs stpm_partial_args(mmsb_ctx* c, int q1, int q2, int q3, int64_t b
   a.part_stride = stride;
   a.nblocks = nblocks;
   a.flags = c->flags;
+  a.wait_limit = c->wait_limit;
   return a;
 }
 

@@ -94,8 +94,16 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
                : "memory");
 }
 
-// waits for the phase with the given parity; false after about one second
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// clock64 cycles a bounded wait gives up after by default (about one second)
+constexpr long long kWaitLimitDefault = 2000000000LL;
+__device__ __forceinline__ long long wait_limit_or_default(long long v) {
+  return v > 0 ? v : kWaitLimitDefault;
+}
+
+// waits for the phase with the given parity; false after `limit` clock64
+// cycles (the caller then reports kFlagTimeout instead of hanging)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          long long limit = kWaitLimitDefault) {
   const uint32_t b = sm_addr(bar);
   const long long start = clock64();
   while (true) {
@@ -107,7 +115,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
         : "r"(b), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (clock64() - start > 2000000000LL) return false;
+    if (clock64() - start > limit) return false;
   }
 }
 

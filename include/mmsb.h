@@ -270,6 +270,18 @@ mmsb_status mmsb_stpm_loss_bwd(mmsb_ctx* ctx, const double* phi, int64_t node_be
  * stops at the next step boundary and the call returns MMSB_ERR_STOPPED. */
 void mmsb_request_stop(mmsb_ctx* ctx);
 const char* mmsb_last_error(const mmsb_ctx* ctx);
+
+/* Failure detection of the device side.  The reference has no device-side
+ * waits to bound (its CULA calls block, GPU/stpm.c:497-809); here every wait
+ * of the STPM kernels and of the tensor-core Grams on a barrier, a copy or a
+ * peer CTA gives up after a limit of clock64 cycles, sets a device flag and
+ * the call returns MMSB_ERR_TIMEOUT with the context still usable.
+ * mmsb_set_wait_limit: that limit for the kernels of this context
+ * (0 = about one second).  mmsb_diag_wait_timeout: one bounded wait, of the
+ * same helper, on a barrier that nothing arrives at, with a limit of `cycles`
+ * (1 .. 2e9): returns MMSB_ERR_TIMEOUT when the give-up path works. */
+mmsb_status mmsb_set_wait_limit(mmsb_ctx* ctx, int64_t cycles);
+mmsb_status mmsb_diag_wait_timeout(mmsb_ctx* ctx, int64_t cycles);
 const char* mmsb_status_string(mmsb_status st);
 /* Writes a buffer larger than L2 on the context's stream (benchmark hygiene). */
 mmsb_status mmsb_flush_l2(mmsb_ctx* ctx);
@@ -297,15 +309,19 @@ mmsb_status mmsb_op_symeig(const double* A, int32_t n, double* evals, double* ev
  * wait on cudaMalloc, which can synchronize the device): same result as
  * mmsb_op_spmm with
  * transpose != 0, but every pointer is a DEVICE pointer the caller owns and
- * the call allocates nothing.  G: n_rows x n_cols CSR (d_val NULL = binary);
- * P: n_rows x p row-major, Y: n_cols x p row-major, p a multiple of 4, 16-byte
- * aligned.  The transposed copy of G is built in a fixed 8 MiB device array
- * compiled into the library (held on every GPU that loads it until exit):
- * blocks needing more (about 16 * (n_cols + 1 + nnz) bytes) return
- * MMSB_ERR_UNSUPPORTED before any work.  All calls share that array, so calls
- * that overlap on the GPU race; serialise them.  The first call on a device
- * looks the array up (this can load the module): make it before any stream
- * capture.  stream: a cudaStream_t (NULL = default stream). */
+ * the call allocates nothing.  G: n_rows x n_cols CSR (d_val NULL = binary)
+ * with row_ptr[0] == 0, non-decreasing offsets, row_ptr[n_rows] == nnz and
+ * 0 <= col < n_cols (not checked: a block breaking them gives a wrong Y, but
+ * no access outside the buffers and the array); P: n_rows x p row-major,
+ * Y: n_cols x p row-major, p a multiple of 4, both 16-byte aligned
+ * (MMSB_ERR_INVALID_ARG otherwise).  The transposed copy of G is built in a
+ * fixed 8 MiB device array compiled into the library (held on every GPU that
+ * loads it until exit): blocks needing more (about 16 * (n_cols + 1 + nnz)
+ * bytes) return MMSB_ERR_UNSUPPORTED before any work.  All calls share that
+ * array, so calls that overlap on the GPU race; serialise them.  The first
+ * call in a CUDA context looks the array up (this can load the module): make
+ * it before any stream capture; after a device reset the next call looks it
+ * up again.  stream: a cudaStream_t (NULL = default stream). */
 mmsb_status mmsb_op_spmm_t_noalloc(const int64_t* d_row_ptr, const int32_t* d_col_idx,
                                    const float* d_val, int64_t n_rows, int64_t n_cols,
                                    int64_t nnz, const float* d_P, int64_t p, float alpha,

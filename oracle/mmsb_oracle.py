@@ -45,24 +45,61 @@ def orthogonalize_cols(Y, tol=TOLERANCE):
     return Y
 
 
-def orthogonalize_cols_cgs2(Y, tol=TOLERANCE):
+def orthogonalize_cols_cgs2(Y, tol=TOLERANCE, block=32):
     """The same column orthonormalisation with classical Gram-Schmidt applied
-    twice per column (vectorised); equal to orthogonalize_cols to round-off.
-    Used where the oracle is timed on large inputs."""
+    twice per column, blocked (each block of columns is projected against the
+    finished ones twice with matrix products, then orthonormalised column by
+    column with the same drop rule); equal to orthogonalize_cols to round-off.
+    Used where the oracle is timed on large inputs.  When every column keeps
+    a residual well above tol (the Householder R's diagonal shows it), no
+    column is dropped and the result is the Q of the QR factorisation with a
+    positive R diagonal, which Householder QR gives directly."""
     Y = np.array(Y, dtype=np.float64, copy=True)
     n, c = Y.shape
+    if n >= c:
+        Qh, R = np.linalg.qr(Y)
+        d = np.abs(np.diag(R))
+        if d.min() > 2.0 * tol:
+            return Qh * np.where(np.diag(R) < 0, -1.0, 1.0)
     Q = np.zeros_like(Y)
-    for j in range(c):
-        v = Y[:, j].copy()
+    for j0 in range(0, c, block):
+        j1 = min(c, j0 + block)
+        V = Y[:, j0:j1].copy()
         for _ in range(2):
-            if j:
-                v -= Q[:, :j] @ (Q[:, :j].T @ v)
-        nrm = np.sqrt(v @ v)
-        Q[:, j] = v * ((1.0 / nrm) if nrm > tol else 0.0)
+            if j0:
+                V -= Q[:, :j0] @ (Q[:, :j0].T @ V)
+        for j in range(j0, j1):
+            v = V[:, j - j0]
+            for _ in range(2):
+                if j > j0:
+                    v -= Q[:, j0:j] @ (Q[:, j0:j].T @ v)
+            nrm = np.sqrt(v @ v)
+            Q[:, j] = v * ((1.0 / nrm) if nrm > tol else 0.0)
     return Q
 
 
 FAST_GS = False  # True: orthogonalize_cols_cgs2 inside svd_sym_nystrom
+SPMM_THREADS = 1  # > 1: sparse x dense products split by rows over host threads
+
+
+def _mm(A, P):
+    """A @ P; with SPMM_THREADS > 1 and a sparse A, row blocks of the product
+    run on a thread pool (scipy's sparse kernels release the GIL; every row is
+    computed exactly as in the single product)."""
+    if SPMM_THREADS <= 1 or not sp.issparse(A) or A.shape[0] < 4096 or np.ndim(P) != 2:
+        return A @ P
+    from concurrent.futures import ThreadPoolExecutor
+    A = A.tocsr()
+    nt = SPMM_THREADS
+    bounds = np.linspace(0, A.shape[0], nt + 1).astype(np.int64)
+    out = np.empty((A.shape[0], P.shape[1]), dtype=np.result_type(A.dtype, P.dtype))
+
+    def run(i):
+        out[bounds[i]:bounds[i + 1]] = A[bounds[i]:bounds[i + 1]] @ P
+
+    with ThreadPoolExecutor(nt) as ex:
+        list(ex.map(run, range(nt)))
+    return out
 
 
 def svd_sym_nystrom(M, k, rows_factor=20, tol=TOLERANCE):
@@ -118,12 +155,12 @@ def second_whiten(Gxa, Gxb, Gxc, k, alpha0, sketches, rows_factor=20, normalize=
     mu_a, mu_b, mu_c = column_means(Gxa, inv), column_means(Gxb, inv), column_means(Gxc, inv)
     Gxa, Gxb, Gxc = (sp.csr_matrix(g, dtype=np.float64) for g in (Gxa, Gxb, Gxc))
     GaT, GbT, GcT = Gxa.T.tocsr(), Gxb.T.tocsr(), Gxc.T.tocsr()
-    zb_num = lambda P: inv * (GaT @ (Gxc @ P))    # Gx_a^T Gx_c (n_A x n_C)
-    zb_den = lambda P: inv * (GbT @ (Gxc @ P))    # Gx_b^T Gx_c (n_B x n_C)
-    zb_den_T = lambda P: inv * (GcT @ (Gxb @ P))
-    zc_num = lambda P: inv * (GaT @ (Gxb @ P))    # Gx_a^T Gx_b (n_A x n_B)
-    zc_den = lambda P: inv * (GcT @ (Gxb @ P))    # Gx_c^T Gx_b (n_C x n_B)
-    zc_den_T = lambda P: inv * (GbT @ (Gxc @ P))
+    zb_num = lambda P: inv * _mm(GaT, _mm(Gxc, P))    # Gx_a^T Gx_c (n_A x n_C)
+    zb_den = lambda P: inv * _mm(GbT, _mm(Gxc, P))    # Gx_b^T Gx_c (n_B x n_C)
+    zb_den_T = lambda P: inv * _mm(GcT, _mm(Gxb, P))
+    zc_num = lambda P: inv * _mm(GaT, _mm(Gxb, P))    # Gx_a^T Gx_b (n_A x n_B)
+    zc_den = lambda P: inv * _mm(GcT, _mm(Gxb, P))    # Gx_c^T Gx_b (n_C x n_B)
+    zc_den_T = lambda P: inv * _mm(GbT, _mm(Gxc, P))
     R_c, R_b, R_a = (np.asarray(r, dtype=np.float64) for r in sketches)
 
     V_c, U_c, Linv_c = pinv_component(zc_den, zc_den_T, R_c, k, rows_factor, tol)
@@ -149,9 +186,9 @@ def whitened_data(Gxa, Gxb, Gxc, wh):
     W = wh["W"]
     Wb = wh["Zb2"].T @ (wh["Zb1"].T @ W)           # ((W^T Zb1) Zb2)^T
     Wc = wh["Zc2"].T @ (wh["Zc1"].T @ W)
-    Da = np.asarray((Gxa @ W).T)
-    Db = np.asarray((Gxb @ Wb).T)
-    Dc = np.asarray((Gxc @ Wc).T)
+    Da = np.asarray(_mm(Gxa, W).T)
+    Db = np.asarray(_mm(Gxb, Wb).T)
+    Dc = np.asarray(_mm(Gxc, Wc).T)
     return dict(Da=Da, Db=Db, Dc=Dc, Da_mu=W.T @ wh["mu_a"], Db_mu=Wb.T @ wh["mu_b"],
                 Dc_mu=Wc.T @ wh["mu_c"], Wb=Wb, Wc=Wc)
 
@@ -330,11 +367,11 @@ def norm_prob_matrix(P):
 def postprocess(Gxa, Gba, Gca, wh, lam, phi, tol=TOLERANCE):
     """CommunityDetection.cpp:98-139: returns (pi_raw, pi) k x (n_X+n_A+n_B+n_C)."""
     P_A = wh["W"] @ (phi * pinv_vector(lam, tol))          # (diag(1/lam) Phi^T W^T)^T
-    pi_x = (Gxa @ P_A).T
-    pi_b = (Gba @ P_A).T
-    pi_c = (Gca @ P_A).T
+    pi_x = _mm(Gxa, P_A).T
+    pi_b = _mm(Gba, P_A).T
+    pi_c = _mm(Gca, P_A).T
     P_A2 = wh["Zb2"].T @ (wh["Zb1"].T @ P_A)
-    pi_a = (Gba.T @ P_A2).T
+    pi_a = _mm(Gba.T.tocsr(), P_A2).T
     raw = np.concatenate([np.asarray(m) for m in (pi_x, pi_a, pi_b, pi_c)], axis=1)
     return raw, norm_prob_matrix(raw)
 

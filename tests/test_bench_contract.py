@@ -1,7 +1,8 @@
 """bench.py's reference arm (the FP64 CPU port timed on the host) keeps the
 JSON-line contract: one line from rank 0, the same metric and config as the
-GPU arm, a cpu_baseline describing the run and an e2e entry without copies.
-Runs on a 20,000-node graph so that it finishes in seconds."""
+GPU arm, a cpu_baseline describing the run and an e2e entry without copies;
+the process never loads the GPU library.  Runs on a 20,000-node graph so that
+it finishes in seconds."""
 import json
 import os
 import socket
@@ -40,6 +41,18 @@ def test_reference_arm_json_line():
     lines = _lines(out.stdout)
     assert len(lines) == 1
     _check(lines[0])
+
+
+def test_reference_arm_does_not_load_the_gpu_library():
+    code = ("import runpy, sys; sys.argv = ['bench.py'] + %r; "
+            "runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('LOADED', 'libmmsb' in maps, 'mmsb_gb300' in sys.modules)") % (ARGS,)
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                         timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert "LOADED False False" in out.stdout
+    assert len(_lines(out.stdout)) == 1
 
 
 def test_reference_arm_under_torchrun_prints_once():
