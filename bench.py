@@ -50,7 +50,7 @@ BATCH = dict(name="mmsb-batch256-n2k-200k-k5-64-online", graphs=256, n_lo=2_000,
 # the precision configuration: the BF16 form beside the FP32 form, errors of
 # both against an FP64 STPM and post-processing
 PRECISION = dict(name="mmsb-n2m-k200-bf16-online", n=2_000_000, k=200, alpha0=0.5, p_in=0.02,
-                 p_out=1e-5, sweeps=5, minibatch=65536, seed=0)
+                 p_out=1e-5, sweeps=30, minibatch=65536, seed=0)
 
 
 def load_pkg():
@@ -626,6 +626,102 @@ def run_precision(args, ws, rank, local):
     print(json.dumps(line), flush=True)
 
 
+# the differentiation configuration: the adjoint of the implicit tensor loss
+ADJOINT = dict(name="mmsb-n500k-k100-bf16-adjoint", n=500_000, k=100, alpha0=1.0, p_in=0.04,
+               p_out=4e-4, sweeps=30, minibatch=8192, seed=0, directions=1000, fd_step=1e-6)
+
+
+def run_adjoint(args, ws, rank, local):
+    """The adjoint form: the device gradient of L(Phi) (mmsb_stpm_loss_bwd, Z
+    recomputed per minibatch) against FP64 central differences of the FP64
+    loss on the device's whitened data along random unit directions and
+    against the FP64 oracle gradient, on one 8,192-node minibatch; then the
+    full BF16 adjoint solve (30 sweeps of 8,192-node minibatches, last sweep
+    FP32) beside the FP32 online solve, node-updates/s."""
+    if rank != 0:
+        return
+    mm = load_pkg()
+    O = oracle_module()
+    wl = dict(ADJOINT)
+    t0 = time.perf_counter()
+    graph = make_graph(mm, wl)
+    t_gen = time.perf_counter() - t0
+    k, a0, nX = wl["k"], wl["alpha0"], graph.parts[0]
+    rng = np.random.default_rng(wl["seed"])
+    check = {}
+    cfg = mm.default_config(k=k, alpha0=a0, stpm_method=mm.STPM_ADJOINT, sweeps=wl["sweeps"],
+                            minibatch=wl["minibatch"], seed=wl["seed"], device=local, tau=0.1,
+                            precision=mm.PREC_BF16)
+    with mm.Pipeline(cfg) as p:
+        p.upload(graph).whiten()
+        y64 = {n_: np.asarray(v, dtype=np.float64) for n_, v in p.whitened().items()}
+        # a point off the orthonormal manifold, where the orthogonality term
+        # of L is not flat
+        phi = O.qr_pos(rng.standard_normal((k, k))) + 0.05 * rng.standard_normal((k, k))
+        b, cnt = 0, wl["minibatch"]
+        nodes = np.arange(b, b + cnt)
+        t1 = time.perf_counter()
+        g_dev = p.loss_grad(phi, b, cnt)
+        L_dev = p.loss(phi, b, cnt)
+        t_dev = time.perf_counter() - t1
+        t1 = time.perf_counter()
+        g_o = O.loss_bwd(phi, y64, nodes, a0, 1.0)
+        L_o = O.loss_fwd(phi, y64, nodes, a0, 1.0)
+        h, errs, scale = wl["fd_step"], [], max(1.0, float(np.abs(g_o).max()))
+        for _ in range(wl["directions"]):
+            d = rng.standard_normal((k, k))
+            d /= np.linalg.norm(d)
+            fd = (O.loss_fwd(phi + h * d, y64, nodes, a0, 1.0)
+                  - O.loss_fwd(phi - h * d, y64, nodes, a0, 1.0)) / (2 * h)
+            errs.append(abs(float(np.sum(g_dev * d)) - fd) / scale)
+        t_fd = time.perf_counter() - t1
+        check = {"directions": wl["directions"], "fd_step": h, "nodes": cnt,
+                 "max_abs_err_over_max_grad": float(max(errs)),
+                 "median_abs_err_over_max_grad": float(np.median(errs)),
+                 "grad_rel_err_vs_fp64": float(np.abs(g_dev - g_o).max() / np.abs(g_o).max()),
+                 "loss_rel_err_vs_fp64": float(abs(L_dev - L_o) / max(abs(L_o), 1e-300)),
+                 "device_fwd_bwd_s": t_dev, "fp64_fd_s": t_fd,
+                 "note": "FP64 central differences of the FP64 loss (oracle) on the device's "
+                         "whitened data; errors relative to max |dL/dPhi|"}
+    forms = {}
+    for name, method, prec in (("bf16_adjoint", mm.STPM_ADJOINT, mm.PREC_BF16),
+                               ("fp32_online", mm.STPM_ONLINE, mm.PREC_FP32)):
+        cfg = mm.default_config(k=k, alpha0=a0, stpm_method=method, sweeps=wl["sweeps"],
+                                minibatch=wl["minibatch"], seed=wl["seed"], device=local,
+                                tau=0.1, precision=prec)
+        with mm.Pipeline(cfg) as p:
+            p.upload(graph)
+            for _ in range(max(1, min(args.warmup, 2))):
+                p.run()
+            ms, stages = [], {"whiten_ms": 0.0, "stpm_ms": 0.0, "post_ms": 0.0}
+            for _ in range(max(1, args.steps)):
+                p.flush_l2()
+                p.synchronize()
+                p.run()
+                st = p.stats()
+                ms.append(st["total_ms"])
+                for key in stages:
+                    stages[key] += st[key]
+            step = statistics.mean(ms)
+            forms[name] = {"value": nX * wl["sweeps"] / (step / 1e3), "unit": "node-updates/s",
+                           "ms_per_step": step,
+                           "stages_ms_per_step": {k_: v / len(ms) for k_, v in stages.items()},
+                           "stpm_node_updates_per_s": nX * wl["sweeps"] / (stages["stpm_ms"]
+                                                                            / len(ms) / 1e3)}
+    line = {
+        "metric": "stpm_node_updates_per_s", "value": forms["bf16_adjoint"]["value"],
+        "unit": "node-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": forms["bf16_adjoint"]["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": wl["name"], **{k_: v for k_, v in wl.items() if k_ != "name"},
+                   "nnz_directed": int(sum(b_.nnz for b_ in graph.blocks[:3]) * 2),
+                   "generation_s": t_gen, "l2": "256 MiB buffer written between timed steps"},
+        "gradient_check": check, "forms": forms,
+        "bf16_adjoint_over_fp32_online": forms["bf16_adjoint"]["value"] / forms["fp32_online"]["value"],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_io(args, ws, rank):
     """The file contract on the default graph: its five blocks written as the
     reference's COO text input (mmsb_write_coo) and read back by the parallel
@@ -702,6 +798,9 @@ def main():
                     help="the batching configuration (256 graphs) instead of the default")
     ap.add_argument("--precision", action="store_true",
                     help="the precision configuration (n = 2M, k = 200, BF16 form vs FP32 vs FP64)")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="the differentiation configuration (n = 500k, k = 100: gradient check "
+                         "against FP64 finite differences, BF16 adjoint solve)")
     ap.add_argument("--io", action="store_true",
                     help="the file contract: COO text parse/write and binary CSR on the default graph")
     args = ap.parse_args()
@@ -718,6 +817,9 @@ def main():
         return
     if args.precision and args.impl != "reference":
         run_precision(args, ws, rank, local)
+        return
+    if args.adjoint and args.impl != "reference":
+        run_adjoint(args, ws, rank, local)
         return
     if args.impl == "reference":
         run_reference(args, wl, ws, rank)

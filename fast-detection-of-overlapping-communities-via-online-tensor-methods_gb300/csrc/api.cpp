@@ -291,10 +291,18 @@ mmsb_status mmsb_write_gpu_outputs(mmsb_ctx* c, const char* dir) {
     const int64_t N = mmsb_num_nodes(c);
     std::vector<float> pi((size_t)N * k), phi((size_t)k * k);
     std::vector<double> lam(k), conv((size_t)c->conv_count);
-    d2h(c, pi.data(), c->pi, sizeof(float) * pi.size());
     d2h(c, phi.data(), c->phi, sizeof(float) * phi.size());
     d2h(c, lam.data(), c->lambda, sizeof(double) * k);
     if (!conv.empty()) d2h(c, conv.data(), c->conv, sizeof(double) * conv.size());
+    ck(cudaStreamSynchronize(c->s), "sync");
+    // Pi files hold the raw unwhitened memberships scaled by ||lambda||_2
+    // (GPU/post_proc.c:86-114), not the normalised Pi of the CPU tree
+    double lnorm = 0.0;
+    for (int i = 0; i < k; ++i) lnorm += lam[i] * lam[i];
+    lnorm = std::sqrt(lnorm);
+    float* raw = c->tbuf<float>("pi_raw", (size_t)N * k);
+    pipeline_post_raw(c, lnorm, raw);
+    d2h(c, pi.data(), raw, sizeof(float) * pi.size());
     ck(cudaStreamSynchronize(c->s), "sync");
     // file names of GPU/stpm.h:82-91: <name>_<NCOM>_<ALPHA_0>_<LEARN_RATE>.txt
     char tail[96];

@@ -54,10 +54,12 @@ cudaError_t row_sums_f64(const int64_t* rp, const float* val, int64_t n_rows, do
 
 // Fused unwhitening + normProbMatrix + threshold over one CSR block:
 // raw[r,:] = G[r,:] * P (ld = ldp, first k columns), normalised per row,
-// written to pi[(row_offset + r) * k + i] and set bits.
+// written to pi[(row_offset + r) * k + i] and set bits.  raw_scale > 0:
+// raw_scale * raw written instead (no normalisation, bits untouched).
 cudaError_t unwhiten_normprob(const int64_t* rp, const int32_t* ci, const float* val,
                               int64_t n_rows, const float* P, int ldp, int k, float tau,
-                              int64_t row_offset, float* pi, uint32_t* bits, cudaStream_t s);
+                              int64_t row_offset, float* pi, uint32_t* bits, cudaStream_t s,
+                              float raw_scale = 0.f);
 
 // ---- dense (k_dense.cu) -----------------------------------------------------
 

@@ -196,7 +196,8 @@ __global__ void row_sums_kernel(const int64_t* __restrict__ rp, const float* __r
 __global__ void __launch_bounds__(256) unwhiten_normprob_kernel(
     const int64_t* __restrict__ rp, const int32_t* __restrict__ ci,
     const float* __restrict__ val, int64_t n_rows, const float4* __restrict__ P, int c4, int k,
-    float tau, int64_t row_offset, float* __restrict__ pi, uint32_t* __restrict__ bits) {
+    float tau, int64_t row_offset, float* __restrict__ pi, uint32_t* __restrict__ bits,
+    float raw_scale) {
   const int lane = threadIdx.x & 31;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (row >= n_rows) return;
@@ -228,6 +229,17 @@ __global__ void __launch_bounds__(256) unwhiten_normprob_kernel(
     neg += __shfl_xor_sync(0xffffffffu, neg, off);
   }
   nz = __any_sync(0xffffffffu, nz);
+  if (raw_scale > 0.f) {
+    // raw unwhitened memberships (the GPU tree's Pi files), no normalisation
+    // and no set bits
+    float* out = pi + (row_offset + row) * (int64_t)k;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int idx = (e < 4 ? 4 * ch0 : 4 * ch1) + (e & 3);
+      if (idx < k) out[idx] = x[e] * raw_scale;
+    }
+    return;
+  }
   if (nz) {
     // Probability.cpp:45-55: the larger-magnitude mass fixes sign and scale
     const bool flip = fabsf(pos) < fabsf(neg);
@@ -367,13 +379,14 @@ cudaError_t row_sums_f64(const int64_t* rp, const float* val, int64_t n_rows, do
 
 cudaError_t unwhiten_normprob(const int64_t* rp, const int32_t* ci, const float* val,
                               int64_t n_rows, const float* P, int ldp, int k, float tau,
-                              int64_t row_offset, float* pi, uint32_t* bits, cudaStream_t s) {
+                              int64_t row_offset, float* pi, uint32_t* bits, cudaStream_t s,
+                              float raw_scale) {
   if (ldp % 4 != 0 || k > 256 || k > ldp) return cudaErrorInvalidValue;
   if (n_rows == 0) return cudaSuccess;
   const int T = 256;
   unwhiten_normprob_kernel<<<(unsigned)ceil_div(n_rows * 32, T), T, 0, s>>>(
       rp, ci, val, n_rows, reinterpret_cast<const float4*>(P), ldp / 4, k, tau, row_offset, pi,
-      bits);
+      bits, raw_scale);
   ++g_launch_count;
   return cudaGetLastError();
 }

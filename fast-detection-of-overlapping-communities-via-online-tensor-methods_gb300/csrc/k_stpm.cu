@@ -2043,18 +2043,22 @@ __global__ void __launch_bounds__(1024) batch_update_kernel(int k, float* __rest
 
 // lambda_i = phi_i . G_i (tensor value); sign fix so lambda_i > 0
 __global__ void tensor_value_kernel(int k, float* __restrict__ phi, const float* __restrict__ G,
-                                    double* __restrict__ lambda) {
+                                    double* __restrict__ lambda, double* __restrict__ phi64) {
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   if (i >= k) return;
   double s = 0.0;
-  for (int j = lane; j < k; j += 32) s += (double)phi[(int64_t)i * k + j] * G[(int64_t)i * k + j];
+  for (int j = lane; j < k; j += 32)
+    s += (phi64 ? phi64[(int64_t)i * k + j] : (double)phi[(int64_t)i * k + j]) * G[(int64_t)i * k + j];
 #pragma unroll
   for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
   const bool flip = s < 0.0;
   if (lane == 0) lambda[i] = flip ? -s : s;
   if (flip)
-    for (int j = lane; j < k; j += 32) phi[(int64_t)i * k + j] = -phi[(int64_t)i * k + j];
+    for (int j = lane; j < k; j += 32) {
+      phi[(int64_t)i * k + j] = -phi[(int64_t)i * k + j];
+      if (phi64) phi64[(int64_t)i * k + j] = -phi64[(int64_t)i * k + j];
+    }
 }
 
 template <int KP, int MODE, bool BF>
@@ -2360,8 +2364,9 @@ cudaError_t stpm_batch_update(int k, float* phi, const float* G, double* lambda,
   return cudaGetLastError();
 }
 
-cudaError_t stpm_tensor_values(int k, float* phi, const float* G, double* lambda, cudaStream_t s) {
-  tensor_value_kernel<<<(unsigned)ceil_div(k, 8), 256, 0, s>>>(k, phi, G, lambda);
+cudaError_t stpm_tensor_values(int k, float* phi, const float* G, double* lambda, cudaStream_t s,
+                               double* phi64) {
+  tensor_value_kernel<<<(unsigned)ceil_div(k, 8), 256, 0, s>>>(k, phi, G, lambda, phi64);
   ++g_launch_count;
   return cudaGetLastError();
 }

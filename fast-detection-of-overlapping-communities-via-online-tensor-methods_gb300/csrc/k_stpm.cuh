@@ -107,6 +107,9 @@ cudaError_t stpm_update_batched(int KP, const StpmUpdateArgs* args, int graphs, 
 cudaError_t stpm_update(const StpmUpdateArgs& a, cudaStream_t s);
 cudaError_t stpm_batch_update(int k, float* phi, const float* G, double* lambda, double* err,
                               cudaStream_t s);
-cudaError_t stpm_tensor_values(int k, float* phi, const float* G, double* lambda, cudaStream_t s);
+// lambda_i = phi_i . G_i in FP64 (phi64: an FP64 copy of Phi to use for the
+// dot product, may be null), sign fixed so lambda_i > 0 (both copies flipped)
+cudaError_t stpm_tensor_values(int k, float* phi, const float* G, double* lambda, cudaStream_t s,
+                               double* phi64 = nullptr);
 
 }  // namespace mmsb

@@ -5,6 +5,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #include "k_stpm.cuh"
@@ -776,16 +777,45 @@ void stpm_prepare(mmsb_ctx* c, const double* phi0) {
   }
 }
 
+// The final orthonormalisation of the BF16 form in FP64: two Cholesky QR
+// passes on the k x k Phi (FP64 Gram, Cholesky, triangular inverse and
+// products), the same Q as the per-step QR (diag(R) > 0).  Returns the FP64
+// Phi (device) and leaves its FP32 rounding in c->phi.
+static double* final_qr_f64(mmsb_ctx* c) {
+  const int k = c->k;
+  cudaStream_t s = c->s;
+  double* Pa = c->tbuf<double>("fq.Pa", (size_t)k * k);
+  double* Pb = c->tbuf<double>("fq.Pb", (size_t)k * k);
+  double* S = c->tbuf<double>("fq.S", (size_t)k * k);
+  double* R = c->tbuf<double>("fq.R", (size_t)k * k);
+  double* T = c->tbuf<double>("fq.T", (size_t)k * k);
+  ck(f32_to_f64(c->phi, Pa, (int64_t)k * k, s), "phi64");
+  for (int pass = 0; pass < 2; ++pass) {
+    ck(dgemm_small(true, false, k, k, k, 1.0, Pa, k, Pa, k, 0.0, S, k, s), "Phi^T Phi");
+    ck(chol_upper_drop(k, S, k, R, 1e-300, c->flags, s), "chol");
+    ck(trinv_upper(k, R, T, s), "R^-1");
+    ck(dgemm_small(false, false, k, k, k, 1.0, Pa, k, T, k, 0.0, Pb, k, s), "Phi R^-1");
+    std::swap(Pa, Pb);
+  }
+  ck(f64_to_f32(Pa, c->phi, (int64_t)k * k, s), "phi32");
+  return Pa;
+}
+
 // lambda_i = That(phi_i, phi_i, phi_i) over all of X, sign fixed so lambda > 0
-// (queued on the context's stream)
+// (queued on the context's stream).  The BF16 form first re-orthonormalises
+// Phi in FP64 and takes the final dot products phi_i . T(I, phi_i, phi_i)
+// with the FP64 Phi.
 void stpm_lambda_pass(mmsb_ctx* c) {
   const int k = c->k;
   const int64_t nx = c->nX;
   const double a0 = c->cfg.alpha0;
   const double p0 = (a0 + 1.0) * (a0 + 2.0) / 2.0, p1 = a0 * a0, p2 = -a0 * (a0 + 1.0) / 2.0;
+  double* phi64 = nullptr;
+  if (c->cfg.precision == MMSB_PREC_BF16 && c->cfg.stpm_method != MMSB_STPM_BATCH_POWER)
+    phi64 = final_qr_f64(c);
   float* G = c->tbuf<float>("G", (size_t)k * k);
   stpm_pass(c, kModePlain, 0, 1, 2, 0, nx, p0 / nx, p1, p2 / nx, 1.0, G, nullptr);
-  ck(stpm_tensor_values(k, c->phi, G, c->lambda, c->s), "lambda");
+  ck(stpm_tensor_values(k, c->phi, G, c->lambda, c->s, phi64), "lambda");
 }
 
 // statistics and device flags of an online / adjoint run (waits for the stream)
@@ -911,6 +941,24 @@ void pipeline_post(mmsb_ctx* c) {
   ck(unwhiten_normprob(BA.rp, BA.ci, BA.val, BA.n_rows, PA, ldk, k, tau, c->nX + c->nA, c->pi, c->bits, s), "pi_b");
   ck(unwhiten_normprob(CA.rp, CA.ci, CA.val, CA.n_rows, PA, ldk, k, tau, c->nX + c->nA + c->nB, c->pi, c->bits, s), "pi_c");
   c->have_post = true;
+}
+
+// The GPU tree's raw memberships (GPU/post_proc.c:86-106: Pi = ((W evecs)
+// inv_evals)^T G^T with inv_evals = diag(||lambda||_2 / lambda_i), the
+// pinv threshold applied, GPU/wrappers.cu genInvEvalMat): ||lambda||_2 times
+// the unnormalised Pi of pipeline_post, node-major N x k into `out` (device).
+void pipeline_post_raw(mmsb_ctx* c, double lambda_norm, float* out) {
+  if (!c->have_post) throw MmsbError(MMSB_ERR_STATE, "raw memberships before postproc");
+  const int k = c->k, ldk = c->ldk;
+  cudaStream_t s = c->s;
+  float* PA = c->tbuf<float>("PA", (size_t)c->nA * ldk);
+  float* PA2 = c->tbuf<float>("PA2", (size_t)c->nB * ldk);
+  const float sc = (float)lambda_norm;
+  const DevCsr &XA = c->g[0], &BA = c->g[3], &CA = c->g[4], &BAt = c->gt[3];
+  ck(unwhiten_normprob(XA.rp, XA.ci, XA.val, XA.n_rows, PA, ldk, k, 0.f, 0, out, nullptr, s, sc), "raw pi_x");
+  ck(unwhiten_normprob(BAt.rp, BAt.ci, BAt.val, BAt.n_rows, PA2, ldk, k, 0.f, c->nX, out, nullptr, s, sc), "raw pi_a");
+  ck(unwhiten_normprob(BA.rp, BA.ci, BA.val, BA.n_rows, PA, ldk, k, 0.f, c->nX + c->nA, out, nullptr, s, sc), "raw pi_b");
+  ck(unwhiten_normprob(CA.rp, CA.ci, CA.val, CA.n_rows, PA, ldk, k, 0.f, c->nX + c->nA + c->nB, out, nullptr, s, sc), "raw pi_c");
 }
 
 // ---------------------------------------------------------------------------

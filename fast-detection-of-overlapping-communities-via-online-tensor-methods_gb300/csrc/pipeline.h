@@ -28,6 +28,8 @@ void pipeline_whiten_finish(mmsb_ctx* c);
 void pipeline_ydata(mmsb_ctx* c);
 void pipeline_stpm(mmsb_ctx* c, const double* phi0);
 void pipeline_post(mmsb_ctx* c);
+// ||lambda||_2 * Lambda^-1 Phi^T W^T G^T (the GPU tree's raw Pi), N x k device
+void pipeline_post_raw(mmsb_ctx* c, double lambda_norm, float* out);
 
 // pieces of the online / adjoint STPM shared with the batched solver
 struct OnlineRound {

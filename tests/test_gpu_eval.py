@@ -70,18 +70,29 @@ def test_online_trace_matches_sweep_snapshots(mm, solved):
     assert abs(tr[4] - d) <= 1e-4 * d + 1e-6, (tr[4], d)
 
 
-def test_gpu_tree_output_files(solved, tmp_path):
+def test_gpu_tree_output_files(solved, tmp_path, oracle):
+    """The GPU tree's files (GPU/post_proc.c:86-114, GPU/stpm.c:915-975): the
+    Pi files hold the raw unwhitened memberships ((W evecs) diag(||lambda||_2 /
+    lambda_i))^T G^T, not the normalised Pi of the CPU tree."""
     g, p = solved
     p.write_gpu_outputs(tmp_path)
     tail = f"_{p.k}_1_1.txt"
-    pi = p.pi()
+    lam, phi = p.lam().astype(np.float64), p.phi().astype(np.float64)
+    Gxa, _, _, Gba, Gca = g.scipy_blocks()
+    raw_o, _ = oracle.postprocess(Gxa, Gba, Gca, p.whitening(), lam, phi)
+    raw_o = raw_o * np.linalg.norm(lam)
     nX, nA, nB, nC = g.parts
-    off = 0
+    off, raw = 0, []
     for name, n in (("Pi_X", nX), ("Pi_A", nA), ("Pi_B", nB), ("Pi_C", nC)):
         lines = (tmp_path / f"{name}{tail}").read_text().splitlines()
         assert len(lines) == p.k * n
-        assert lines[:50] == ["%5.25e" % float(v) for v in pi[:, off:off + n].ravel(order="F")[:50]]
+        assert all(re.fullmatch(r"-?\d\.\d{25}e[+-]\d\d", l) for l in lines[:50])
+        raw.append(np.array([float(l) for l in lines]).reshape(n, p.k).T)
         off += n
+    raw = np.concatenate(raw, axis=1)
+    assert np.abs(raw - raw_o).max() < 1e-4 * np.abs(raw_o).max()
+    # normalising the raw file content column by column gives the returned Pi
+    assert np.abs(oracle.norm_prob_matrix(raw) - p.pi()).max() < 1e-4
     ev = np.loadtxt(tmp_path / f"evals{tail}")
     lam = p.lam()
     np.testing.assert_allclose(ev, (1 / lam ** 2) / np.sum(1 / lam ** 2), rtol=1e-12)
