@@ -649,9 +649,10 @@ def run_adjoint(args, ws, rank, local):
     k, a0, nX = wl["k"], wl["alpha0"], graph.parts[0]
     rng = np.random.default_rng(wl["seed"])
     check = {}
+    # the gradient of L with theta = 1 (L = ||T - sum phi^x3||^2 - ||T||^2)
     cfg = mm.default_config(k=k, alpha0=a0, stpm_method=mm.STPM_ADJOINT, sweeps=wl["sweeps"],
                             minibatch=wl["minibatch"], seed=wl["seed"], device=local, tau=0.1,
-                            precision=mm.PREC_BF16)
+                            precision=mm.PREC_BF16, theta=1.0)
     with mm.Pipeline(cfg) as p:
         p.upload(graph).whiten()
         y64 = {n_: np.asarray(v, dtype=np.float64) for n_, v in p.whitened().items()}

@@ -91,7 +91,11 @@ void mmsb_config_default(mmsb_config* cfg) {
   cfg->sweeps = 10;
   cfg->minibatch = 100;
   cfg->lr0 = 1.0;
-  cfg->theta = 1.0;
+  // 1/4: the Phi term's weight 1 - 3 theta beta_t of the online step stays in
+  // [1/4, 1) for beta_t = 1/(1+t); at theta = 1 it is 0 at t = 2, where the
+  // step becomes the bare minibatch gradient, singular whenever the
+  // minibatch's whitened data miss a direction, and its QR factor not unique
+  cfg->theta = 0.25;
   cfg->min_iter = 100;
   cfg->max_iter = 10000;
   cfg->tol = 1e-6;

@@ -125,11 +125,14 @@ __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
 // n + 2 only, after every receiver has waited for broadcast n + 1 (sent by
 // each rank after it received all of broadcast n).
 
-// pivot ratio R_jj^2 / A_jj below which one more exact Cholesky QR pass runs,
-// the floor a non-positive pivot is raised to (relative to A_jj), and the
+// pivot ratio R_jj^2 / A_jj below which one more exact Cholesky QR pass runs
+// (one pass leaves Q1^T Q1 - I of about eps / ratio times a small constant, and
+// the first-order pass squares it), the floor a pivot below FP32 round-off of
+// A_jj is raised to (a column numerically dependent on the ones before it:
+// the floor keeps R^-1 bounded, the next pass orthonormalises), and the
 // largest number of exact passes per step
-constexpr float kQrExactBelow = 1e-3f;
-constexpr float kPivotFloor = 1e-12f;
+constexpr float kQrExactBelow = 1e-2f;
+constexpr float kPivotFloor = 1e-7f;
 constexpr int kQrMaxPasses = 4;
 
 // column stride of the k x k matrices: KP + 4 (== 4 mod 8 for KP a multiple
@@ -266,7 +269,7 @@ enum StepProd : int { kProdGram = 0, kProdTimes = 1 };
 
 template <int KP, int CL, int PROD, typename Epi>
 __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const float* __restrict__ Bm,
-                                           float* __restrict__ part, Epi&& epi) {
+                                           float* part, Epi&& epi) {
   using S = StepSmem<KP, CL>;
   constexpr int XLD = S::XLD;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -319,9 +322,8 @@ __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const fl
 // it and counted as ratio 0.  Returns, in every lane, the smallest ratio
 // R_jj^2 / dg[j] over the live columns j0 + j < k.
 template <int XLD>
-__device__ __forceinline__ float factor_diag16(float* __restrict__ A, int j0, int k,
-                                               float* __restrict__ tb, float* __restrict__ rd,
-                                               const float* __restrict__ dg) {
+__device__ __forceinline__ float factor_diag16(float* A, int j0, int k, float* tb, float* rd,
+                                               const float* dg) {
   const int lane = threadIdx.x & 31, l = lane & 15;
   float a[16];
 #pragma unroll
@@ -371,10 +373,14 @@ __device__ __forceinline__ float factor_diag16(float* __restrict__ A, int j0, in
 
 // Whole CTA.  Returns the smallest pivot ratio (the same value in every
 // thread: every CTA of a cluster factors the same matrix the same way).
+// (No __restrict__ on these shared-memory pointers: other threads write what
+// a thread reads after each barrier, and the ratio decides the control flow
+// of the whole CTA, so no load may be moved across a barrier.  With
+// __restrict__ the compiler did move the read of the ratio above the
+// barrier: warps left the pass loop apart and the kernel hung.)
 template <int KP>
-__device__ float chol_blocked(float* __restrict__ A, int k, float* __restrict__ tinv,
-                              float* __restrict__ rd, float* __restrict__ dg,
-                              float* __restrict__ s_ratio) {
+__device__ float chol_blocked(float* A, int k, float* tinv, float* rd, float* dg,
+                              volatile float* s_ratio) {
   constexpr int XLD = step_xld(KP), NBK = KP / 16;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
   const int nw = blockDim.x >> 5;
@@ -438,8 +444,7 @@ __device__ float chol_blocked(float* __restrict__ A, int k, float* __restrict__ 
 // block back substitution: W_KK = T_KK, W_JK = -T_JJ sum_{L=J+1..K} R_JL W_LK.
 // tmp: 16 * NB floats.  Whole CTA; ends with a barrier.
 template <int KP, int NB>
-__device__ void inverse_columns(const float* __restrict__ R, const float* __restrict__ tinv, int c0,
-                                float* __restrict__ Wb, float* __restrict__ tmp) {
+__device__ void inverse_columns(const float* R, const float* tinv, int c0, float* Wb, float* tmp) {
   constexpr int XLD = step_xld(KP);
   const int tid = threadIdx.x;
   const int K = c0 / 16, co = c0 % 16;
@@ -797,8 +802,11 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     float* t = M;
     M = F;
     F = S::SB ? M : t;
-    if (ratio >= kQrExactBelow || passes >= a.max_passes) {
-      if (ratio < kQrExactBelow && rank == 0 && tid == 0) atomicOr(a.flags, kFlagNoConvergence);
+    // the decision is taken by the whole CTA together (a barrier OR), so
+    // every warp leaves or repeats the loop
+    const bool again = __syncthreads_or(ratio < kQrExactBelow) != 0;
+    if (!again || passes >= a.max_passes) {
+      if (again && rank == 0 && tid == 0) atomicOr(a.flags, kFlagNoConvergence);
       break;
     }
   }

@@ -16,7 +16,7 @@ def test_adjoint_gradient_vs_fp64_finite_differences(mm, oracle):
     k, a0 = 100, 1.0
     g = mm.generate(24_000, k, a0, 0.04, 4e-4, seed=4)
     rng = np.random.default_rng(5)
-    with mm.Pipeline(k=k, alpha0=a0, stpm_method=mm.STPM_ADJOINT) as p:
+    with mm.Pipeline(k=k, alpha0=a0, stpm_method=mm.STPM_ADJOINT, theta=1.0) as p:
         p.upload(g).whiten()
         y = {n: np.asarray(v, np.float64) for n, v in p.whitened().items()}
         phi = oracle.qr_pos(rng.standard_normal((k, k))) + 0.05 * rng.standard_normal((k, k))

@@ -171,7 +171,7 @@ def test_adjoint_loss_and_gradient(mm, oracle, golden_cfg1):
     nodes = np.arange(100, 700)
     L_o = oracle.loss_fwd(phi, y, nodes, g.alpha0, 1.0)
     dL_o = oracle.loss_bwd(phi, y, nodes, g.alpha0, 1.0)
-    with mm.Pipeline(k=g.k, alpha0=g.alpha0) as p:
+    with mm.Pipeline(k=g.k, alpha0=g.alpha0, theta=1.0) as p:
         p.upload(g.graph(mm)).set_whitened(y)
         L = p.loss(phi, 100, 600)
         dL = p.loss_grad(phi, 100, 600)
