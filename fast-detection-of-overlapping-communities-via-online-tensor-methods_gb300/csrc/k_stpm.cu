@@ -150,15 +150,15 @@ struct StepSmem {
   static constexpr int NB = KP / CL, XLD = step_xld(KP), MT = KP / 16, NT = NB / 8;
   static constexpr int TILES = MT * NT, KS = TILES <= 8 ? 2 : 1;  // K split over warps
   static constexpr bool SB = KP > 128;
-  static constexpr int NBK = KP / 16;  // 16-column blocks of the Cholesky factor
+  static constexpr int NBK = KP / 8;  // 8-column blocks of the Cholesky factor
   static constexpr size_t full = (size_t)(SB ? 1 : 2) * KP * XLD;
   static constexpr size_t tiles = (size_t)4 * NB * XLD;  // B block, 2 staging tiles, G block
   static constexpr size_t kpart = KS == 2 ? (size_t)TILES * 128 : 0;
-  static constexpr size_t small = 3 * KP + 3 * NB + 16 * NB + 8;  // mean terms, d-sums, tmp
-  static constexpr size_t tinv = SB ? 0 : (size_t)256 * NBK;      // SB: in the G block's tile
+  static constexpr size_t small = 3 * KP + 3 * NB + 64 + 8;  // mean terms, d-sums, tmp
+  static constexpr size_t tinv = SB ? 0 : (size_t)64 * NBK;  // SB: in the G block's tile
   static constexpr size_t floats = full + tiles - (SB ? NB * XLD : 0) + kpart + small + tinv +
                                    2 * KP;  // original diagonal, 1 / R_jj
-  static_assert(!SB || (size_t)256 * NBK <= (size_t)NB * XLD, "inverse blocks in the G tile");
+  static_assert(!SB || (size_t)64 * NBK <= (size_t)NB * XLD, "inverse blocks in the G tile");
   static_assert(floats * sizeof(float) <= 227 * 1024 - 2048, "step kernel shared memory");
 };
 
@@ -308,31 +308,33 @@ __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const fl
 // ---- Cholesky factor and its inverse on one CTA ----------------------------------
 //
 // A (KP x KP symmetric, column-major, leading dimension XLD, upper triangle
-// read) = R^T R with R upper triangular, blocked by 16 columns (right-looking):
-// a warp factors the diagonal block and inverts it, the block row of R right
-// of it is T_JJ^T A_J,K (T_JJ = R_JJ^-1), and the trailing upper triangle is
-// updated by 3xTF32 tensor-core tiles.  R overwrites A's upper triangle; the
-// inverse diagonal blocks go to tinv (16 x 16 column-major each), 1 / R_jj to
-// rd.  Rows and columns >= k must hold the identity (the caller sets their
-// diagonal to 1; X's padding columns are zero).
+// read) = R^T R with R upper triangular, blocked by 8 columns (right-looking,
+// one block of look-ahead): one thread factors the 8 x 8 diagonal block and
+// inverts it in registers (no shuffles on the pivot chain), every thread
+// forms one column of the block row R_J = T_JJ^T A_J (T_JJ = R_JJ^-1), then
+// warp 0 updates and factors the next diagonal block while the other warps
+// update the rest of the trailing upper triangle.  R overwrites A's upper
+// triangle; the inverse diagonal blocks go to tinv (8 x 8 column-major each),
+// 1 / R_jj to rd.  Rows and columns >= k must hold the identity (the caller
+// sets their diagonal to 1; X's padding columns are zero).
 
-// One warp: the 16 x 16 diagonal block at (j0, j0) (already updated by the
-// blocks above it).  Lane l < 16 holds column l (a[i] = A(j0+i, j0+l)); a
+// One thread: the (already updated) 8 x 8 diagonal block at (j0, j0).  A
 // pivot that is not above kPivotFloor * dg (breakdown, or NaN) is raised to
-// it and counted as ratio 0.  Returns, in every lane, the smallest ratio
-// R_jj^2 / dg[j] over the live columns j0 + j < k.
+// it and counted as ratio 0.  Returns the smallest ratio R_jj^2 / dg[j] over
+// the live columns j0 + j < k.
 template <int XLD>
-__device__ __forceinline__ float factor_diag16(float* A, int j0, int k, float* tb, float* rd,
-                                               const float* dg) {
-  const int lane = threadIdx.x & 31, l = lane & 15;
-  float a[16];
+__device__ __forceinline__ float factor_diag8(float* A, int j0, int k, float* tb, float* rd,
+                                              const float* dg) {
+  float a[8][8];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) a[i] = A[(j0 + i) + (j0 + l) * XLD];
-  float rv[16];
+  for (int l = 0; l < 8; ++l)
+#pragma unroll
+    for (int i = 0; i <= l; ++i) a[i][l] = A[(j0 + i) + (j0 + l) * XLD];
+  float rv[8];
   float rmin = 1.f;
 #pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    float d = __shfl_sync(0xffffffffu, a[j], j);
+  for (int j = 0; j < 8; ++j) {
+    float d = a[j][j];
     const float d0 = dg[j0 + j];
     float ratio = d / d0;
     if (!(d > kPivotFloor * d0)) {
@@ -342,31 +344,36 @@ __device__ __forceinline__ float factor_diag16(float* A, int j0, int k, float* t
     if (j0 + j < k) rmin = fminf(rmin, ratio);
     const float ri = rsqrtf(d);
     rv[j] = ri;
-    const float u = (l == j) ? d * ri : a[j] * ri;  // R(j, l); lane j: sqrt(d)
-    a[j] = u;
+    a[j][j] = d * ri;
 #pragma unroll
-    for (int i = j + 1; i < 16; ++i) {
-      const float rji = __shfl_sync(0xffffffffu, u, i);  // R(j, i)
-      a[i] = fmaf(-rji, u, a[i]);
+    for (int l = j + 1; l < 8; ++l) a[j][l] *= ri;
+#pragma unroll
+    for (int i = j + 1; i < 8; ++i)
+#pragma unroll
+      for (int l = i; l < 8; ++l) a[i][l] = fmaf(-a[j][i], a[j][l], a[i][l]);
+  }
+  // T = R^-1, column by column: T(j, j) = 1 / R_jj,
+  // T(m, j) = -(sum_{m <= i < j} T(m, i) R(i, j)) / R(j, j)
+  float t[8][8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    t[j][j] = rv[j];
+#pragma unroll
+    for (int m = 0; m < j; ++m) {
+      float s = 0.f;
+#pragma unroll
+      for (int i = m; i < j; ++i) s = fmaf(t[m][i], a[i][j], s);
+      t[m][j] = -s * rv[j];
     }
   }
-  // T = R^-1 by rows: lane m < 16 holds t[j] = T(m, j); T(m, j) =
-  // (delta_mj - sum_{i<j} T(m, i) R(i, j)) / R(j, j), zero for j < m
-  float t[16];
 #pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    float s = (l == j) ? 1.f : 0.f;
+  for (int l = 0; l < 8; ++l) {
 #pragma unroll
-    for (int i = 0; i < j; ++i) s = fmaf(-t[i], __shfl_sync(0xffffffffu, a[i], j), s);
-    t[j] = s * rv[j];
-  }
-  if (lane < 16) {
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      if (i <= l) A[(j0 + i) + (j0 + l) * XLD] = a[i];
-      tb[l + 16 * i] = t[i];
-      if (l == i) rd[j0 + i] = rv[i];
+    for (int i = 0; i < 8; ++i) {
+      if (i <= l) A[(j0 + i) + (j0 + l) * XLD] = a[i][l];
+      tb[i + 8 * l] = i <= l ? t[i][l] : 0.f;
     }
+    rd[j0 + l] = rv[l];
   }
   return rmin;
 }
@@ -381,9 +388,8 @@ __device__ __forceinline__ float factor_diag16(float* A, int j0, int k, float* t
 template <int KP>
 __device__ float chol_blocked(float* A, int k, float* tinv, float* rd, float* dg,
                               volatile float* s_ratio) {
-  constexpr int XLD = step_xld(KP), NBK = KP / 16;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
-  const int nw = blockDim.x >> 5;
+  constexpr int XLD = step_xld(KP), NBK = KP / 8;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int i = tid; i < KP; i += blockDim.x) {
     float d = A[i + i * XLD];
     if (i >= k) {
@@ -394,42 +400,63 @@ __device__ float chol_blocked(float* A, int k, float* tinv, float* rd, float* dg
   }
   __syncthreads();
   float rmin = 1.f;
-  for (int J = 0; J < NBK; ++J) {
-    const int j0 = 16 * J;
-    if (warp == 0) rmin = fminf(rmin, factor_diag16<XLD>(A, j0, k, tinv + 256 * J, rd, dg));
-    __syncthreads();
-    const int rest = KP - j0 - 16;
-    if (rest <= 0) break;
-    // block row: R(j0 + a, c) = sum_{b <= a} T(b, a) A(j0 + b, c), c >= j0 + 16
+  if (tid == 0) rmin = factor_diag8<XLD>(A, 0, k, tinv, rd, dg);
+  __syncthreads();
+  for (int J = 0; J + 1 < NBK; ++J) {
+    const int j0 = 8 * J, rest = KP - j0 - 8;
+    // block row: R(j0 + a, c) = sum_{b <= a} T(b, a) A(j0 + b, c), c >= j0 + 8
     // (a thread per column)
-    const float* tb = tinv + 256 * J;
+    const float* tb = tinv + 64 * J;
     for (int e = tid; e < rest; e += blockDim.x) {
-      const int c = j0 + 16 + e;
-      float x[16];
+      const int c = j0 + 8 + e;
+      float x[8];
 #pragma unroll
-      for (int b = 0; b < 16; ++b) x[b] = A[(j0 + b) + c * XLD];
+      for (int b = 0; b < 8; ++b) x[b] = A[(j0 + b) + c * XLD];
 #pragma unroll
-      for (int aa = 15; aa >= 0; --aa) {
+      for (int aa = 7; aa >= 0; --aa) {
         float s = 0.f;
 #pragma unroll
-        for (int b = 0; b <= aa; ++b) s = fmaf(tb[b + 16 * aa], x[b], s);
+        for (int b = 0; b <= aa; ++b) s = fmaf(tb[b + 8 * aa], x[b], s);
         x[aa] = s;  // rows below aa are still the inputs
       }
 #pragma unroll
-      for (int b = 0; b < 16; ++b) A[(j0 + b) + c * XLD] = x[b];
+      for (int b = 0; b < 8; ++b) A[(j0 + b) + c * XLD] = x[b];
     }
     __syncthreads();
-    // trailing update of the upper triangle: A(c, c') -= sum_b R(j0+b, c) R(j0+b, c')
-    const int nm = rest / 16, nn = rest / 8;
-    for (int tl = warp; tl < nm * nn; tl += nw) {
-      const int m0 = j0 + 16 + (tl % nm) * 16, n0 = j0 + 16 + (tl / nm) * 8;
-      if (m0 > n0 + 7) continue;  // entirely below the diagonal
-      float acc[4];
-      warp_tile_3xtf32<XLD, 1, 1, XLD>(A + j0 + m0 * XLD, A + j0 + n0 * XLD, 0, 16, acc);
+    // trailing update of the upper triangle, A(c, c') -= sum_b R(j0+b, c)
+    // R(j0+b, c') for j0 + 8 <= c <= c': warp 0 takes the next diagonal block
+    // and factors it, the other warps the rest
+    const int n0 = j0 + 8;
+    if (warp == 0) {
+      for (int e = lane; e < 64; e += 32) {
+        const int i = e & 7, l = e >> 3;
+        if (i <= l) {
+          float s = A[(n0 + i) + (n0 + l) * XLD];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int r = m0 + g + ((q & 2) ? 8 : 0), c = n0 + 2 * t4 + (q & 1);
-        A[r + c * XLD] -= acc[q];
+          for (int b = 0; b < 8; ++b)
+            s = fmaf(-A[(j0 + b) + (n0 + i) * XLD], A[(j0 + b) + (n0 + l) * XLD], s);
+          A[(n0 + i) + (n0 + l) * XLD] = s;
+        }
+      }
+      __syncwarp();
+      if (lane == 0) rmin = fminf(rmin, factor_diag8<XLD>(A, n0, k, tinv + 64 * (J + 1), rd, dg));
+    } else if (rest > 8) {
+      // column c' (threads of a warp take consecutive columns), rows c of
+      // the upper part outside the next diagonal block, in chunks
+      const int ncol = rest - 8;  // columns c' in [n0 + 8, KP)
+      const int nthr = (int)blockDim.x - 32, t = tid - 32;
+      const int chunks = max(1, nthr / ncol);
+      for (int u = t; u < ncol * chunks; u += nthr) {
+        const int cp = n0 + 8 + u % ncol, ch = u / ncol;
+        float rc[8];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) rc[b] = A[(j0 + b) + cp * XLD];
+        for (int c = n0 + ch; c <= cp; c += chunks) {
+          float s = A[c + cp * XLD];
+#pragma unroll
+          for (int b = 0; b < 8; ++b) s = fmaf(-A[(j0 + b) + c * XLD], rc[b], s);
+          A[c + cp * XLD] = s;
+        }
       }
     }
     __syncthreads();
@@ -439,51 +466,54 @@ __device__ float chol_blocked(float* A, int k, float* tinv, float* rd, float* dg
   return *s_ratio;
 }
 
-// Columns c0 .. c0+NB of W = R^-1 (NB = 8 or 16, inside the 16-block K =
-// c0 / 16) into Wb (column jb at Wb + jb * XLD, rows >= 16 K + 16 zero), by
-// block back substitution: W_KK = T_KK, W_JK = -T_JJ sum_{L=J+1..K} R_JL W_LK.
-// tmp: 16 * NB floats.  Whole CTA; ends with a barrier.
+// Columns c0 .. c0+NB of W = R^-1 (NB = 8 or 16: whole 8-column blocks) into
+// Wb (column jb at Wb + jb * XLD, rows past the diagonal block zero), by
+// block back substitution per 8-column block K: W_KK = T_KK,
+// W_JK = -T_JJ sum_{L=J+1..K} R_JL W_LK.  tmp: 64 floats.  Whole CTA; ends
+// with a barrier.
 template <int KP, int NB>
 __device__ void inverse_columns(const float* R, const float* tinv, int c0, float* Wb, float* tmp) {
   constexpr int XLD = step_xld(KP);
   const int tid = threadIdx.x;
-  const int K = c0 / 16, co = c0 % 16;
   for (int e = tid; e < NB * KP; e += blockDim.x) {
     const int r = e % KP, jb = e / KP;
     Wb[r + jb * XLD] = 0.f;
   }
-  for (int e = tid; e < 16 * NB; e += blockDim.x) {
-    const int aa = e % 16, jb = e / 16;
-    tmp[e] = tinv[256 * K + aa + 16 * (co + jb)];  // W_KK
-  }
-  __syncthreads();
-  for (int L = K;; --L) {
-    // W_LK (in tmp) into place; rows above block L accumulate -R_JL W_LK
-    for (int e = tid; e < 16 * NB; e += blockDim.x) {
-      const int aa = e % 16, jb = e / 16;
-      Wb[16 * L + aa + jb * XLD] = tmp[e];
-    }
-    for (int e = tid; e < 16 * L * NB; e += blockDim.x) {
-      const int r = e % (16 * L), jb = e / (16 * L);
-      float s = 0.f;
-#pragma unroll
-      for (int b = 0; b < 16; ++b) s = fmaf(R[r + (16 * L + b) * XLD], tmp[b + 16 * jb], s);
-      Wb[r + jb * XLD] -= s;
-    }
+#pragma unroll 1
+  for (int sb = 0; sb < NB / 8; ++sb) {
+    const int K = c0 / 8 + sb;
+    float* W = Wb + 8 * sb * XLD;
+    for (int e = tid; e < 64; e += blockDim.x) tmp[e] = tinv[64 * K + e];  // W_KK (col-major)
     __syncthreads();
-    if (L == 0) break;
-    // W_(L-1)K = T_(L-1) (the accumulated rows of block L-1)
-    const float* tb = tinv + 256 * (L - 1);
-    for (int e = tid; e < 16 * NB; e += blockDim.x) {
-      const int aa = e % 16, jb = e / 16;
-      const float* src = Wb + 16 * (L - 1) + jb * XLD;
-      float s = 0.f;
+    for (int L = K;; --L) {
+      // W_LK (tmp, column jb at tmp + 8 jb) into place; rows above block L
+      // accumulate -R_{.,L} W_LK
+      for (int e = tid; e < 64; e += blockDim.x) {
+        const int aa = e & 7, jb = e >> 3;
+        W[8 * L + aa + jb * XLD] = tmp[e];
+      }
+      for (int e = tid; e < 8 * L * 8; e += blockDim.x) {
+        const int r = e % (8 * L), jb = e / (8 * L);
+        float s = 0.f;
 #pragma unroll
-      for (int b = 0; b < 16; ++b)
-        if (b >= aa) s = fmaf(tb[aa + 16 * b], src[b], s);
-      tmp[e] = s;
+        for (int b = 0; b < 8; ++b) s = fmaf(R[r + (8 * L + b) * XLD], tmp[b + 8 * jb], s);
+        W[r + jb * XLD] -= s;
+      }
+      __syncthreads();
+      if (L == 0) break;
+      // W_(L-1)K = T_(L-1) (the accumulated rows of block L-1)
+      const float* tb = tinv + 64 * (L - 1);
+      for (int e = tid; e < 64; e += blockDim.x) {
+        const int aa = e & 7, jb = e >> 3;
+        const float* src = W + 8 * (L - 1) + jb * XLD;
+        float s = 0.f;
+#pragma unroll
+        for (int b = 0; b < 8; ++b)
+          if (b >= aa) s = fmaf(tb[aa + 8 * b], src[b], s);
+        tmp[e] = s;
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
@@ -521,9 +551,9 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   float* part = Gb + NB * XLD;                    // K-split partial tiles
   float* mv = part + S::kpart;                    // m1, m2, m3 of this block
   float* dcol = mv + 3 * KP;                      // 3 * NB d-sums
-  float* tmp = dcol + 3 * NB;                     // 16 * NB (inverse columns)
-  float* tinv = S::SB ? Gb : tmp + 16 * NB + 8;   // 16 x 16 inverse diagonal blocks
-  float* dg = (S::SB ? tmp + 16 * NB + 8 : tinv + 256 * S::NBK);  // original diagonal
+  float* tmp = dcol + 3 * NB;                     // 64 (inverse columns)
+  float* tinv = S::SB ? Gb : tmp + 64 + 8;        // 8 x 8 inverse diagonal blocks
+  float* dg = (S::SB ? tmp + 64 + 8 : tinv + 64 * S::NBK);  // original diagonal
   float* rd = dg + KP;                            // 1 / R_jj
   __shared__ float s_ratio;
   __shared__ float s_emax[16];

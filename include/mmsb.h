@@ -142,8 +142,8 @@ typedef struct mmsb_ctx mmsb_ctx;
 /* Fills the reference's defaults: alpha0 1, binary, batch power with
  * MINITER 100 / MAXITER 10000 / TOLERANCE 1e-6 (CPU/stdafx.h:56-60),
  * pinv tolerance 1e-6, Nystrom factor 20, NORMALIZE on; online schedule
- * 10 sweeps, minibatch 100, beta_t = 1/(1+t), theta 1/4 (the weight
- * 1 - 3 theta beta_t of Phi in the online step then stays in [1/4, 1)). */
+ * 10 sweeps, minibatch 100, beta_t = 1/(1+t), theta 1/2 (the weight
+ * 1 - 3 theta beta_t of Phi in the online step is then never 0). */
 void mmsb_config_default(mmsb_config* cfg);
 
 /* Replaces the reference's globals NX..KHID/alpha0/DATATYPE

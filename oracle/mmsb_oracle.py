@@ -317,7 +317,7 @@ def tensor_values(phi, y, alpha0):
     return np.einsum("ji,ji->i", phi, G)
 
 
-def stpm_online(y, alpha0, phi0, sweeps, minibatch, lr0=1.0, theta=0.25, adjoint=False,
+def stpm_online(y, alpha0, phi0, sweeps, minibatch, lr0=1.0, theta=0.5, adjoint=False,
                 orth="qr"):
     """Minibatch STPM: per step Phi <- qr_pos(Phi - beta_t (3 theta O - 3 G))
     with O = Phi (Phi^T Phi)^.2 (Diff_Loss, Util.cpp:257-284, averaged over
