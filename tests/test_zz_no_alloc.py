@@ -18,7 +18,8 @@ LIMIT = 8 << 20  # bytes of the fixed device array
 
 
 def rel(a, b):
-    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
 def make_block(rng, n_rows, n_cols, density, weighted, used_cols=None):
