@@ -154,7 +154,7 @@ struct StepSmem {
   static constexpr size_t full = (size_t)(SB ? 1 : 2) * KP * XLD;
   static constexpr size_t tiles = (size_t)4 * NB * XLD;  // B block, 2 staging tiles, G block
   static constexpr size_t kpart = KS == 2 ? (size_t)TILES * 128 : 0;
-  static constexpr size_t small = 3 * KP + 3 * NB + 64 + 8;  // mean terms, d-sums, tmp
+  static constexpr size_t small = 3 * KP + 4 * NB + 64 + 8;  // mean terms, d-sums, |phi_i|^2, tmp
   static constexpr size_t tinv = SB ? 0 : (size_t)64 * NBK;  // SB: in the G block's tile
   static constexpr size_t floats = full + tiles - (SB ? NB * XLD : 0) + kpart + small + tinv +
                                    2 * KP;  // original diagonal, 1 / R_jj
@@ -309,13 +309,15 @@ __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const fl
 //
 // A (KP x KP symmetric, column-major, leading dimension XLD, upper triangle
 // read) = R^T R with R upper triangular, blocked by 8 columns (right-looking,
-// one block of look-ahead): one thread factors the 8 x 8 diagonal block and
-// inverts it in registers (no shuffles on the pivot chain), every thread
-// forms one column of the block row R_J = T_JJ^T A_J (T_JJ = R_JJ^-1), then
-// warp 0 updates and factors the next diagonal block while the other warps
-// update the rest of the trailing upper triangle.  R overwrites A's upper
-// triangle; the inverse diagonal blocks go to tinv (8 x 8 column-major each),
-// 1 / R_jj to rd.  Rows and columns >= k must hold the identity (the caller
+// one block of look-ahead).  Per block J: every thread forms one column of
+// the block row R_J = R_JJ^-T A_J by forward substitution; then warp 0
+// updates the next 8 x 8 diagonal block and one thread factors it in
+// registers (no shuffles on the pivot chain), while the other warps update
+// the rest of the trailing upper triangle with 3xTF32 tensor-core tiles
+// (a rank-8 update is one k-step).  R overwrites A's upper triangle, 1 / R_jj
+// goes to rd; the inverses T_JJ = R_JJ^-1 of the diagonal blocks (tinv, 8 x 8
+// column-major each) are formed afterwards, one block per thread, off the
+// pivot chain.  Rows and columns >= k must hold the identity (the caller
 // sets their diagonal to 1; X's padding columns are zero).
 
 // One thread: the (already updated) 8 x 8 diagonal block at (j0, j0).  A
@@ -323,27 +325,25 @@ __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const fl
 // it and counted as ratio 0.  Returns the smallest ratio R_jj^2 / dg[j] over
 // the live columns j0 + j < k.
 template <int XLD>
-__device__ __forceinline__ float factor_diag8(float* A, int j0, int k, float* tb, float* rd,
-                                              const float* dg) {
+__device__ __forceinline__ float factor_diag8(float* A, int j0, int k, float* rd, const float* dg) {
   float a[8][8];
 #pragma unroll
   for (int l = 0; l < 8; ++l)
 #pragma unroll
     for (int i = 0; i <= l; ++i) a[i][l] = A[(j0 + i) + (j0 + l) * XLD];
-  float rv[8];
   float rmin = 1.f;
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     float d = a[j][j];
     const float d0 = dg[j0 + j];
-    float ratio = d / d0;
+    float ratio = __fdividef(d, d0);
     if (!(d > kPivotFloor * d0)) {
       d = kPivotFloor * d0;
       ratio = 0.f;
     }
     if (j0 + j < k) rmin = fminf(rmin, ratio);
     const float ri = rsqrtf(d);
-    rv[j] = ri;
+    rd[j0 + j] = ri;
     a[j][j] = d * ri;
 #pragma unroll
     for (int l = j + 1; l < 8; ++l) a[j][l] *= ri;
@@ -352,30 +352,39 @@ __device__ __forceinline__ float factor_diag8(float* A, int j0, int k, float* tb
 #pragma unroll
       for (int l = i; l < 8; ++l) a[i][l] = fmaf(-a[j][i], a[j][l], a[i][l]);
   }
-  // T = R^-1, column by column: T(j, j) = 1 / R_jj,
-  // T(m, j) = -(sum_{m <= i < j} T(m, i) R(i, j)) / R(j, j)
-  float t[8][8];
+#pragma unroll
+  for (int l = 0; l < 8; ++l)
+#pragma unroll
+    for (int i = 0; i <= l; ++i) A[(j0 + i) + (j0 + l) * XLD] = a[i][l];
+  return rmin;
+}
+
+// One thread: T = R_JJ^-1 (upper, 8 x 8 column-major into tb) of the
+// diagonal block at (j0, j0), column by column: T(j, j) = 1 / R_jj,
+// T(m, j) = -(sum_{m <= i < j} T(m, i) R(i, j)) / R(j, j).
+template <int XLD>
+__device__ __forceinline__ void invert_diag8(const float* A, int j0, const float* rd, float* tb) {
+  float r[8][8], t[8][8];
+#pragma unroll
+  for (int l = 0; l < 8; ++l)
+#pragma unroll
+    for (int i = 0; i < l; ++i) r[i][l] = A[(j0 + i) + (j0 + l) * XLD];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    t[j][j] = rv[j];
+    const float rv = rd[j0 + j];
+    t[j][j] = rv;
 #pragma unroll
     for (int m = 0; m < j; ++m) {
       float s = 0.f;
 #pragma unroll
-      for (int i = m; i < j; ++i) s = fmaf(t[m][i], a[i][j], s);
-      t[m][j] = -s * rv[j];
+      for (int i = m; i < j; ++i) s = fmaf(t[m][i], r[i][j], s);
+      t[m][j] = -s * rv;
     }
   }
 #pragma unroll
-  for (int l = 0; l < 8; ++l) {
+  for (int l = 0; l < 8; ++l)
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      if (i <= l) A[(j0 + i) + (j0 + l) * XLD] = a[i][l];
-      tb[i + 8 * l] = i <= l ? t[i][l] : 0.f;
-    }
-    rd[j0 + l] = rv[l];
-  }
-  return rmin;
+    for (int i = 0; i < 8; ++i) tb[i + 8 * l] = i <= l ? t[i][l] : 0.f;
 }
 
 // Whole CTA.  Returns the smallest pivot ratio (the same value in every
@@ -389,7 +398,8 @@ template <int KP>
 __device__ float chol_blocked(float* A, int k, float* tinv, float* rd, float* dg,
                               volatile float* s_ratio) {
   constexpr int XLD = step_xld(KP), NBK = KP / 8;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
+  const int nw = blockDim.x >> 5;
   for (int i = tid; i < KP; i += blockDim.x) {
     float d = A[i + i * XLD];
     if (i >= k) {
@@ -400,67 +410,67 @@ __device__ float chol_blocked(float* A, int k, float* tinv, float* rd, float* dg
   }
   __syncthreads();
   float rmin = 1.f;
-  if (tid == 0) rmin = factor_diag8<XLD>(A, 0, k, tinv, rd, dg);
+  if (tid == 0) rmin = factor_diag8<XLD>(A, 0, k, rd, dg);
   __syncthreads();
   for (int J = 0; J + 1 < NBK; ++J) {
     const int j0 = 8 * J, rest = KP - j0 - 8;
-    // block row: R(j0 + a, c) = sum_{b <= a} T(b, a) A(j0 + b, c), c >= j0 + 8
-    // (a thread per column)
-    const float* tb = tinv + 64 * J;
+    // block row: R(j0 + a, c) = (A(j0 + a, c) - sum_{b < a} R(j0 + b, j0 + a)
+    // R(j0 + b, c)) / R(j0 + a, j0 + a), c >= j0 + 8 (a thread per column)
     for (int e = tid; e < rest; e += blockDim.x) {
       const int c = j0 + 8 + e;
       float x[8];
 #pragma unroll
       for (int b = 0; b < 8; ++b) x[b] = A[(j0 + b) + c * XLD];
 #pragma unroll
-      for (int aa = 7; aa >= 0; --aa) {
-        float s = 0.f;
+      for (int aa = 0; aa < 8; ++aa) {
+        float s = x[aa];
 #pragma unroll
-        for (int b = 0; b <= aa; ++b) s = fmaf(tb[b + 8 * aa], x[b], s);
-        x[aa] = s;  // rows below aa are still the inputs
+        for (int b = 0; b < aa; ++b) s = fmaf(-A[(j0 + b) + (j0 + aa) * XLD], x[b], s);
+        x[aa] = s * rd[j0 + aa];
       }
 #pragma unroll
       for (int b = 0; b < 8; ++b) A[(j0 + b) + c * XLD] = x[b];
     }
     __syncthreads();
     // trailing update of the upper triangle, A(c, c') -= sum_b R(j0+b, c)
-    // R(j0+b, c') for j0 + 8 <= c <= c': warp 0 takes the next diagonal block
-    // and factors it, the other warps the rest
+    // R(j0+b, c') for j0 + 8 <= c <= c'
     const int n0 = j0 + 8;
     if (warp == 0) {
+      // the next diagonal block, then its factorisation
       for (int e = lane; e < 64; e += 32) {
         const int i = e & 7, l = e >> 3;
         if (i <= l) {
-          float s = A[(n0 + i) + (n0 + l) * XLD];
+          float sv = A[(n0 + i) + (n0 + l) * XLD];
 #pragma unroll
           for (int b = 0; b < 8; ++b)
-            s = fmaf(-A[(j0 + b) + (n0 + i) * XLD], A[(j0 + b) + (n0 + l) * XLD], s);
-          A[(n0 + i) + (n0 + l) * XLD] = s;
+            sv = fmaf(-A[(j0 + b) + (n0 + i) * XLD], A[(j0 + b) + (n0 + l) * XLD], sv);
+          A[(n0 + i) + (n0 + l) * XLD] = sv;
         }
       }
       __syncwarp();
-      if (lane == 0) rmin = fminf(rmin, factor_diag8<XLD>(A, n0, k, tinv + 64 * (J + 1), rd, dg));
+      if (lane == 0) rmin = fminf(rmin, factor_diag8<XLD>(A, n0, k, rd, dg));
     } else if (rest > 8) {
-      // column c' (threads of a warp take consecutive columns), rows c of
-      // the upper part outside the next diagonal block, in chunks
-      const int ncol = rest - 8;  // columns c' in [n0 + 8, KP)
-      const int nthr = (int)blockDim.x - 32, t = tid - 32;
-      const int chunks = max(1, nthr / ncol);
-      for (int u = t; u < ncol * chunks; u += nthr) {
-        const int cp = n0 + 8 + u % ncol, ch = u / ncol;
-        float rc[8];
+      // columns c' >= n0 + 8 in 8-wide tiles, rows c in [n0, c'] in 16-row
+      // tiles from mb; a last tile that would pass KP is computed at KP - 16
+      // (rows below mb not written), so no read leaves the matrix
+      const int mt = (rest + 15) / 16, ntl = (rest - 8) / 8;
+      for (int tl = warp - 1; tl < mt * ntl; tl += nw - 1) {
+        const int mb = n0 + 16 * (tl % mt), nc0 = n0 + 8 + 8 * (tl / mt);
+        if (mb > nc0 + 7) continue;  // entirely below the diagonal
+        const int m0 = min(mb, KP - 16);
+        float acc[4];
+        warp_tile_3xtf32<XLD, 1, 1, XLD>(A + j0 + m0 * XLD, A + j0 + nc0 * XLD, 0, 8, acc);
 #pragma unroll
-        for (int b = 0; b < 8; ++b) rc[b] = A[(j0 + b) + cp * XLD];
-        for (int c = n0 + ch; c <= cp; c += chunks) {
-          float s = A[c + cp * XLD];
-#pragma unroll
-          for (int b = 0; b < 8; ++b) s = fmaf(-A[(j0 + b) + c * XLD], rc[b], s);
-          A[c + cp * XLD] = s;
+        for (int q = 0; q < 4; ++q) {
+          const int r = m0 + g + ((q & 2) ? 8 : 0), c = nc0 + 2 * t4 + (q & 1);
+          if (r >= mb && r <= c) A[r + c * XLD] -= acc[q];
         }
       }
     }
     __syncthreads();
   }
+  // the inverses of the diagonal blocks, one block per thread
+  for (int J = tid; J < NBK; J += blockDim.x) invert_diag8<XLD>(A, 8 * J, rd, tinv + 64 * J);
   if (tid == 0) *s_ratio = rmin;
   __syncthreads();
   return *s_ratio;
@@ -469,48 +479,59 @@ __device__ float chol_blocked(float* A, int k, float* tinv, float* rd, float* dg
 // Columns c0 .. c0+NB of W = R^-1 (NB = 8 or 16: whole 8-column blocks) into
 // Wb (column jb at Wb + jb * XLD, rows past the diagonal block zero), by
 // block back substitution per 8-column block K: W_KK = T_KK,
-// W_JK = -T_JJ sum_{L=J+1..K} R_JL W_LK.  tmp: 64 floats.  Whole CTA; ends
-// with a barrier.
+// W_LK = -T_LL S_L with S_L = sum_{M=L+1..K} R_LM W_MK.  One barrier per
+// level: warp 0 adds the last term of S_(L-1) and applies -T, while the
+// other warps add R_rL W_LK into the partial sums of the rows above (held
+// in Wb until their block's turn).  tmp: 64 floats.  Whole CTA; ends with
+// a barrier.
 template <int KP, int NB>
 __device__ void inverse_columns(const float* R, const float* tinv, int c0, float* Wb, float* tmp) {
   constexpr int XLD = step_xld(KP);
-  const int tid = threadIdx.x;
-  for (int e = tid; e < NB * KP; e += blockDim.x) {
-    const int r = e % KP, jb = e / KP;
-    Wb[r + jb * XLD] = 0.f;
-  }
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int e = tid; e < NB * XLD; e += blockDim.x) Wb[e] = 0.f;
+  __syncthreads();
 #pragma unroll 1
   for (int sb = 0; sb < NB / 8; ++sb) {
     const int K = c0 / 8 + sb;
     float* W = Wb + 8 * sb * XLD;
-    for (int e = tid; e < 64; e += blockDim.x) tmp[e] = tinv[64 * K + e];  // W_KK (col-major)
+    for (int e = tid; e < 64; e += blockDim.x) {
+      const int aa = e & 7, jb = e >> 3;
+      W[8 * K + aa + jb * XLD] = tinv[64 * K + e];  // W_KK = T_KK (column-major)
+    }
     __syncthreads();
-    for (int L = K;; --L) {
-      // W_LK (tmp, column jb at tmp + 8 jb) into place; rows above block L
-      // accumulate -R_{.,L} W_LK
-      for (int e = tid; e < 64; e += blockDim.x) {
-        const int aa = e & 7, jb = e >> 3;
-        W[8 * L + aa + jb * XLD] = tmp[e];
-      }
-      for (int e = tid; e < 8 * L * 8; e += blockDim.x) {
-        const int r = e % (8 * L), jb = e / (8 * L);
-        float s = 0.f;
+    for (int L = K; L >= 1; --L) {
+      const int l0 = 8 * L, p0 = l0 - 8;
+      if (warp == 0) {
+        // S_(L-1) += R_(L-1),L W_LK, then W_(L-1)K = -T_(L-1) S_(L-1)
 #pragma unroll
-        for (int b = 0; b < 8; ++b) s = fmaf(R[r + (8 * L + b) * XLD], tmp[b + 8 * jb], s);
-        W[r + jb * XLD] -= s;
-      }
-      __syncthreads();
-      if (L == 0) break;
-      // W_(L-1)K = T_(L-1) (the accumulated rows of block L-1)
-      const float* tb = tinv + 64 * (L - 1);
-      for (int e = tid; e < 64; e += blockDim.x) {
-        const int aa = e & 7, jb = e >> 3;
-        const float* src = W + 8 * (L - 1) + jb * XLD;
-        float s = 0.f;
+        for (int h = 0; h < 2; ++h) {
+          const int e = lane + 32 * h, aa = e & 7, jb = e >> 3, r = p0 + aa;
+          float sv = W[r + jb * XLD];
 #pragma unroll
-        for (int b = 0; b < 8; ++b)
-          if (b >= aa) s = fmaf(tb[aa + 8 * b], src[b], s);
-        tmp[e] = s;
+          for (int b = 0; b < 8; ++b) sv = fmaf(R[r + (l0 + b) * XLD], W[l0 + b + jb * XLD], sv);
+          tmp[e] = sv;
+        }
+        __syncwarp();
+        const float* tb = tinv + 64 * (L - 1);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int e = lane + 32 * h, aa = e & 7, jb = e >> 3;
+          float w = 0.f;
+#pragma unroll
+          for (int b = 0; b < 8; ++b)
+            if (b >= aa) w = fmaf(tb[aa + 8 * b], tmp[b + 8 * jb], w);
+          W[p0 + aa + jb * XLD] = -w;
+        }
+      } else {
+        // rows above block L-1 accumulate R_rL W_LK
+        const int rows = p0;
+        for (int e = tid - 32; e < rows * 8; e += (int)blockDim.x - 32) {
+          const int r = e % rows, jb = e / rows;
+          float sv = W[r + jb * XLD];
+#pragma unroll
+          for (int b = 0; b < 8; ++b) sv = fmaf(R[r + (l0 + b) * XLD], W[l0 + b + jb * XLD], sv);
+          W[r + jb * XLD] = sv;
+        }
       }
       __syncthreads();
     }
@@ -551,7 +572,8 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   float* part = Gb + NB * XLD;                    // K-split partial tiles
   float* mv = part + S::kpart;                    // m1, m2, m3 of this block
   float* dcol = mv + 3 * KP;                      // 3 * NB d-sums
-  float* tmp = dcol + 3 * NB;                     // 64 (inverse columns)
+  float* nn = dcol + 3 * NB;                      // |phi_i|^2 of this block
+  float* tmp = nn + NB;                           // 64 (inverse columns)
   float* tinv = S::SB ? Gb : tmp + 64 + 8;        // 8 x 8 inverse diagonal blocks
   float* dg = (S::SB ? tmp + 64 + 8 : tinv + 64 * S::NBK);  // original diagonal
   float* rd = dg + KP;                            // 1 / R_jj
@@ -587,17 +609,21 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   if (tid <= 2 * CL) asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   __syncthreads();
   if (a.step_mode == kStepOnline) {
-    // the mean terms phi_i . mu of this block's columns (a warp per dot
-    // product, lanes along the k entries): Phi and mu only, so before the wait
-    for (int e = tid / 32; e < 3 * NB; e += blockDim.x / 32) {
+    // the mean terms phi_i . mu and |phi_i|^2 of this block's columns (a warp
+    // per dot product, lanes along the k entries): Phi and mu only, so
+    // before the wait
+    for (int e = tid / 32; e < 4 * NB; e += blockDim.x / 32) {
       const int which = e / NB, jb = e % NB, i = c0 + jb;
-      const float* mu = which == 0 ? a.mu1 : which == 1 ? a.mu2 : a.mu3;
+      const float* col = Xa + i * XLD;
+      const float* mu = which == 0 ? a.mu1 : which == 1 ? a.mu2 : which == 2 ? a.mu3 : col;
       float sv = 0.f;
       if (i < k && mu)
-        for (int j = lane; j < k; j += 32) sv = fmaf(Xa[i * XLD + j], mu[j], sv);
+        for (int j = lane; j < k; j += 32) sv = fmaf(col[j], mu[j], sv);
 #pragma unroll
       for (int off = 16; off; off >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, off);
-      if (lane == 0) mv[which * KP + jb] = sv;
+      if (lane == 0) {
+        if (which < 3) mv[which * KP + jb] = sv; else nn[jb] = sv;
+      }
     }
   }
   cluster.sync();  // Phi read and barriers initialised everywhere before any copy
@@ -758,24 +784,39 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       Gb[jb * XLD + j] = gval;
     }
     // X = Phi - beta (3 theta Phi (Phi^T Phi)^.2 - gscale G)   (Util.cpp:259-272)
-    step_tiles<KP, CL, kProdGram>(M, M + c0 * XLD, part, [&](const float (&acc)[4], int m0, int n0) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int i = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1);
-        Ab[jb * XLD + i] = acc[q] * acc[q];
-      }
-    });
-    __syncthreads();
-    float* Otc = stage_next();
+    float* Otc;
     const float alpha = -a.beta * a.theta3, gamma = a.beta * a.gscale;
-    step_tiles<KP, CL, kProdTimes>(M, Ab, part, [&](const float (&acc)[4], int m0, int n0) {
+    if (a.phi_general) {
+      // the literal product (first step of a run: Phi0 need not be orthonormal)
+      step_tiles<KP, CL, kProdGram>(M, M + c0 * XLD, part, [&](const float (&acc)[4], int m0, int n0) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int r = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
-        const float v = alpha * acc[q] + M[col * XLD + r] + gamma * Gb[jb * XLD + r];
-        Otc[jb * XLD + r] = (r < k && col < k) ? v : 0.f;
+        for (int q = 0; q < 4; ++q) {
+          const int i = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1);
+          Ab[jb * XLD + i] = acc[q] * acc[q];
+        }
+      });
+      __syncthreads();
+      Otc = stage_next();
+      step_tiles<KP, CL, kProdTimes>(M, Ab, part, [&](const float (&acc)[4], int m0, int n0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int r = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
+          const float v = alpha * acc[q] + M[col * XLD + r] + gamma * Gb[jb * XLD + r];
+          Otc[jb * XLD + r] = (r < k && col < k) ? v : 0.f;
+        }
+      });
+    } else {
+      // Phi is the previous step's Q: Phi^T Phi = I to ~1e-7, so
+      // (Phi^T Phi)^.2 = diag(|phi_i|^4) + O(1e-14) and Phi times it is
+      // phi_i |phi_i|^4, column by column
+      __syncthreads();
+      Otc = stage_next();
+      for (int e = tid; e < NB * XLD; e += blockDim.x) {
+        const int r = e % XLD, jb = e / XLD, col = c0 + jb;
+        const float n2 = nn[jb] * nn[jb];
+        Otc[e] = (r < k && col < k) ? M[col * XLD + r] * (1.f + alpha * n2) + gamma * Gb[e] : 0.f;
       }
-    });
+    }
     broadcast(Otc, F, S::SB);
     if (!wait_buf(F)) timed_out = true;
     float* t = M;

@@ -81,6 +81,10 @@ struct StpmUpdateArgs {
   float* xstash;         // KP x KP scratch in global memory (KP > 128 only)
   long long wait_limit;  // clock64 cycles a bounded wait may take (0: about one second)
   int active;            // batched launches: 0 = no update for this graph in this round
+  // online steps: 1 = form Phi (Phi^T Phi)^.2 literally (the first step of a
+  // run, whose Phi0 need not be orthonormal); 0 = Phi is the previous step's
+  // Q (orthonormal to ~1e-7), so the diagonal of (Phi^T Phi)^.2 suffices
+  int phi_general;
   // convergence trace (may be null): CTA q writes sum over its columns of
   // (Phi_new - trace_snap)^2 to trace_out[q] and sets trace_snap = Phi_new there
   float* trace_snap;

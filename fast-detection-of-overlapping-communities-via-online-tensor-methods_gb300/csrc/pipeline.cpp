@@ -688,6 +688,7 @@ StpmUpdateArgs stpm_online_update_args(mmsb_ctx* c, const OnlineRound& rd, float
   u.count = (double)rd.cnt;
   u.beta = (float)rd.beta;
   u.gscale = (float)rd.gscale;
+  u.phi_general = rd.r == 0 ? 1 : 0;
   return u;
 }
 
@@ -702,6 +703,7 @@ bool stpm_online_round(const mmsb_ctx* c, int64_t r, OnlineRound* out) {
   const double a0 = c->cfg.alpha0;
   const double p0 = (a0 + 1.0) * (a0 + 2.0) / 2.0, p1 = a0 * a0, p2 = -a0 * (a0 + 1.0) / 2.0;
   const int64_t sw = r / per;
+  out->r = r;
   out->x0 = (r % per) * b;
   out->cnt = std::min<int64_t>(b, nx - out->x0);
   out->beta = c->cfg.lr0 / (1.0 + (double)r);

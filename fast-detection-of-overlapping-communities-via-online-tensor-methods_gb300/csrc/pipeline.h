@@ -34,6 +34,7 @@ void pipeline_post_raw(mmsb_ctx* c, double lambda_norm, float* out);
 // pieces of the online / adjoint STPM shared with the batched solver
 struct OnlineRound {
   int mode;                    // kModePlain (online) or kModeAdjoint
+  int64_t r;                   // update index within the run
   int64_t x0, cnt;             // minibatch nodes
   double beta;                 // step size lr0 / (1 + r)
   bool bf16;                   // BF16 contraction (BF16 form, all sweeps but the last)

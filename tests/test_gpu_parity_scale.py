@@ -10,12 +10,29 @@ perturbed by 1e-6 relative noise, and max_i |T(I,phi_i,phi_i) - lambda_i
 phi_i| / max lambda is still ~0.3 after 20 (or 60) sweeps.  So the stages
 are compared where they are determined by the data:
   W (whitening, full size)       rel 1e-4 after the best orthogonal alignment
-  one sweep of 16,384-node       lambda, Phi rel 1e-4 up to column permutation
-  minibatches (4 QR steps; the   and sign, Pi abs 1e-3, community sets
-  oracle's 1e-6-noise response   identical away from tau -- on the device's
-  there is ~1e-5)                whitened data, and end to end from the
-                                 oracle's whitening (the method is equivariant
-                                 under W -> W R for orthogonal R, QR included)
+  one sweep of 16,384-node       on the device's whitened data: lambda, Phi
+  minibatches (4 QR steps; the   rel 1e-4 up to column permutation and sign;
+  oracle's 1e-6-noise response   Pi abs 1e-3 and community sets identical
+  there is ~1e-5 in Phi)         away from tau against the oracle's
+                                 post-processing of the device's lambda and
+                                 Phi, on the nodes whose Pi row the oracle
+                                 itself determines (its response to the 1e-6
+                                 noise below 1e-3: normProb's sign rule flips
+                                 rows whose positive and negative parts nearly
+                                 cancel; 24 of 200,000 here)
+  the same, end to end from the  lambda rel 1e-4 against the oracle's own
+  oracle's whitening (the method pipeline; Phi rel 1e-4 against the oracle
+  is equivariant under W -> W R  STPM on the device's y rotated into the
+  for orthogonal R, QR included) oracle's frame, and within 3 x that run's
+                                 distance from the oracle pipeline plus 1e-4
+                                 (the whitening difference, 1e-5, moves Phi by
+                                 ~20x that); every node's Pi row within 3 x
+                                 the same run's change of the row plus 1e-3,
+                                 except the ~2% of nodes whose raw row's
+                                 positive and negative parts are within 1% of
+                                 each other (normProb's sign rule flips them;
+                                 Pi rows are far more sensitive than Phi: at
+                                 1e-6 noise 38% of them move by > 1e-4)
   the full 20-sweep schedule     within 3 x the oracle's own response to 1e-6
                                  relative noise in y, plus 1e-4
 Reference: CPU/Util.cpp:38-127 (whitening), CPU/CommunityDetection.cpp:66-139,
@@ -75,17 +92,17 @@ def scale_case(mm, oracle):
                 **out)
 
 
-def _oracle(oracle, case, wh, y, phi0, sched, noise=None):
+def _oracle(oracle, case, wh, y, phi0, sched, noise=None, size=1e-6):
     a0 = WL["alpha0"]
     Gxa, Gba, Gca = case["blocks"]
     if noise:
         r = np.random.default_rng(noise)
-        y = {n: (v * (1 + 1e-6 * r.standard_normal(v.shape)) if n in ("Da", "Db", "Dc") else v)
+        y = {n: (v * (1 + size * r.standard_normal(v.shape)) if n in ("Da", "Db", "Dc") else v)
              for n, v in y.items()}
     lam, phi, steps = oracle.stpm_online(y, a0, phi0, sweeps=sched["sweeps"],
                                          minibatch=sched["minibatch"])
-    _, pi = oracle.postprocess(Gxa, Gba, Gca, wh, lam, phi)
-    return lam, phi, pi, steps
+    raw, pi = oracle.postprocess(Gxa, Gba, Gca, wh, lam, phi)
+    return lam, phi, pi, steps, raw
 
 
 def _errors(ref, lam, phi, pi, rot=None):
@@ -96,16 +113,23 @@ def _errors(ref, lam, phi, pi, rot=None):
                 pi=float(np.abs(pi[perm].astype(np.float64) - pi_o).max()), perm=perm)
 
 
-def _assert_close(case, ref, res, rot=None):
+def _determined_nodes(ref, pert, max_excluded):
+    """Nodes whose Pi row moves by less than 1e-3 when the oracle's own input
+    is perturbed (pert: the perturbed oracle run)."""
+    _, perm = match_columns(ref[1], pert[1])
+    moved = np.abs(pert[2][perm].astype(np.float64) - ref[2]).max(axis=0)
+    keep = moved < 1e-3
+    assert (~keep).sum() <= max_excluded, (~keep).sum()
+    return keep
+
+
+def _assert_stpm_close(ref, res, rot=None, phi_tol=1e-4):
     k = WL["k"]
     phi = res["phi"] if rot is None else rot @ res["phi"]
     assert np.abs(phi.T @ phi - np.eye(k)).max() < 1e-5
     e = _errors(ref, res["lam"], res["phi"], res["pi"], rot)
-    assert e["phi"] < 1e-4 and e["lam"] < 1e-4, e
-    assert e["pi"] < 1e-3, e
-    pi_o = ref[2]
-    away = np.abs(pi_o - TAU) > 2e-3
-    assert np.array_equal(res["sets"][e["perm"]][away], (pi_o > TAU)[away])
+    assert e["phi"] < phi_tol and e["lam"] < 1e-4, e
+    return e
 
 
 def test_scale_whitening_matches_oracle(scale_case):
@@ -122,8 +146,17 @@ def test_scale_stpm_and_post_match_oracle_on_device_whitening(oracle, scale_case
     post-processing on the device's whitened data and whitening, same Phi0."""
     c = scale_case
     ref = _oracle(oracle, c, c["wh_d"], c["y_d"], c["phi0"], SHORT)
-    assert c["short"]["stats"]["stpm_steps"] == ref[3]
-    _assert_close(c, ref, c["short"])
+    pert = _oracle(oracle, c, c["wh_d"], c["y_d"], c["phi0"], SHORT, noise=1)
+    keep = _determined_nodes(ref, pert, max_excluded=100)
+    res = c["short"]
+    assert res["stats"]["stpm_steps"] == ref[3]
+    _assert_stpm_close(ref, res)
+    # post-processing of the device's own lambda and Phi
+    Gxa, Gba, Gca = c["blocks"]
+    _, pi_o = oracle.postprocess(Gxa, Gba, Gca, c["wh_d"], res["lam"], res["phi"])
+    assert np.abs(res["pi"].astype(np.float64) - pi_o)[:, keep].max() < 1e-3
+    away = (np.abs(pi_o - TAU) > 2e-3) & keep[None, :]
+    assert np.array_equal(res["sets"][away], (pi_o > TAU)[away])
 
 
 def test_scale_end_to_end_matches_oracle(oracle, scale_case):
@@ -131,8 +164,29 @@ def test_scale_end_to_end_matches_oracle(oracle, scale_case):
     device pipeline started from the rotated Phi0 (four steps)."""
     c = scale_case
     U, _, Vt = np.linalg.svd(c["wh_o"]["W"].T @ c["wh_d"]["W"])
+    rot = U @ Vt
     ref = _oracle(oracle, c, c["wh_o"], c["y_o"], c["phi0"], SHORT)
-    _assert_close(c, ref, c["short_e2e"], rot=U @ Vt)
+    # the oracle's STPM on the device's whitened data in the oracle's frame
+    y_rot = {n: rot @ v for n, v in c["y_d"].items()}
+    alt = _oracle(oracle, c, c["wh_o"], y_rot, c["phi0"], SHORT)
+    resp = _errors(ref, *alt[:3])
+    res = c["short_e2e"]
+    same = _errors(alt, res["lam"], res["phi"], res["pi"], rot)
+    print("whitening difference moves the oracle by", {q: v for q, v in resp.items() if q != "perm"},
+          "device vs oracle on the same data:", same["phi"], same["lam"])
+    assert same["phi"] < 1e-4 and same["lam"] < 1e-4, same
+    e = _assert_stpm_close(ref, res, rot=rot, phi_tol=3 * resp["phi"] + 1e-4)
+    pi_o = ref[2]
+    moved = np.abs(alt[2][resp["perm"]].astype(np.float64) - pi_o).max(axis=0)
+    dev = np.abs(res["pi"][e["perm"]].astype(np.float64) - pi_o).max(axis=0)
+    # nodes near normProb's sign decision (positive and negative parts of
+    # the raw row within 1% of each other) flip under a 1e-3 change of Phi
+    raw = ref[4]
+    pos = np.where(raw > 0, raw, 0.0).sum(axis=0)
+    neg = -np.where(raw > 0, 0.0, raw).sum(axis=0)
+    keep = np.abs(pos - neg) >= 1e-2 * (pos + neg)
+    assert (~keep).sum() <= 0.03 * keep.size, (~keep).sum()
+    assert np.all((dev <= 3 * moved + 1e-3)[keep]), (dev - 3 * moved)[keep].max()
 
 
 def test_scale_full_schedule_within_oracle_noise(oracle, scale_case):
