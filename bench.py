@@ -550,11 +550,15 @@ def run_precision(args, ws, rank, local):
         with mm.Pipeline(cfg) as p:
             p.upload(graph)
             runs = []
+            sp_ms = sp_by = 0.0
             for rep in range(1 + max(1, args.steps)):
                 p.flush_l2()
                 p.synchronize()
                 p.whiten()
                 w_ms = p.stats()["whiten_ms"]
+                if rep > 0:
+                    sp_ms += p.stats()["spmm_ms"]
+                    sp_by += p.stats()["spmm_bytes"]
                 p.stpm(phi0)
                 s_ms = p.stats()["stpm_ms"]
                 p.postproc()
@@ -566,7 +570,8 @@ def run_precision(args, ws, rank, local):
                            "ms_per_step": step,
                            "stages_ms": {"whiten_ms": statistics.median(r[0] for r in runs),
                                          "stpm_ms": statistics.median(r[1] for r in runs),
-                                         "post_ms": statistics.median(r[2] for r in runs)}}
+                                         "post_ms": statistics.median(r[2] for r in runs)},
+                           "whitening_spmm_gbs": sp_by / max(sp_ms, 1e-9) / 1e6}
             res[name] = (np.asarray(p.lam(), np.float64), np.asarray(p.phi(), np.float64), p.pi())
             if y64 is None:
                 y64 = {n_: np.asarray(v, dtype=np.float64) for n_, v in p.whitened().items()}
@@ -623,6 +628,53 @@ def run_precision(args, ws, rank, local):
                            "Phi0; eigen_residual = max_i |T(I,phi_i,phi_i) - lambda_i phi_i| / "
                            "max_j lambda_j over all of X"},
     }
+    print(json.dumps(line), flush=True)
+
+
+# the whitening SpMM where its panel cannot stay in L2: n_X = 500,000, 2k = 400
+# panel columns (a 400-float row gathered per nonzero from an 800 MB panel)
+SPMM = dict(name="mmsb-spmm-n2m-k200", n=2_000_000, k=200, alpha0=0.5, p_in=0.005, p_out=1e-6,
+            sweeps=1, minibatch=65536, seed=0)
+
+
+def run_spmm(args, ws, rank, local):
+    """The whitening's CSR SpMM launches (spmm_rows_kernel) on a graph whose
+    2k-wide panels are far larger than L2: one untimed whitening, then
+    `steps` whitenings; GB/s = the launches' algorithmic bytes (CSR, one
+    panel-row gather per nonzero, output) / their CUDA-event time."""
+    if rank != 0:
+        return
+    mm = load_pkg()
+    wl = dict(SPMM)
+    graph = make_graph(mm, wl)
+    cfg = mm.default_config(k=wl["k"], alpha0=wl["alpha0"], stpm_method=mm.STPM_ONLINE,
+                            sweeps=wl["sweeps"], minibatch=wl["minibatch"], seed=wl["seed"],
+                            device=local)
+    ms = by = 0.0
+    launches = 0
+    with mm.Pipeline(cfg) as p:
+        p.upload(graph)
+        p.whiten()
+        for _ in range(max(1, args.steps)):
+            p.flush_l2()
+            p.whiten()
+            st = p.stats()
+            ms += st["spmm_ms"]
+            by += st["spmm_bytes"]
+            launches += st["spmm_launches"]
+    pk = peaks()
+    gbs = by / max(ms, 1e-9) / 1e6
+    line = {"metric": "whitening_spmm_gbs", "value": gbs, "unit": "GB/s", "n_gpus": 1,
+            "steps": max(1, args.steps), "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": wl["name"], **{k_: v for k_, v in wl.items() if k_ != "name"},
+                       "nnz_directed": int(sum(b.nnz for b in graph.blocks[:3]) * 2),
+                       "panel_columns": 2 * wl["k"]},
+            "spmm_launches_per_whitening": launches / max(1, args.steps),
+            "spmm_ms_per_whitening": ms / max(1, args.steps),
+            "roofline": {"kernel": "spmm_rows_kernel", "bound": "hbm", "achieved": gbs,
+                         "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": gbs / pk["hbm_gbs"],
+                         "peak_source": pk["source"]}}
     print(json.dumps(line), flush=True)
 
 
@@ -802,6 +854,8 @@ def main():
     ap.add_argument("--adjoint", action="store_true",
                     help="the differentiation configuration (n = 500k, k = 100: gradient check "
                          "against FP64 finite differences, BF16 adjoint solve)")
+    ap.add_argument("--spmm", action="store_true",
+                    help="the whitening SpMM on panels larger than L2 (n = 2M, 2k = 400)")
     ap.add_argument("--io", action="store_true",
                     help="the file contract: COO text parse/write and binary CSR on the default graph")
     args = ap.parse_args()
@@ -815,6 +869,9 @@ def main():
         return
     if args.io and args.impl != "reference":
         run_io(args, ws, rank)
+        return
+    if args.spmm and args.impl != "reference":
+        run_spmm(args, ws, rank, local)
         return
     if args.precision and args.impl != "reference":
         run_precision(args, ws, rank, local)

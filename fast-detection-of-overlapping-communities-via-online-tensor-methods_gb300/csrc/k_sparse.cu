@@ -6,6 +6,7 @@
 // every panel row is gathered as 16-byte vectors.  One group of G lanes owns
 // one output row; each lane keeps up to two float4 accumulators, and four
 // nonzeros are in flight per lane to cover gather latency.
+#include <cstdlib>
 #include "common.cuh"
 
 #include <cfloat>
@@ -286,8 +287,14 @@ cudaError_t spmm_f32(const int64_t* rp, const int32_t* ci, const float* val, int
   const int c4 = ld / 4;
   // a panel far larger than L2 (129 MB): column slices of <= 64 MB, one pass
   // over the CSR each, so that every slice's gathered rows stay L2-resident
-  if (p_rows > 0 && (double)p_rows * ld * sizeof(float) > 96e6) {
-    int w4 = (int)std::min<int64_t>(c4, std::max<int64_t>(8, (int64_t)(64e6 / (16.0 * p_rows))));
+  // MMSB_SPMM_SLICE_MB overrides the 64 MB slice (a tuning override)
+  static const double slice = []() {
+    const char* e = std::getenv("MMSB_SPMM_SLICE_MB");
+    const double v = e ? std::strtod(e, nullptr) : 0.0;
+    return v >= 1.0 ? v * 1e6 : 64e6;
+  }();
+  if (p_rows > 0 && (double)p_rows * ld * sizeof(float) > 1.5 * slice) {
+    int w4 = (int)std::min<int64_t>(c4, std::max<int64_t>(8, (int64_t)(slice / (16.0 * p_rows))));
     w4 = std::max(8, w4 / 8 * 8);
     for (int cb = 0; cb < c4; cb += w4) {
       const int ce = std::min(c4, cb + w4);
