@@ -108,9 +108,16 @@ __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
 // reference forms.  When a pivot of the Cholesky shows that X's columns are
 // far from independent (R_jj^2 / A_jj below kQrExactBelow; the loss of
 // orthogonality of one pass grows like eps / that ratio), further exact
-// Cholesky QR passes run on Q1 before the first-order step.  Every CTA of
-// the cluster computes the same Cholesky from the same data, so the pass
-// count needs no vote.
+// Cholesky QR passes run on Q1 before the first-order step.  When a pivot
+// has lost (nearly) all its digits (ratio below kShiftBelow: the FP32 Gram
+// squares cond(X), which reaches 1e4 - 2e5 in the first sweep of the
+// benchmarked workloads, beyond 1 / sqrt(eps)), the Gram is formed again
+// and factored with a diagonal shift s = kShiftScale trace(A) (shifted
+// Cholesky QR, Fukaya et al., SIAM J. Sci. Comput. 42 (2020)): A + s I is
+// safely positive definite, Q1 = X R_s^-1 has cond ~ sqrt(s) / sigma_min, and
+// the plain passes that follow orthonormalise it.  Every CTA of the cluster
+// computes the same Cholesky from the same data, so the pass count needs no
+// vote.
 //
 // Layout: every CTA holds whole k x k matrices (column-major, leading
 // dimension KP + 4) and owns NB = 8 or 16 columns.  The products
@@ -134,6 +141,12 @@ __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
 constexpr float kQrExactBelow = 1e-2f;
 constexpr float kPivotFloor = 1e-7f;
 constexpr int kQrMaxPasses = 4;
+// shifted restarts: below this pivot ratio the factorisation is redone with
+// the shift kShiftScale trace(A) (times 100 for each further restart, at
+// most kMaxShifts)
+constexpr float kShiftBelow = 1e-5f;
+constexpr float kShiftScale = 1e-5f;
+constexpr int kMaxShifts = 3;
 
 // column stride of the k x k matrices: KP + 4 (== 4 mod 8 for KP a multiple
 // of 16) makes the fragment loads of the Gram product conflict-free
@@ -396,16 +409,14 @@ __device__ __forceinline__ void invert_diag8(const float* A, int j0, const float
 // barrier: warps left the pass loop apart and the kernel hung.)
 template <int KP>
 __device__ float chol_blocked(float* A, int k, float* tinv, float* rd, float* dg,
-                              volatile float* s_ratio) {
+                              volatile float* s_ratio, float shift = 0.f) {
   constexpr int XLD = step_xld(KP), NBK = KP / 8;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
   const int nw = blockDim.x >> 5;
   for (int i = tid; i < KP; i += blockDim.x) {
-    float d = A[i + i * XLD];
-    if (i >= k) {
-      d = 1.f;
-      A[i + i * XLD] = 1.f;
-    }
+    float d = A[i + i * XLD] + shift;
+    if (i >= k) d = 1.f;
+    A[i + i * XLD] = d;
     dg[i] = fmaxf(d, 1e-30f);
   }
   __syncthreads();
@@ -827,7 +838,19 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   // columns of R^-1 this CTA needs (computed by every CTA from the same A),
   // M R^-1 gathered into F, which becomes M.  (SB: M is kept in global
   // memory while its buffer holds A.)
-  int passes = 0;
+  int passes = 0, shifts = 0, plain_left = a.max_passes;
+  float shift = 0.f;
+  bool resync = false;  // a rank may still be factoring the last Gram in F
+  __shared__ float s_shift;
+  // SB: the buffer (R, read by no one now) gets M back from the stash
+  // (written before the barrier of the last broadcast)
+  auto restore_m = [&]() {
+    for (int e = tid; e < KP * KP; e += blockDim.x) {
+      const int r = e % KP, c = e / KP;
+      M[c * XLD + r] = __ldcg(a.xstash + (int64_t)c * KP + r);
+    }
+    __syncthreads();
+  };
   while (!timed_out) {
     float* Otc = stage_next();
     gram_stage(M, Otc);
@@ -838,23 +861,30 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
         a.xstash[(int64_t)(c0 + jb) * KP + r] = M[(c0 + jb) * XLD + r];
       }
     }
-    broadcast(Otc, F, S::SB);
+    broadcast(Otc, F, S::SB || resync);
+    resync = false;
     if (!wait_buf(F)) {
       timed_out = true;
       break;
     }
-    const float ratio = chol_blocked<KP>(F, k, tinv, rd, dg, &s_ratio);
-    inverse_columns<KP, NB>(F, tinv, c0, Ab, tmp);
-    ++passes;
-    if (S::SB) {
-      // the buffer (R, read by no one now) gets M back from the stash
-      // (written before the barrier of the last broadcast)
-      for (int e = tid; e < KP * KP; e += blockDim.x) {
-        const int r = e % KP, c = e / KP;
-        M[c * XLD + r] = __ldcg(a.xstash + (int64_t)c * KP + r);
+    const float ratio = chol_blocked<KP>(F, k, tinv, rd, dg, &s_ratio, shift);
+    if (__syncthreads_or(ratio < kShiftBelow) && shifts < kMaxShifts) {
+      // near breakdown: the Gram again, factored with a diagonal shift
+      if (tid == 0) {
+        float tr = 0.f;
+        for (int i = 0; i < k; ++i) tr += dg[i];
+        s_shift = shift > 0.f ? 100.f * shift : kShiftScale * tr;
       }
       __syncthreads();
+      shift = s_shift;
+      ++shifts;
+      if (S::SB) restore_m();
+      resync = true;
+      continue;
     }
+    inverse_columns<KP, NB>(F, tinv, c0, Ab, tmp);
+    ++passes;
+    if (S::SB) restore_m();
     Otc = stage_next();
     step_tiles<KP, CL, kProdTimes>(M, Ab, part, [&](const float (&acc)[4], int m0, int n0) {
 #pragma unroll
@@ -873,10 +903,18 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     float* t = M;
     M = F;
     F = S::SB ? M : t;
+    if (shift > 0.f) {
+      // Q1 of a shifted factor is well conditioned, not orthonormal: plain
+      // passes follow
+      shift = 0.f;
+      plain_left = a.max_passes;
+      continue;
+    }
+    --plain_left;
     // the decision is taken by the whole CTA together (a barrier OR), so
     // every warp leaves or repeats the loop
     const bool again = __syncthreads_or(ratio < kQrExactBelow) != 0;
-    if (!again || passes >= a.max_passes) {
+    if (!again || plain_left <= 0) {
       if (again && rank == 0 && tid == 0) atomicOr(a.flags, kFlagNoConvergence);
       break;
     }
