@@ -234,9 +234,12 @@ __global__ void __launch_bounds__(1024) chol_upper_kernel(int p, const double* _
     }
     __syncthreads();
     const double r = rjj;
+    // one FP64 division per pivot (the FP64 pipe is ~2 operations per clock
+    // per SM here), then multiplications
+    const double ri = r > 0.0 ? 1.0 / r : 0.0;
     for (int l = j + 1 + tid; l < p; l += nt) {
       double* x = &R[(int64_t)l * p + j];
-      const double v = r > 0.0 ? *x / r : 0.0;
+      const double v = *x * ri;
       *x = v;
       rowj[l] = v;
     }
@@ -281,6 +284,7 @@ __global__ void __launch_bounds__(256, 1) chol_upper_cluster_kernel(int p, const
   T* Rl = chs;                                   // Rl[lc p + i]
   T* BR = Rl + (size_t)ncl * p;                  // row block: BR[c p + i] = R[jb + c, i]
   __shared__ T DJ[KB * KB];                 // DJ[cc KB + c] = R[jb + c, jb + cc]
+  __shared__ T DI[KB];                      // 1 / R[jb + c, jb + c] (0 where dropped)
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   for (int e = tid; e < ncl * p; e += nt) {
     const int lc = e / p, i = e % p, l = lc * CL + rank;
@@ -310,13 +314,11 @@ __global__ void __launch_bounds__(256, 1) chol_upper_cluster_kernel(int p, const
             atomicOr(flags, kFlagNonFinite);
           }
           DJ[c * KB + c] = r;
+          DI[c] = r > (T)0 ? (T)1 / r : (T)0;  // one division per pivot
         }
         __syncwarp();
-        const T r = DJ[c * KB + c];
-        for (int cc = c + 1 + lane; cc < bs; cc += 32) {
-          const T x = DJ[cc * KB + c];
-          DJ[cc * KB + c] = r > (T)0 ? x / r : (T)0;
-        }
+        const T ri = DI[c];
+        for (int cc = c + 1 + lane; cc < bs; cc += 32) DJ[cc * KB + c] *= ri;
         __syncwarp();
         for (int e = lane; e < KB * KB; e += 32) {
           const int i = e % KB, cc = e / KB;
@@ -336,8 +338,7 @@ __global__ void __launch_bounds__(256, 1) chol_upper_cluster_kernel(int p, const
       for (int c = 0; c < bs; ++c) {
         T x = col[c];
         for (int c2 = 0; c2 < c; ++c2) x = fma(-DJ[c * KB + c2], col[c2], x);
-        const T r = DJ[c * KB + c];
-        col[c] = r > (T)0 ? x / r : (T)0;
+        col[c] = x * DI[c];
       }
     }
     // every CTA has gathered S_JJ and row block J is complete everywhere;
@@ -391,19 +392,27 @@ __global__ void __launch_bounds__(256) trinv_upper_kernel(int p, const double* _
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int j = blockIdx.x * (blockDim.x >> 5) + w;
   if (j >= p) return;
-  double b[kSlots];
+  double b[kSlots], rinv[kSlots];
+  // 1 / R_ll of the rows this lane holds, all divisions issued together (the
+  // FP64 pipe is ~2 operations per clock per SM): the back substitution's
+  // dependent chain then has multiplications only
 #pragma unroll
-  for (int q = 0; q < kSlots; ++q) b[q] = (lane + 32 * q == j) ? 1.0 : 0.0;
+  for (int q = 0; q < kSlots; ++q) {
+    const int i = lane + 32 * q;
+    b[q] = i == j ? 1.0 : 0.0;
+    const double rii = i <= j ? R[(int64_t)i * p + i] : 0.0;
+    rinv[q] = rii != 0.0 ? 1.0 / rii : 0.0;
+  }
   for (int l = j; l >= 0; --l) {
     const int ql = l >> 5, ll = l & 31;
-    double bl = 0.0;
+    double bl = 0.0, il = 0.0;
 #pragma unroll
     for (int q = 0; q < kSlots; ++q)
-      if (q == ql) bl = b[q];
+      if (q == ql) bl = b[q], il = rinv[q];
     bl = __shfl_sync(0xffffffffu, bl, ll);
+    il = __shfl_sync(0xffffffffu, il, ll);
     const double* rc = R + (int64_t)l * p;
-    const double rll = rc[l];
-    const double tl = rll != 0.0 ? bl / rll : 0.0;
+    const double tl = bl * il;
     // only slots holding rows i <= l take part: a warp-uniform branch per
     // slot, so the FP64 pipe (~2 DFMA per clock per SM) does no dead work
 #pragma unroll
