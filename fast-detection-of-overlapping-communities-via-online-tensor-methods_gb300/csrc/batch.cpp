@@ -135,6 +135,9 @@ void fill_args(mmsb_batch* B, Bucket& b, int ctas, int64_t rounds) {
       const int nb = std::min(ctas, need);
       p[rd.bf16 ? G : 0] =
           stpm_partial_args(c, 0, 1, 2, rd.x0, rd.cnt, rd.c0, rd.c2, rd.bf16, gp, stride, nb);
+      // rounds after the first read the operand image of Phi that the
+      // graph's previous step wrote (plain FP32 tensor-core form)
+      if (r > 0 && rd.mode == kModePlain && !rd.bf16) p[0].phi_img = stpm_phi_image(c);
       b.has_prec[rd.bf16 ? 1 : 0][(size_t)r] = 1;
       u = stpm_online_update_args(c, rd, gp, stride, nb / stpm_partial_cluster());
       u.active = 1;

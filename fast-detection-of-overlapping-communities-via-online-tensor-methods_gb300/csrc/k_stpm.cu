@@ -136,11 +136,10 @@ __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
 // (one pass leaves Q1^T Q1 - I of about eps / ratio times a small constant, and
 // the first-order pass squares it), the floor a pivot below FP32 round-off of
 // A_jj is raised to (a column numerically dependent on the ones before it:
-// the floor keeps R^-1 bounded, the next pass orthonormalises), and the
-// largest number of exact passes per step
+// the floor keeps R^-1 bounded, the next pass orthonormalises); the largest
+// number of plain exact passes per step is StpmUpdateArgs::max_passes
 constexpr float kQrExactBelow = 1e-2f;
 constexpr float kPivotFloor = 1e-7f;
-constexpr int kQrMaxPasses = 4;
 // shifted restarts: below this pivot ratio the factorisation is redone with
 // the shift kShiftScale trace(A) (times 100 for each further restart, at
 // most kMaxShifts)
@@ -207,6 +206,17 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
 
 // waits for the phase with the given parity to complete; false after `limit`
 // clock64 cycles (then the caller reports kFlagTimeout instead of hanging)
+// global -> this CTA's shared memory, completing on `bar` (16-byte aligned
+// addresses, bytes a multiple of 16)
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes,
+                                              uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
                                                   long long limit) {
   const long long start = clock64();
@@ -564,6 +574,9 @@ __device__ __forceinline__ bool mbar_wait_cluster_bounded(uint64_t* bar, uint32_
     if (clock64() - start > limit) return false;
   }
 }
+
+template <int KP>
+struct ContractTc;  // the tensor-core contraction's shared-memory layout (below)
 
 template <int KP, int CL>
 __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
@@ -955,6 +968,38 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       const int r = e % KP, jb = e / KP, col = c0 + jb;
       if (r < k && col < k) a.phi[(int64_t)col * k + r] = Otc[jb * XLD + r];
     }
+    if constexpr (KP <= 112) {
+      if (a.phi_img) {
+        // the next contraction's operand image of this CTA's columns i (rows
+        // of its A operand, K = j): TF32 hi / lo in the core-matrix layout,
+        // then Phi^T mu1, Phi^T mu2 of the columns
+        using CT = ContractTc<KP>;
+        unsigned char* img = static_cast<unsigned char*>(a.phi_img);
+        for (int e = tid; e < NB * (KP / 4); e += blockDim.x) {
+          const int jb = e / (KP / 4), jq = e % (KP / 4), i = c0 + jb;
+          float v[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) v[u] = Otc[jb * XLD + 4 * jq + u];  // zero past k
+          uint4 h;
+          float4 l;
+          tc::split4(v, h, l);
+          const uint32_t off = tc::kmajor_off(i, 4 * jq, CT::SBOJ);
+          *reinterpret_cast<uint4*>(img + CT::PH + off) = h;
+          *reinterpret_cast<float4*>(img + CT::PL + off) = l;
+        }
+        float* mimg = reinterpret_cast<float*>(img + 2 * CT::PSZ);
+        for (int e = tid >> 5; e < 2 * NB; e += blockDim.x >> 5) {
+          const int which = e / NB, jb = e % NB, i = c0 + jb;
+          const float* mu = which == 0 ? a.mu1 : a.mu2;
+          float sv = 0.f;
+          if (mu && i < k)
+            for (int j = lane; j < k; j += 32) sv = fmaf(Otc[jb * XLD + j], mu[j], sv);
+#pragma unroll
+          for (int off = 16; off; off >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, off);
+          if (lane == 0) mimg[which * KP + i] = sv;
+        }
+      }
+    }
     if (a.trace_out) {  // ||Phi_new - snapshot||_F^2 over this CTA's columns, fixed order
       double d2 = 0.0;
       for (int e = tid; e < KP * NB; e += blockDim.x) {
@@ -1207,7 +1252,7 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
                                             unsigned char* smraw, float* stage) {
   using C = ContractTc<KP>;
   constexpr int TM = C::TM, NT = 512, NQ = KP / 4;
-  __shared__ __align__(8) uint64_t bars[2];  // Z products done | G products done
+  __shared__ __align__(8) uint64_t bars[3];  // Z products done | G products done | Phi image
   __shared__ uint32_t tmem_slot;
   unsigned char* base = smraw + ((1024 - (tc::sm_addr(smraw) & 1023)) & 1023);
   float* mv = reinterpret_cast<float*>(base + C::REGION);  // m1 | m2
@@ -1218,6 +1263,7 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
   if (tid == 0) {
     tc::mbar_init(&bars[0], 1);
     tc::mbar_init(&bars[1], 1);
+    tc::mbar_init(&bars[2], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   // Staging tasks are laid out so that the 8 lanes of a quarter-warp write
@@ -1326,7 +1372,28 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
   };
   float* part = reinterpret_cast<float*>(base + C::CH);  // [q][i][jq]
   static_assert(2 * KP * NQ * 4 <= 2 * C::TSZ, "partials fit the C area");
-  {
+  bool img_timed_out = false;
+  if (a.phi_img) {
+    // the previous step kernel wrote Phi's operand image and Phi^T mu1|2:
+    // bulk copies of the hi | lo image (in 4 pieces) and plain loads of m
+    __syncthreads();  // every thread past its first-tile stores (the barrier init is ordered)
+    if (tid == 0) {
+      constexpr uint32_t bytes = 2 * C::PSZ, piece = bytes / 4;
+      static_assert(bytes % 64 == 0, "16-byte pieces");
+      mbar_arrive_expect_tx(&bars[2], bytes);
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        bulk_copy_g2s(base + C::PH + q * piece, static_cast<const unsigned char*>(a.phi_img) + q * piece,
+                      piece, &bars[2]);
+    }
+    const float* mimg = reinterpret_cast<const float*>(static_cast<const unsigned char*>(a.phi_img) +
+                                                       2 * C::PSZ);
+    float m = 0.f;
+    if (tid < 2 * KP) m = mimg[tid];
+    __syncthreads();  // every read of mus done (mv and mus share storage)
+    if (tid < 2 * KP) mv[tid] = m;
+    if (!tc::mbar_wait(&bars[2], 0u, tc::wait_limit_or_default(a.wait_limit))) img_timed_out = true;
+  } else {
     float v[PT][4];
 #pragma unroll
     for (int t = 0; t < PT; ++t) {
@@ -1378,7 +1445,7 @@ __device__ __forceinline__ void contract_tc(const StpmPartialArgs& a, int nblock
   const uint32_t tmem = tmem_slot, sbase = tc::sm_addr(base);
   const float cc0 = a.c0, cc2 = a.c2;
   uint32_t ph_z = 0u, ph_g = 0u;
-  bool g_pending = false, timed_out = false, any = false;
+  bool g_pending = false, timed_out = img_timed_out, any = false;
   int64_t tile = blockIdx.x;
   for (; tile < ntiles; tile += nblocks) {
     // the G products of the previous tile read y3 and C
@@ -2444,6 +2511,12 @@ cudaError_t stpm_update(const StpmUpdateArgs& a, cudaStream_t s) {
 }
 
 int stpm_step_kp(int k) { return stpm_kp(k); }
+
+size_t stpm_phi_image_bytes(int k) {
+  const int kp = stpm_kp(k);
+  if (kp < 32 || kp > 112) return 0;
+  return (size_t)8 * kp * kp + (size_t)8 * kp;  // hi | lo (ContractTc<KP>::PSZ each), m1 | m2
+}
 
 cudaError_t stpm_partial_batched(int mode, int KP, const StpmPartialArgs* args, int graphs,
                                  int grid, bool bf16, cudaStream_t s) {

@@ -37,7 +37,16 @@ struct StpmPartialArgs {
   int nblocks;           // batched launches: CTAs of this graph (multiple of the cluster size)
   unsigned* flags;       // device flag word (MMSB_ERR_TIMEOUT of a bounded wait), may be null
   long long wait_limit;  // clock64 cycles a bounded wait may take (0: about one second)
+  // tensor-core plain FP32 form (KP <= 112): Phi already split into its TF32
+  // hi / lo operand image, followed by Phi^T mu1 | Phi^T mu2 (2 KP floats),
+  // as the previous step kernel wrote it (stpm_phi_image_bytes); null: the
+  // contraction stages Phi itself
+  const void* phi_img;
 };
+
+// bytes of the operand image of Phi that the step kernel writes for the
+// tensor-core contraction (0 where that form does not exist for k)
+size_t stpm_phi_image_bytes(int k);
 
 struct StpmReduceArgs {
   int mode;
@@ -85,6 +94,9 @@ struct StpmUpdateArgs {
   // run, whose Phi0 need not be orthonormal); 0 = Phi is the previous step's
   // Q (orthonormal to ~1e-7), so the diagonal of (Phi^T Phi)^.2 suffices
   int phi_general;
+  // the contraction's operand image of the new Phi (stpm_phi_image_bytes), or
+  // null
+  void* phi_img;
   // convergence trace (may be null): CTA q writes sum over its columns of
   // (Phi_new - trace_snap)^2 to trace_out[q] and sets trace_snap = Phi_new there
   float* trace_snap;

@@ -610,12 +610,14 @@ StpmPartialArgs stpm_partial_args(mmsb_ctx* c, int q1, int q2, int q3, int64_t b
 
 // per-CTA partial contractions over nodes [begin, begin+count)
 static PartialOut stpm_partials(mmsb_ctx* c, int mode, int q1, int q2, int q3, int64_t begin,
-                                int64_t count, double c0, double c2, bool bf16 = false) {
+                                int64_t count, double c0, double c2, bool bf16 = false,
+                                const void* phi_img = nullptr) {
   const int k = c->k;
   const int grid = stpm_partial_grid(count, bf16);
   const int64_t stride = (int64_t)k * k + 3 * k + 4;
   float* gpart = c->tbuf<float>("gpart", (size_t)grid * stride);
   StpmPartialArgs a = stpm_partial_args(c, q1, q2, q3, begin, count, c0, c2, bf16, gpart, stride, grid);
+  a.phi_img = phi_img;
   timed_launch(c, 0, [&]() { ck(stpm_partial(mode, a, grid, bf16, c->s), "stpm_partial"); });
   const int products = mode == kModePlain ? 3 : mode == kModeAdjoint ? 6 : 3;
   c->stats.contract_flops += 2.0 * k * k * (double)count * products;
@@ -671,6 +673,11 @@ static void qr_only(mmsb_ctx* c) {
   ck(stpm_update(u, c->s), "stpm_qr");
 }
 
+void* stpm_phi_image(mmsb_ctx* c) {
+  const size_t bytes = stpm_phi_image_bytes(c->k);
+  return bytes ? c->buf("phi_img", bytes) : nullptr;
+}
+
 StpmUpdateArgs stpm_online_update_args(mmsb_ctx* c, const OnlineRound& rd, float* gpart,
                                        int64_t stride, int nparts) {
   const int k = c->k;
@@ -689,6 +696,7 @@ StpmUpdateArgs stpm_online_update_args(mmsb_ctx* c, const OnlineRound& rd, float
   u.beta = (float)rd.beta;
   u.gscale = (float)rd.gscale;
   u.phi_general = rd.r == 0 ? 1 : 0;
+  u.phi_img = stpm_phi_image(c);
   return u;
 }
 
@@ -739,7 +747,12 @@ int64_t stpm_online_rounds(const mmsb_ctx* c) {
 static void stpm_step(mmsb_ctx* c, const OnlineRound& rd, bool timed = true,
                       float* trace_snap = nullptr, double* trace_out = nullptr) {
   c->ksample = timed;
-  PartialOut po = stpm_partials(c, rd.mode, 0, 1, 2, rd.x0, rd.cnt, rd.c0, rd.c2, rd.bf16);
+  // the previous step of the run wrote Phi's operand image for the
+  // tensor-core contraction of the plain FP32 form
+  void* img = stpm_phi_image(c);
+  const bool use_img = img && rd.r > 0 && rd.mode == kModePlain && !rd.bf16;
+  PartialOut po = stpm_partials(c, rd.mode, 0, 1, 2, rd.x0, rd.cnt, rd.c0, rd.c2, rd.bf16,
+                                use_img ? img : nullptr);
   StpmUpdateArgs u = stpm_online_update_args(c, rd, po.gpart, po.stride, po.grid);
   u.trace_snap = trace_snap;
   u.trace_out = trace_out;

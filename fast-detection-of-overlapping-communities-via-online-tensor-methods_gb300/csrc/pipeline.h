@@ -48,6 +48,9 @@ mmsb::StpmPartialArgs stpm_partial_args(mmsb_ctx* c, int q1, int q2, int q3, int
                                   int64_t stride, int nblocks);
 mmsb::StpmUpdateArgs stpm_online_update_args(mmsb_ctx* c, const OnlineRound& rd, float* gpart,
                                        int64_t stride, int nparts);
+// the context's buffer for the step kernel's operand image of Phi (null
+// where the tensor-core contraction does not exist for k)
+void* stpm_phi_image(mmsb_ctx* c);
 void stpm_lambda_pass(mmsb_ctx* c);
 void stpm_online_stats(mmsb_ctx* c, int64_t steps);
 void stpm_finish_online(mmsb_ctx* c, int64_t steps);
