@@ -107,26 +107,37 @@ __global__ void count_cols_kernel(const int32_t* __restrict__ ci, int64_t nnz, i
   }
 }
 
-// Exclusive scan in place over n+1 entries (entry 0 == 0 on input), one CTA.
+// Inclusive scan in place over n+1 entries, one CTA of 1024 threads: with
+// entry 0 == 0 and entry c + 1 == the count of column c on input, entry c is
+// then the offset of column c.  Coalesced tiles of 1024 entries, a warp scan
+// by shuffles, then a scan of the 32 warp totals, and a carry across tiles.
 __global__ void __launch_bounds__(1024) scan_kernel(unsigned long long* __restrict__ a, int64_t n1) {
-  __shared__ unsigned long long part[1024];
-  const int t = threadIdx.x;
-  const int64_t per = (n1 + 1023) / 1024;
-  const int64_t b = t * per, e = min(n1, b + per);
-  unsigned long long s = 0;
-  for (int64_t i = b; i < e; ++i) s += a[i];
-  part[t] = s;
-  __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    unsigned long long v = t >= off ? part[t - off] : 0ull;
+  __shared__ unsigned long long wsum[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  unsigned long long carry = 0ull;
+  for (int64_t base = 0; base < n1; base += 1024) {
+    const int64_t i = base + t;
+    unsigned long long x = i < n1 ? a[i] : 0ull;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= off) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
     __syncthreads();
-    part[t] += v;
+    if (w == 0) {
+      unsigned long long v = wsum[lane];
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, v, off);
+        if (lane >= off) v += y;
+      }
+      wsum[lane] = v;
+    }
     __syncthreads();
-  }
-  unsigned long long run = t ? part[t - 1] : 0ull;
-  for (int64_t i = b; i < e; ++i) {
-    run += a[i];
-    a[i] = run;
+    if (i < n1) a[i] = carry + (w ? wsum[w - 1] : 0ull) + x;
+    carry += wsum[31];
+    __syncthreads();  // wsum is rewritten by the next tile
   }
 }
 
@@ -151,14 +162,37 @@ __global__ void scatter_kernel(const int64_t* __restrict__ rp, const int32_t* __
 // Sorts every row segment of the transposed CSR by column (rank sort, one
 // warp per segment; equal columns, from duplicate entries of the input, keep
 // their input order, so the ranks always form a permutation).
-__global__ void segment_sort_kernel(const int64_t* __restrict__ rpT, int64_t n_rowsT,
-                                    const int32_t* __restrict__ in_c, const float* __restrict__ in_v,
-                                    int32_t* __restrict__ out_c, float* __restrict__ out_v) {
-  const int lane = threadIdx.x & 31;
+constexpr int kSegStage = 512;  // segment entries a warp stages in shared memory
+
+__global__ void __launch_bounds__(256) segment_sort_kernel(const int64_t* __restrict__ rpT,
+                                                           int64_t n_rowsT,
+                                                           const int32_t* __restrict__ in_c,
+                                                           const float* __restrict__ in_v,
+                                                           int32_t* __restrict__ out_c,
+                                                           float* __restrict__ out_v) {
+  __shared__ int32_t seg[8][kSegStage];
+  const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (w >= n_rowsT) return;
+  if (w >= n_rowsT) return;  // warp-uniform
   const int64_t b = rpT[w], e = rpT[w + 1];
   const int64_t L = e - b;
+  if (L <= kSegStage) {
+    // the segment in shared memory: the rank loop reads broadcast words
+    int32_t* sg = seg[wb];
+    for (int64_t i = lane; i < L; i += 32) sg[i] = in_c[b + i];
+    __syncwarp();
+    for (int64_t i = lane; i < L; i += 32) {
+      const int32_t x = sg[i];
+      int rank = 0;
+      for (int j = 0; j < (int)L; ++j) {
+        const int32_t y = sg[j];
+        rank += (y < x) || (y == x && j < i);
+      }
+      out_c[b + rank] = x;
+      if (out_v) out_v[b + rank] = in_v[b + i];
+    }
+    return;
+  }
   for (int64_t i = lane; i < L; i += 32) {
     const int32_t x = in_c[b + i];
     int64_t rank = 0;
