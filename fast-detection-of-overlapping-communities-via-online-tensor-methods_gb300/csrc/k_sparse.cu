@@ -109,35 +109,48 @@ __global__ void count_cols_kernel(const int32_t* __restrict__ ci, int64_t nnz, i
 
 // Inclusive scan in place over n+1 entries, one CTA of 1024 threads: with
 // entry 0 == 0 and entry c + 1 == the count of column c on input, entry c is
-// then the offset of column c.  Coalesced tiles of 1024 entries, a warp scan
-// by shuffles, then a scan of the 32 warp totals, and a carry across tiles.
+// then the offset of column c.  Groups of kScanTiles coalesced tiles of 1024
+// entries are loaded together (one memory latency per group), then scanned
+// tile by tile: a warp scan by shuffles, a scan of the 32 warp totals, and a
+// carry across tiles.
+constexpr int kScanTiles = 16;
+
 __global__ void __launch_bounds__(1024) scan_kernel(unsigned long long* __restrict__ a, int64_t n1) {
   __shared__ unsigned long long wsum[32];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   unsigned long long carry = 0ull;
-  for (int64_t base = 0; base < n1; base += 1024) {
-    const int64_t i = base + t;
-    unsigned long long x = i < n1 ? a[i] : 0ull;
+  for (int64_t group = 0; group < n1; group += (int64_t)kScanTiles * 1024) {
+    unsigned long long v[kScanTiles];
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, off);
-      if (lane >= off) x += y;
+    for (int q = 0; q < kScanTiles; ++q) {
+      const int64_t i = group + (int64_t)q * 1024 + t;
+      v[q] = i < n1 ? a[i] : 0ull;
     }
-    if (lane == 31) wsum[w] = x;
-    __syncthreads();
-    if (w == 0) {
-      unsigned long long v = wsum[lane];
+#pragma unroll
+    for (int q = 0; q < kScanTiles; ++q) {
+      const int64_t i = group + (int64_t)q * 1024 + t;
+      unsigned long long x = v[q];
 #pragma unroll
       for (int off = 1; off < 32; off <<= 1) {
-        const unsigned long long y = __shfl_up_sync(0xffffffffu, v, off);
-        if (lane >= off) v += y;
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
       }
-      wsum[lane] = v;
+      if (lane == 31) wsum[w] = x;
+      __syncthreads();
+      if (w == 0) {
+        unsigned long long u = wsum[lane];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const unsigned long long y = __shfl_up_sync(0xffffffffu, u, off);
+          if (lane >= off) u += y;
+        }
+        wsum[lane] = u;
+      }
+      __syncthreads();
+      if (i < n1) a[i] = carry + (w ? wsum[w - 1] : 0ull) + x;
+      carry += wsum[31];
+      __syncthreads();  // wsum is rewritten by the next tile
     }
-    __syncthreads();
-    if (i < n1) a[i] = carry + (w ? wsum[w - 1] : 0ull) + x;
-    carry += wsum[31];
-    __syncthreads();  // wsum is rewritten by the next tile
   }
 }
 
