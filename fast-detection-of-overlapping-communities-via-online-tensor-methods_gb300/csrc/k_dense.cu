@@ -664,15 +664,24 @@ __global__ void __launch_bounds__(512) jacobi_cluster_kernel(int p, const double
   __syncthreads();
   // rotate column u against column v (both in local shared memory) if they
   // are not yet orthogonal to tol; uniform shuffles across the warp
+  // (16-byte vectors: a column's ld is a multiple of 16 floats and its rows
+  // past p hold zeros, which the rotations keep; the rotation parameters use
+  // the fast division: the FP64 refinement that follows absorbs its ulps.
+  // The sweep count is set by the issue rate of this loop: ~200 instructions
+  // per rotation with scalar words)
+  const int n4 = (p + 3) / 4;
+  const float tol2 = tol * tol;
   auto rotate = [&](float* u, float* v, bool live, int& rotated) {
     float al = 0.f, be = 0.f, ga = 0.f;
+    float4* u4 = reinterpret_cast<float4*>(u);
+    float4* v4 = reinterpret_cast<float4*>(v);
     if (live) {
-#pragma unroll 4
-      for (int i = ln; i < p; i += LANES) {
-        const float x = u[i], y = v[i];
-        al = fmaf(x, x, al);
-        be = fmaf(y, y, be);
-        ga = fmaf(x, y, ga);
+#pragma unroll 2
+      for (int i = ln; i < n4; i += LANES) {
+        const float4 x = u4[i], y = v4[i];
+        al = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, al))));
+        be = fmaf(y.x, y.x, fmaf(y.y, y.y, fmaf(y.z, y.z, fmaf(y.w, y.w, be))));
+        ga = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, fmaf(x.w, y.w, ga))));
       }
     }
 #pragma unroll
@@ -681,15 +690,17 @@ __global__ void __launch_bounds__(512) jacobi_cluster_kernel(int p, const double
       be += __shfl_xor_sync(0xffffffffu, be, off);
       ga += __shfl_xor_sync(0xffffffffu, ga, off);
     }
-    if (live && fabsf(ga) > tol * sqrtf(al * be) && ga != 0.f) {
-      const float zeta = (be - al) / (2.f * ga);
-      const float tt = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-      const float c = rsqrtf(1.f + tt * tt), sn = c * tt;
-#pragma unroll 4
-      for (int i = ln; i < p; i += LANES) {
-        const float x = u[i], y = v[i];
-        u[i] = c * x - sn * y;
-        v[i] = sn * x + c * y;
+    if (live && ga * ga > tol2 * (al * be) && ga != 0.f) {
+      const float zeta = __fdividef(be - al, 2.f * ga);
+      const float tt = __fdividef(copysignf(1.f, zeta), fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.f)));
+      const float c = rsqrtf(fmaf(tt, tt, 1.f)), sn = c * tt;
+#pragma unroll 2
+      for (int i = ln; i < n4; i += LANES) {
+        const float4 x = u4[i], y = v4[i];
+        u4[i] = make_float4(c * x.x - sn * y.x, c * x.y - sn * y.y, c * x.z - sn * y.z,
+                            c * x.w - sn * y.w);
+        v4[i] = make_float4(sn * x.x + c * y.x, sn * x.y + c * y.y, sn * x.z + c * y.z,
+                            sn * x.w + c * y.w);
       }
       rotated = 1;
     }
