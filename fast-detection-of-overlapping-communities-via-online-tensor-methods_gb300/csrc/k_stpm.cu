@@ -1223,22 +1223,41 @@ __device__ __forceinline__ void partial_cluster_sum(const StpmPartialArgs& a, fl
   const int crank = (int)cluster.block_rank(), tid = threadIdx.x, NT = blockDim.x, k = a.k;
   constexpr int CLP = kPartialCluster;
   constexpr int STAGE = KP * IB + 3 * IB + 1;
+  // 16-byte slices: the staging areas have room past STAGE (the tile region
+  // they overlay is larger), and KP, IB are multiples of 4, so the 4 entries
+  // of a vector share their row i of G
+  constexpr int STAGE4 = (STAGE + 3) / 4;
+  static_assert(KP % 4 == 0 && IB % 4 == 0, "16-byte slices");
   cluster.sync();
   float* gp = a.gpart + (int64_t)(blockIdx.x / CLP) * a.part_stride;
-  const int slice = (STAGE + CLP - 1) / CLP;
-  for (int e = crank * slice + tid; e < min(STAGE, (crank + 1) * slice); e += NT) {
-    float v = 0.f;
-#pragma unroll
-    for (int q = 0; q < CLP; ++q) v += cluster.map_shared_rank(stage, q)[e];
+  const int slice4 = (STAGE4 + CLP - 1) / CLP;
+  auto put = [&](int e, float v) {
     if (e < KP * IB) {
       const int i = i0 + e / KP, j = e % KP;
       if (i < k && j < k && MODE != kModeLoss) gp[(int64_t)i * k + j] = v;
     } else if (e < KP * IB + 3 * IB) {
       const int q = (e - KP * IB) / IB, i = i0 + (e - KP * IB) % IB;
       if (i < k) gp[(int64_t)k * k + q * k + i] = v;
-    } else {
+    } else if (e < STAGE) {
       gp[(int64_t)k * k + 3 * k + cb] = v;
     }
+  };
+  for (int e4 = crank * slice4 + tid; e4 < min(STAGE4, (crank + 1) * slice4); e4 += NT) {
+    float4 r[CLP];
+#pragma unroll
+    for (int q = 0; q < CLP; ++q) r[q] = reinterpret_cast<const float4*>(cluster.map_shared_rank(stage, q))[e4];
+    float4 v = r[0];
+#pragma unroll
+    for (int q = 1; q < CLP; ++q) {
+      v.x += r[q].x;
+      v.y += r[q].y;
+      v.z += r[q].z;
+      v.w += r[q].w;
+    }
+    put(4 * e4, v.x);
+    put(4 * e4 + 1, v.y);
+    put(4 * e4 + 2, v.z);
+    put(4 * e4 + 3, v.w);
   }
   if (cb == 0 && crank == 0 && tid < 4 && tid >= NBC) gp[(int64_t)k * k + 3 * k + tid] = 0.f;
   cluster.sync();  // keep shared memory alive until every remote read is done
