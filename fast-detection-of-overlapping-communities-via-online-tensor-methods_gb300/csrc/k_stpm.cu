@@ -166,11 +166,14 @@ struct StepSmem {
   static constexpr size_t full = (size_t)(SB ? 1 : 2) * KP * XLD;
   static constexpr size_t tiles = (size_t)4 * NB * XLD;  // B block, 2 staging tiles, G block
   static constexpr size_t kpart = KS == 2 ? (size_t)TILES * 128 : 0;
-  static constexpr size_t small = 3 * KP + 4 * NB + 64 + 8;  // mean terms, d-sums, |phi_i|^2, tmp
-  static constexpr size_t tinv = SB ? 0 : (size_t)64 * NBK;  // SB: in the G block's tile
+  // mean terms, d-sums, |phi_i|^2, mu1..3, tmp
+  static constexpr size_t small = 6 * KP + 4 * NB + 128 + 8;
+  // inverse diagonal blocks and superblock corners (SB: in the G block's tile)
+  static constexpr size_t tinv = SB ? 0 : (size_t)64 * NBK + 64 * (KP / 16);
   static constexpr size_t floats = full + tiles - (SB ? NB * XLD : 0) + kpart + small + tinv +
                                    2 * KP;  // original diagonal, 1 / R_jj
-  static_assert(!SB || (size_t)64 * NBK <= (size_t)NB * XLD, "inverse blocks in the G tile");
+  static_assert(!SB || (size_t)64 * NBK + 64 * (KP / 16) <= (size_t)NB * XLD,
+                "inverse blocks in the G tile");
   static_assert(floats * sizeof(float) <= 227 * 1024 - 2048, "step kernel shared memory");
 };
 
@@ -499,64 +502,112 @@ __device__ float chol_blocked(float* A, int k, float* tinv, float* rd, float* dg
 
 // Columns c0 .. c0+NB of W = R^-1 (NB = 8 or 16: whole 8-column blocks) into
 // Wb (column jb at Wb + jb * XLD, rows past the diagonal block zero), by
-// block back substitution per 8-column block K: W_KK = T_KK,
-// W_LK = -T_LL S_L with S_L = sum_{M=L+1..K} R_LM W_MK.  One barrier per
-// level: warp 0 adds the last term of S_(L-1) and applies -T, while the
-// other warps add R_rL W_LK into the partial sums of the rows above (held
-// in Wb until their block's turn).  tmp: 64 floats.  Whole CTA; ends with
-// a barrier.
+// block back substitution per 8-column block K: W_KK = T_KK, then upwards in
+// levels of 16 rows aligned to 16 (one 8-row level first when K is odd):
+// W_Q = -T_Q S_Q with S_Q = sum over the rows P below Q of R_QP W_PK, where
+// for a 16-row superblock Q = (a, b) of 8-row blocks T_Q = [T_a X; 0 T_b],
+// X = -T_a R_ab T_b (x16, 8 x 8 column-major per superblock, formed here
+// first).  One barrier per level: warps 0-3 add the last term of S_Q and
+// apply -T_Q (a named barrier between the two), while the other warps add
+// R_rP W_PK of the last level into the partial sums of the rows above
+// (held in Wb until their level).  The levels of the last column block are
+// about KP / 16 instead of KP / 8, which is what the cluster waits for.
+// Blocks that lie wholly in the padding (8K >= k: R is the identity there)
+// get unit columns.  tmp: 128 floats.  Whole CTA of at least 5 warps; ends
+// with a barrier.
 template <int KP, int NB>
-__device__ void inverse_columns(const float* R, const float* tinv, int c0, float* Wb, float* tmp) {
-  constexpr int XLD = step_xld(KP);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int e = tid; e < NB * XLD; e += blockDim.x) Wb[e] = 0.f;
-  __syncthreads();
+__device__ void inverse_columns(const float* R, const float* tinv, float* x16, int c0, int k,
+                                float* Wb, float* tmp) {
+  constexpr int XLD = step_xld(KP), NSB = KP / 16;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < NB * XLD; e += nt) Wb[e] = 0.f;
+  // X(a, b) = -sum_i T_2m(a, i) sum_j R(16m + i, 16m + 8 + j) T_2m+1(j, b)
+  // (the T blocks hold explicit zeros below their diagonals; the R reads of
+  // a warp are broadcasts)
+  for (int e = tid; e < NSB * 64; e += nt) {
+    const int m = e >> 6, aa = e & 7, b = (e >> 3) & 7, r0 = 16 * m;
+    const float* ta = tinv + 64 * (2 * m);
+    const float* tb = ta + 64;
+    float tv[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) tv[j] = tb[j + 8 * b];
+    float x = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      float y = 0.f;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) y = fmaf(R[(r0 + i) + (r0 + 8 + j) * XLD], tv[j], y);
+      x = fmaf(ta[aa + 8 * i], y, x);
+    }
+    x16[e] = -x;
+  }
 #pragma unroll 1
   for (int sb = 0; sb < NB / 8; ++sb) {
     const int K = c0 / 8 + sb;
     float* W = Wb + 8 * sb * XLD;
-    for (int e = tid; e < 64; e += blockDim.x) {
+    __syncthreads();  // zero fill, X and the previous column block done
+    if (8 * K >= k) {
+      if (tid < 8) W[8 * K + tid + tid * XLD] = 1.f;
+      continue;
+    }
+    for (int e = tid; e < 64; e += nt) {
       const int aa = e & 7, jb = e >> 3;
       W[8 * K + aa + jb * XLD] = tinv[64 * K + e];  // W_KK = T_KK (column-major)
     }
     __syncthreads();
-    for (int L = K; L >= 1; --L) {
-      const int l0 = 8 * L, p0 = l0 - 8;
-      if (warp == 0) {
-        // S_(L-1) += R_(L-1),L W_LK, then W_(L-1)K = -T_(L-1) S_(L-1)
+    int lo = 8 * K, h = 8;  // rows [lo, lo + h) were the last level
+    while (lo > 0) {
+      const int hn = (lo & 15) ? 8 : 16, nlo = lo - hn;
+      if (tid < 128) {
+        // S_Q (row i, column jb) = partial sum + R(nlo + i, lo ..) W(lo .., jb)
+        const int i = tid & 15, jb = tid >> 4;
+        if (i < hn) {
+          float sv = W[nlo + i + jb * XLD];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int e = lane + 32 * h, aa = e & 7, jb = e >> 3, r = p0 + aa;
-          float sv = W[r + jb * XLD];
+          for (int b = 0; b < 8; ++b) sv = fmaf(R[(nlo + i) + (lo + b) * XLD], W[lo + b + jb * XLD], sv);
+          if (h == 16) {
 #pragma unroll
-          for (int b = 0; b < 8; ++b) sv = fmaf(R[r + (l0 + b) * XLD], W[l0 + b + jb * XLD], sv);
-          tmp[e] = sv;
+            for (int b = 8; b < 16; ++b) sv = fmaf(R[(nlo + i) + (lo + b) * XLD], W[lo + b + jb * XLD], sv);
+          }
+          tmp[i + 16 * jb] = sv;
         }
-        __syncwarp();
-        const float* tb = tinv + 64 * (L - 1);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int e = lane + 32 * h, aa = e & 7, jb = e >> 3;
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        if (i < hn) {
+          const float* s = tmp + 16 * jb;
           float w = 0.f;
+          // T rows from the diagonal on (zeros below it are stored)
+          const int ii = i & 7;
+          const float* t = tinv + 64 * (nlo / 8 + (i >> 3));
+          const float* sv = s + (i & 8);
 #pragma unroll
-          for (int b = 0; b < 8; ++b)
-            if (b >= aa) w = fmaf(tb[aa + 8 * b], tmp[b + 8 * jb], w);
-          W[p0 + aa + jb * XLD] = -w;
+          for (int b = 0; b < 8; ++b) w = fmaf(t[ii + 8 * b], sv[b], w);
+          if (hn == 16 && i < 8) {
+            const float* x = x16 + 64 * (nlo / 16) + i;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) w = fmaf(x[8 * j], s[8 + j], w);
+          }
+          W[nlo + i + jb * XLD] = -w;
         }
       } else {
-        // rows above block L-1 accumulate R_rL W_LK
-        const int rows = p0;
-        for (int e = tid - 32; e < rows * 8; e += (int)blockDim.x - 32) {
-          const int r = e % rows, jb = e / rows;
+        // rows above the level accumulate R(r, lo ..) W(lo .., jb)
+        for (int e = tid - 128; e < nlo * 8; e += nt - 128) {
+          const int r = e % nlo, jb = e / nlo;
           float sv = W[r + jb * XLD];
 #pragma unroll
-          for (int b = 0; b < 8; ++b) sv = fmaf(R[r + (l0 + b) * XLD], W[l0 + b + jb * XLD], sv);
+          for (int b = 0; b < 8; ++b) sv = fmaf(R[r + (lo + b) * XLD], W[lo + b + jb * XLD], sv);
+          if (h == 16) {
+#pragma unroll
+            for (int b = 8; b < 16; ++b) sv = fmaf(R[r + (lo + b) * XLD], W[lo + b + jb * XLD], sv);
+          }
           W[r + jb * XLD] = sv;
         }
       }
       __syncthreads();
+      h = hn;
+      lo = nlo;
     }
   }
+  __syncthreads();
 }
 
 __device__ __forceinline__ bool mbar_wait_cluster_bounded(uint64_t* bar, uint32_t parity,
@@ -597,9 +648,11 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   float* mv = part + S::kpart;                    // m1, m2, m3 of this block
   float* dcol = mv + 3 * KP;                      // 3 * NB d-sums
   float* nn = dcol + 3 * NB;                      // |phi_i|^2 of this block
-  float* tmp = nn + NB;                           // 64 (inverse columns)
-  float* tinv = S::SB ? Gb : tmp + 64 + 8;        // 8 x 8 inverse diagonal blocks
-  float* dg = (S::SB ? tmp + 64 + 8 : tinv + 64 * S::NBK);  // original diagonal
+  float* mus = nn + NB;                           // mu1, mu2, mu3 (KP each)
+  float* tmp = mus + 3 * KP;                      // 128 (inverse columns)
+  float* tinv = S::SB ? Gb : tmp + 128 + 8;       // 8 x 8 inverse diagonal blocks
+  float* x16 = tinv + 64 * S::NBK;                // corners of the 16 x 16 inverse blocks
+  float* dg = (S::SB ? tmp + 128 + 8 : x16 + 64 * (KP / 16));  // original diagonal
   float* rd = dg + KP;                            // 1 / R_jj
   __shared__ float s_ratio;
   __shared__ float s_emax[16];
@@ -633,9 +686,14 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   if (tid <= 2 * CL) asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   __syncthreads();
   if (a.step_mode == kStepOnline) {
-    // the mean terms phi_i . mu and |phi_i|^2 of this block's columns (a warp
-    // per dot product, lanes along the k entries): Phi and mu only, so
-    // before the wait
+    // mu1..3 for the G block below, and the mean terms phi_i . mu and
+    // |phi_i|^2 of this block's columns (a warp per dot product, lanes along
+    // the k entries): Phi and mu only, so before the wait
+    for (int e = tid; e < 3 * KP; e += blockDim.x) {
+      const int which = e / KP, j = e % KP;
+      const float* mu = which == 0 ? a.mu1 : which == 1 ? a.mu2 : a.mu3;
+      mus[e] = (mu && j < k) ? __ldg(mu + j) : 0.f;
+    }
     for (int e = tid / 32; e < 4 * NB; e += blockDim.x / 32) {
       const int which = e / NB, jb = e % NB, i = c0 + jb;
       const float* col = Xa + i * XLD;
@@ -673,17 +731,23 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   // bounded cluster barrier: every thread of every CTA has passed the
   // __syncthreads before its rank's arrival (remote mbarrier arrives with
   // release semantics, waited for with acquire); false after a timeout
-  auto csync = [&]() -> bool {
+  auto csync_arrive = [&]() {
     __syncthreads();
     if (tid < CL) {
       uint32_t remote;
       asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(smem_addr(&s_csync)), "r"(tid));
       asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(remote) : "memory");
     }
+  };
+  auto csync_wait = [&]() -> bool {
     bool ok = true;
     if (tid == 0) ok = mbar_wait_cluster_bounded(&s_csync, csync_parity, wl);
     csync_parity ^= 1u;
     return !__syncthreads_or(!ok);
+  };
+  auto csync = [&]() -> bool {
+    csync_arrive();
+    return csync_wait();
   };
   // the staged block Otc (this CTA's columns) into `dst` of every rank,
   // own copy included; sync_first: a cluster barrier first, because some
@@ -796,12 +860,12 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
         const float m1 = mv[jb], m2 = mv[KP + jb], m3 = mv[2 * KP + jb];
         const float c1 = (float)a.c1, c2 = (float)a.c2;
         if (a.mode == kModePlain) {
-          gv += a.mu3[j] * (c1 * m1 * m2 + c2 * dcol[jb]);
+          gv += mus[2 * KP + j] * (c1 * m1 * m2 + c2 * dcol[jb]);
         } else {
           const float ic = (float)(1.0 / a.count);
-          gv += a.mu1[j] * (c2 * dcol[jb] * ic + c1 * m2 * m3) +
-                a.mu2[j] * (c2 * dcol[NB + jb] * ic + c1 * m1 * m3) +
-                a.mu3[j] * (c2 * dcol[2 * NB + jb] * ic + c1 * m1 * m2);
+          gv += mus[j] * (c2 * dcol[jb] * ic + c1 * m2 * m3) +
+                mus[KP + j] * (c2 * dcol[NB + jb] * ic + c1 * m1 * m3) +
+                mus[2 * KP + j] * (c2 * dcol[2 * NB + jb] * ic + c1 * m1 * m2);
         }
         gval = gv;
       }
@@ -895,7 +959,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       resync = true;
       continue;
     }
-    inverse_columns<KP, NB>(F, tinv, c0, Ab, tmp);
+    inverse_columns<KP, NB>(F, tinv, x16, c0, k, Ab, tmp);
     ++passes;
     if (S::SB) restore_m();
     Otc = stage_next();
@@ -932,6 +996,13 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
       break;
     }
   }
+  // every copy of the last exchange has landed in this CTA, and each rank
+  // sent its blocks only after the barrier that opened that exchange, so
+  // every rank's phase of that barrier is complete: this CTA's arrival at
+  // the closing barrier (no remote access follows) goes out now, its wait
+  // comes at the end
+  const bool early_arrive = !timed_out;
+  if (early_arrive) csync_arrive();
   // first-order second pass: E = M^T M - I, F = strict upper part of E plus
   // half its diagonal (this CTA's columns, in Ab), Phi = M (I - F)
   float emax = 0.f;
@@ -1029,7 +1100,7 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
   if (rank == 0 && tid == 0 && a.orth_passes) atomicAdd(a.orth_passes, passes);
   // keep shared memory alive until remote writers are done (bounded: after a
   // timeout the ranks may stand at different barriers)
-  if (!csync()) {
+  if (!(early_arrive ? csync_wait() : csync())) {
     if (tid == 0) atomicOr(a.flags, kFlagTimeout);
     __nanosleep(100000);  // let copies a stalled exchange left in flight land
   }
