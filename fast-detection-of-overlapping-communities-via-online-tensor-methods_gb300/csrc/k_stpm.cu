@@ -255,8 +255,9 @@ __device__ __forceinline__ void bulk_copy_to_rank(const void* dst_local, const v
 // tile at pa = &A(0, 0) of the tile, pb = &B(0, 0) of the tile, with
 // A(m, k) = pa[m AM + k AK] and B(k, n) = pb[k BK + n BN].  Fragments of
 // m16n8k8 (g = lane / 4, t = lane % 4): a = A(g|g+8, t|t+4), b = B(t|t+4, g),
-// acc = C(g|g+8, 2t|2t+1).
-template <int AM, int AK, int BK, int BN>
+// acc = C(g|g+8, 2t|2t+1).  SPLIT = false: one TF32 product (for a small
+// correction term whose relative error may be ~1e-3).
+template <int AM, int AK, int BK, int BN, bool SPLIT = true>
 __device__ __forceinline__ void warp_tile_3xtf32(const float* __restrict__ pa,
                                                  const float* __restrict__ pb, int kb, int ke,
                                                  float (&acc)[4]) {
@@ -279,11 +280,13 @@ __device__ __forceinline__ void warp_tile_3xtf32(const float* __restrict__ pa,
       bl[q] = __float_as_uint(bv[q] - __uint_as_float(bh[q]));
     }
     mma_tf32(c0, ah, bh);
-    mma_tf32(c1, ah, bl);
-    mma_tf32(c2, al, bh);
+    if (SPLIT) {
+      mma_tf32(c1, ah, bl);
+      mma_tf32(c2, al, bh);
+    }
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) acc[q] = c0[q] + (c1[q] + c2[q]);
+  for (int q = 0; q < 4; ++q) acc[q] = SPLIT ? c0[q] + (c1[q] + c2[q]) : c0[q];
 }
 
 // Tile products of the step.  Warp w < TILES * KS owns tile w % TILES and
@@ -293,7 +296,7 @@ __device__ __forceinline__ void warp_tile_3xtf32(const float* __restrict__ pa,
 // epi(acc, m0, n0) receives each finished 16 x 8 tile.
 enum StepProd : int { kProdGram = 0, kProdTimes = 1 };
 
-template <int KP, int CL, int PROD, typename Epi>
+template <int KP, int CL, int PROD, bool SPLIT = true, typename Epi>
 __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const float* __restrict__ Bm,
                                            float* part, Epi&& epi) {
   using S = StepSmem<KP, CL>;
@@ -302,9 +305,9 @@ __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const fl
   auto product = [&](int tile, int kb, int ke, float (&acc)[4]) {
     const int m0 = (tile % S::MT) * 16, n0 = (tile / S::MT) * 8;
     if (PROD == kProdGram)
-      warp_tile_3xtf32<XLD, 1, 1, XLD>(X + m0 * XLD, Bm + n0 * XLD, kb, ke, acc);
+      warp_tile_3xtf32<XLD, 1, 1, XLD, SPLIT>(X + m0 * XLD, Bm + n0 * XLD, kb, ke, acc);
     else
-      warp_tile_3xtf32<1, XLD, 1, XLD>(X + m0, Bm + n0 * XLD, kb, ke, acc);
+      warp_tile_3xtf32<1, XLD, 1, XLD, SPLIT>(X + m0, Bm + n0 * XLD, kb, ke, acc);
   };
   if (S::KS == 2) {
     const int tile = warp % S::TILES, ks = warp / S::TILES;
@@ -455,25 +458,36 @@ __device__ float chol_blocked(float* A, int k, float* tinv, float* rd, float* dg
 #pragma unroll
       for (int b = 0; b < 8; ++b) A[(j0 + b) + c * XLD] = x[b];
     }
-    __syncthreads();
     // trailing update of the upper triangle, A(c, c') -= sum_b R(j0+b, c)
     // R(j0+b, c') for j0 + 8 <= c <= c'
     const int n0 = j0 + 8;
     if (warp == 0) {
-      // the next diagonal block, then its factorisation
-      for (int e = lane; e < 64; e += 32) {
-        const int i = e & 7, l = e >> 3;
-        if (i <= l) {
-          float sv = A[(n0 + i) + (n0 + l) * XLD];
+      // the next diagonal block needs only the block row's columns n0 ..
+      // n0+7, which lanes 0-7 of this warp formed: the other warps are
+      // released through barrier 2 (arrive: release), and this warp goes on
+      // with the diagonal block and its factorisation at once
+      asm volatile("bar.arrive 2, %0;" ::"r"(nw * 32) : "memory");
+      __syncwarp();
+      float sv[2];
 #pragma unroll
-          for (int b = 0; b < 8; ++b)
-            sv = fmaf(-A[(j0 + b) + (n0 + i) * XLD], A[(j0 + b) + (n0 + l) * XLD], sv);
-          A[(n0 + i) + (n0 + l) * XLD] = sv;
-        }
+      for (int h = 0; h < 2; ++h) {
+        const int e = lane + 32 * h, i = e & 7, l = e >> 3;
+        sv[h] = A[(n0 + i) + (n0 + l) * XLD];
+#pragma unroll
+        for (int b = 0; b < 8; ++b)
+          sv[h] = fmaf(-A[(j0 + b) + (n0 + i) * XLD], A[(j0 + b) + (n0 + l) * XLD], sv[h]);
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int e = lane + 32 * h, i = e & 7, l = e >> 3;
+        if (i <= l) A[(n0 + i) + (n0 + l) * XLD] = sv[h];
       }
       __syncwarp();
       if (lane == 0) rmin = fminf(rmin, factor_diag8<XLD>(A, n0, k, rd, dg));
-    } else if (rest > 8) {
+    } else {
+      asm volatile("bar.sync 2, %0;" ::"r"(nw * 32) : "memory");  // every block-row column
+    }
+    if (warp != 0 && rest > 8) {
       // columns c' >= n0 + 8 in 8-wide tiles, rows c in [n0, c'] in 16-row
       // tiles from mb; a last tile that would pass KP is computed at KP - 16
       // (rows below mb not written), so no read leaves the matrix
@@ -1022,7 +1036,10 @@ __device__ __forceinline__ void step_body(const StpmUpdateArgs& a) {
     if (lane == 0) s_emax[tid >> 5] = emax;
     __syncthreads();
     float* Otc = stage_next();
-    step_tiles<KP, CL, kProdTimes>(M, Ab, part, [&](const float (&acc)[4], int m0, int n0) {
+    // |F| is at most ~1e-5 here (an exact pass left M orthonormal to u times
+    // at most 1 / the pivot ratio bound), so a single TF32 product keeps
+    // M F to ~1e-9, below the FP32 resolution of Phi's entries
+    step_tiles<KP, CL, kProdTimes, false>(M, Ab, part, [&](const float (&acc)[4], int m0, int n0) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int r = m0 + g + ((q & 2) ? 8 : 0), jb = n0 + 2 * t4 + (q & 1), col = c0 + jb;
