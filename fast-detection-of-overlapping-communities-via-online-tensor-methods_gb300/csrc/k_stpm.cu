@@ -339,15 +339,17 @@ __device__ __forceinline__ void step_tiles(const float* __restrict__ X, const fl
 // A (KP x KP symmetric, column-major, leading dimension XLD, upper triangle
 // read) = R^T R with R upper triangular, blocked by 8 columns (right-looking,
 // one block of look-ahead).  Per block J: every thread forms one column of
-// the block row R_J = R_JJ^-T A_J by forward substitution; then warp 0
-// updates the next 8 x 8 diagonal block and one thread factors it in
-// registers (no shuffles on the pivot chain), while the other warps update
-// the rest of the trailing upper triangle with 3xTF32 tensor-core tiles
-// (a rank-8 update is one k-step).  R overwrites A's upper triangle, 1 / R_jj
-// goes to rd; the inverses T_JJ = R_JJ^-1 of the diagonal blocks (tinv, 8 x 8
-// column-major each) are formed afterwards, one block per thread, off the
-// pivot chain.  Rows and columns >= k must hold the identity (the caller
-// sets their diagonal to 1; X's padding columns are zero).
+// the block row R_J = R_JJ^-T A_J by forward substitution; then warp 0,
+// which formed the block row's first 8 columns itself, goes straight on to
+// update the next 8 x 8 diagonal block, and one thread factors it in
+// registers (no shuffles on the pivot chain), while the other warps wait at
+// a named barrier for the whole block row and update the rest of the
+// trailing upper triangle with 3xTF32 tensor-core tiles (a rank-8 update is
+// one k-step); one CTA barrier closes the block.  R overwrites A's upper
+// triangle, 1 / R_jj goes to rd; the inverses T_JJ = R_JJ^-1 of the diagonal
+// blocks (tinv, 8 x 8 column-major each) are formed afterwards, one block per
+// thread, off the pivot chain.  Rows and columns >= k must hold the identity
+// (the caller sets their diagonal to 1; X's padding columns are zero).
 
 // One thread: the (already updated) 8 x 8 diagonal block at (j0, j0).  A
 // pivot that is not above kPivotFloor * dg (breakdown, or NaN) is raised to
