@@ -131,6 +131,11 @@ __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
 // arrived.  A staging tile used for broadcast n is rewritten at broadcast
 // n + 2 only, after every receiver has waited for broadcast n + 1 (sent by
 // each rank after it received all of broadcast n).
+//
+// Hardware barriers of the step kernel's CTA: 0 = __syncthreads (whole CTA),
+// 1 = the four panel warps of inverse_columns (128 threads), 2 = the block-row
+// release of chol_blocked (warp 0 arrives, the other warps sync; whole CTA).
+// The three are never in use at the same time.
 
 // pivot ratio R_jj^2 / A_jj below which one more exact Cholesky QR pass runs
 // (one pass leaves Q1^T Q1 - I of about eps / ratio times a small constant, and
