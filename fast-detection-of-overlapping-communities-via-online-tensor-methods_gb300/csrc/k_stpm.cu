@@ -124,6 +124,7 @@ __global__ void stpm_reduce_kernel(StpmReduceArgs a) {
 // X^T Y[:, blk] (Gram) and X B_blk (times) run on the tensor cores as
 // warp-level m16n8k8 TF32 MMAs with the 3xTF32 split (a = a_hi + a_lo;
 // hi*hi + hi*lo + lo*hi accumulated in FP32, relative error ~1e-6 per
+// product; the first-order correction M F, |F| <= ~1e-5, as one TF32
 // product), one warp per 16 x 8 output tile.  A CTA's new column block is
 // staged in shared memory and sent to every CTA by bulk asynchronous copies
 // (cp.async.bulk shared::cta -> shared::cluster) that complete on the
