@@ -357,14 +357,22 @@ void pipeline_ydata(mmsb_ctx* c) {
   const double* mu_a = c->mu;
   const double* mu_b = c->mu + c->nA;
   const double* mu_c = c->mu + c->nA + c->nB;
-  // Wb_eff = Ub (Zb1^T W), Wc_eff = Uc (Zc1^T W)
+  // Wb_eff = Ub (Zb1^T W), Wc_eff = Uc (Zc1^T W).  The C side (its own
+  // Gram workspace) runs on the second stream beside the A and B sides.
+  cudaStream_t s2 = c->s2;
+  double* part2 = c->tbuf<double>("gram_part_y2", (size_t)cap);
+  double* ZW2 = c->tbuf<double>("ZW2", (size_t)k * k);
+  ck(cudaEventRecord(c->fork_ev, s), "fork");
+  ck(cudaStreamWaitEvent(s2, c->fork_ev, 0), "fork wait");
+  ck(gram_tsk(c->Zc1, ldk, k, c->W, ldk, k, c->nA, 1.0, ZW2, part2, cap, s2), "Zc1^T W");
+  ck(panel_times_small(c->Uc, ldk, k, c->nC, ZW2, k, k, Wc, ldk, s2), "Wc");
+  spmm(c, c->g[MMSB_BLOCK_XC], Wc, ldk, 1.f, c->y[2], s2);
+  ck(cudaEventRecord(c->join_ev, s2), "join");
   ck(gram_tsk(c->Zb1, ldk, k, c->W, ldk, k, c->nA, 1.0, ZW, part, cap, s), "Zb1^T W");
   ck(panel_times_small(c->Ub, ldk, k, c->nB, ZW, k, k, Wb, ldk, s), "Wb");
-  ck(gram_tsk(c->Zc1, ldk, k, c->W, ldk, k, c->nA, 1.0, ZW, part, cap, s), "Zc1^T W");
-  ck(panel_times_small(c->Uc, ldk, k, c->nC, ZW, k, k, Wc, ldk, s), "Wc");
   spmm(c, c->g[MMSB_BLOCK_XA], c->W, ldk, 1.f, c->y[0]);
   spmm(c, c->g[MMSB_BLOCK_XB], Wb, ldk, 1.f, c->y[1]);
-  spmm(c, c->g[MMSB_BLOCK_XC], Wc, ldk, 1.f, c->y[2]);
+  ck(cudaStreamWaitEvent(s, c->join_ev, 0), "join wait");
   // whitened means: W_P^T mu_P (mu as an n x 1 panel, ld 4)
   ck(colmajor64_to_panel(mu_a, c->nA, 1, c->nA, mu32, 4, s), "mu32a");
   ck(gram_tsk(c->W, ldk, k, mu32, 4, 1, c->nA, 1.0, c->ymu64, part, cap, s), "ymu_a");
