@@ -480,37 +480,50 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches, bool finish) {
   float* T3 = c->tbuf<float>("zc.T3", (size_t)c->nX * ldk);
   float* VL = c->tbuf<float>("VL", (size_t)nmax * ldk);
   double* Linv_sqrt = c->tbuf<double>("Linv_sqrt", (size_t)k);
-  // Z_C_part1 = Zc_num V_c diag(Linv_c), Zc_num = inv Gx_a^T Gx_b (Util.cpp:83-84)
-  ck(cudaMemcpyAsync(VL, Vc, sizeof(float) * c->nB * ldk, cudaMemcpyDeviceToDevice, s), "VL");
-  ck(panel_scale_cols(VL, ldk, c->nB, k, Linv_c, s), "Vc scale");
-  spmm(c, XB, VL, ldk, 1.f, T3);
-  spmm(c, XAt, T3, ldk, (float)inv, c->Zc1);
-  // Z_B_part1 = Zb_num V_b diag(Linv_b), Zb_num = inv Gx_a^T Gx_c (Util.cpp:96-97)
-  ck(cudaMemcpyAsync(VL, Vb, sizeof(float) * c->nC * ldk, cudaMemcpyDeviceToDevice, s), "VL");
-  ck(panel_scale_cols(VL, ldk, c->nC, k, Linv_b, s), "Vb scale");
-  spmm(c, XC, VL, ldk, 1.f, T3);
-  spmm(c, XAt, T3, ldk, (float)inv, c->Zb1);
-  // core = U_c^T Zc_den U_b = inv (Gx_c U_c)^T (Gx_b U_b)  (Util.cpp:90-94)
   float* T4 = c->tbuf<float>("T4", (size_t)c->nX * ldk);
   double* core = c->tbuf<double>("core", (size_t)k * k);
   const int64_t cap = (int64_t)gram_tsk_partials(nmax, std::max(k, p), p);
   double* part = c->tbuf<double>("gram_part_w", (size_t)cap);
-  spmm(c, XC, c->Uc, ldk, 1.f, T3);
-  spmm(c, XB, c->Ub, ldk, 1.f, T4);
-  ck(gram_tsk(T3, ldk, k, T4, ldk, k, c->nX, inv, core, part, cap, s), "core");
-  ck(diag_guard(k, core, s), "core guard");
-  // M2 sketch = (a0+1) Zc1 core (Zb1^T R_a) - a0 mu_a (mu_a^T R_a)  (Util.cpp:103-113),
-  // kept factored as M2 = [Zc1 | mu_a] B with B = [(a0+1) core Zb1^T R_a ; -a0 mu_a^T R_a]
-  // (rank <= k+1, so its Gram-Schmidt must see FP64 round-off, not FP32)
   const int m2 = k + 1, ldm2 = (int)round_up(m2, 4);
   double* Q1 = c->tbuf<double>("ZbR", (size_t)k * p);
   double* ma = c->tbuf<double>("muR", (size_t)p);
   double* Bm = c->tbuf<double>("M2B", (size_t)m2 * p);
   float* mu32 = c->tbuf<float>("mu32", (size_t)(c->nA + c->nB + c->nC) * 4);
   float* Am = c->tbuf<float>("M2A", (size_t)c->nA * ldm2);
-  ck(gram_tsk(c->Zb1, ldk, k, R[2], ldp, p, c->nA, 1.0, Q1, part, cap, s), "Zb1^T R");
-  ck(colmajor64_to_panel(c->mu, c->nA, 1, c->nA, mu32, 4, s), "mu32");
-  ck(gram_tsk(mu32, 4, 1, R[2], ldp, p, c->nA, 1.0, ma, part, cap, s), "mu^T R");
+  {
+    // the B side (Z_B_part1 and its sketch products) on the second stream,
+    // with the side's own panels and Gram workspace, beside the C side and
+    // the core on this one
+    cudaStream_t s2 = c->s2;
+    float* T3b = c->tbuf<float>("zb.T3", (size_t)c->nX * ldk);
+    float* VLb = c->tbuf<float>("zb.VL", (size_t)c->nC * ldk);
+    double* part2 = c->tbuf<double>("gram_part_w2", (size_t)cap);
+    ck(cudaEventRecord(c->fork_ev, s), "fork");
+    ck(cudaStreamWaitEvent(s2, c->fork_ev, 0), "fork wait");
+    // Z_B_part1 = Zb_num V_b diag(Linv_b), Zb_num = inv Gx_a^T Gx_c (Util.cpp:96-97)
+    ck(cudaMemcpyAsync(VLb, Vb, sizeof(float) * c->nC * ldk, cudaMemcpyDeviceToDevice, s2), "VL");
+    ck(panel_scale_cols(VLb, ldk, c->nC, k, Linv_b, s2), "Vb scale");
+    spmm(c, XC, VLb, ldk, 1.f, T3b, s2);
+    spmm(c, XAt, T3b, ldk, (float)inv, c->Zb1, s2);
+    ck(gram_tsk(c->Zb1, ldk, k, R[2], ldp, p, c->nA, 1.0, Q1, part2, cap, s2), "Zb1^T R");
+    ck(colmajor64_to_panel(c->mu, c->nA, 1, c->nA, mu32, 4, s2), "mu32");
+    ck(gram_tsk(mu32, 4, 1, R[2], ldp, p, c->nA, 1.0, ma, part2, cap, s2), "mu^T R");
+    ck(cudaEventRecord(c->join_ev, s2), "join");
+  }
+  // Z_C_part1 = Zc_num V_c diag(Linv_c), Zc_num = inv Gx_a^T Gx_b (Util.cpp:83-84)
+  ck(cudaMemcpyAsync(VL, Vc, sizeof(float) * c->nB * ldk, cudaMemcpyDeviceToDevice, s), "VL");
+  ck(panel_scale_cols(VL, ldk, c->nB, k, Linv_c, s), "Vc scale");
+  spmm(c, XB, VL, ldk, 1.f, T3);
+  spmm(c, XAt, T3, ldk, (float)inv, c->Zc1);
+  // core = U_c^T Zc_den U_b = inv (Gx_c U_c)^T (Gx_b U_b)  (Util.cpp:90-94)
+  spmm(c, XC, c->Uc, ldk, 1.f, T3);
+  spmm(c, XB, c->Ub, ldk, 1.f, T4);
+  ck(gram_tsk(T3, ldk, k, T4, ldk, k, c->nX, inv, core, part, cap, s), "core");
+  ck(diag_guard(k, core, s), "core guard");
+  ck(cudaStreamWaitEvent(s, c->join_ev, 0), "join wait");
+  // M2 sketch = (a0+1) Zc1 core (Zb1^T R_a) - a0 mu_a (mu_a^T R_a)  (Util.cpp:103-113),
+  // kept factored as M2 = [Zc1 | mu_a] B with B = [(a0+1) core Zb1^T R_a ; -a0 mu_a^T R_a]
+  // (rank <= k+1, so its Gram-Schmidt must see FP64 round-off, not FP32)
   ck(dgemm_small(false, false, k, p, k, c->cfg.alpha0 + 1.0, core, k, Q1, k, 0.0, Bm, m2, s), "B");
   ck(set_row_scaled(m2, p, Bm, m2, k, -c->cfg.alpha0, ma, s), "B shift row");
   ck(panel_copy(c->Zc1, ldk, c->nA, k, Am, ldm2, s), "A_M");
