@@ -180,9 +180,10 @@ namespace {
 //   Nystrom branch (n > 20k):  QQ = Q[0:p,:],  H = P QQ  (C = M QQ = Q_A H)
 //   thin-SVD branch:           H = P
 // The eigen-pairs (sigma^2, W) of H H^T give U = C V diag(1/sigma) = Q_A W
-// = A R_A^{-1} W and sigma.
+// = A R_A^{-1} W and sigma.  aux (optional, idle on entry): a second stream
+// for R2^{-1} and Q_A[0:p] while the Gram-Schmidt of R_A B runs on s.
 Nys svd_sym_nystrom(mmsb_ctx* c, const std::string& tag, const float* A, int lda, int m,
-                    const double* B, int64_t n, cudaStream_t s) {
+                    const double* B, int64_t n, cudaStream_t s, cudaStream_t aux = nullptr) {
   const int p = c->p, k = c->k, ldk = c->ldk;
   const double tol = c->cfg.pinv_tol;
   const int64_t cap = (int64_t)gram_tsk_partials(std::max<int64_t>(n, 1), m, m);
@@ -211,32 +212,42 @@ Nys svd_sym_nystrom(mmsb_ctx* c, const std::string& tag, const float* A, int lda
   ck(gram_tsk(Q1, ldq, m, Q1, ldq, m, n, 1.0, S2, part, cap, s, c->flags, c->wait_limit), "gram2");
   // S2 = Q1^T Q1 is close to I: its factor needs no more than FP32 (Q1 itself is FP32)
   ck(chol_upper_drop_f32(m, S2, m, R2, c->flags, s), "chol2");
-  ck(dgemm_small(false, false, m, m, m, 1.0, R2, m, R1, m, 0.0, RA, m, s), "R_A");
   // Q_A = Q1 R2^{-1} with R2 ~ I: products with Q_A use Q1 and T2 = R2^{-1}
   double* T2 = c->tbuf<double>(tag + ".T2", (size_t)m * m);
-  ck(trinv_upper(m, R2, T2, s), "R2^-1");
+  const bool nystrom = n > (int64_t)c->cfg.nystrom_rows_factor * k;
+  // QQ = Q[0:p, :] = Q_A[0:p, :] Q_small = Q1[0:p, :] R2^{-1} Q_small  (Spectral.cpp:185-188)
+  double* Ap = nystrom ? c->tbuf<double>(tag + ".Ap", (size_t)p * m) : nullptr;
+  double* QAp = nystrom ? c->tbuf<double>(tag + ".QAp", (size_t)p * m) : nullptr;
+  cudaStream_t st2 = aux ? aux : s;
+  if (aux) {
+    ck(cudaEventRecord(c->fork_ev, s), "fork");
+    ck(cudaStreamWaitEvent(aux, c->fork_ev, 0), "fork wait");
+  }
+  ck(trinv_upper(m, R2, T2, st2), "R2^-1");
+  if (nystrom) {
+    ck(panel_to_colmajor64(Q1, ldq, p, m, Ap, p, st2), "Q1[0:p]");
+    ck(dgemm_small(false, false, p, m, m, 1.0, Ap, p, T2, m, 0.0, QAp, p, st2), "Q_A[0:p]");
+  }
+  if (aux) ck(cudaEventRecord(c->join_ev, aux), "join");
+  ck(dgemm_small(false, false, m, m, m, 1.0, R2, m, R1, m, 0.0, RA, m, s), "R_A");
   // P = R_A B
   if (B)
     ck(dgemm_small(false, false, m, p, m, 1.0, RA, m, B, m, 0.0, P, m, s), "P");
   else
     ck(cudaMemcpyAsync(P, RA, sizeof(double) * m * p, cudaMemcpyDeviceToDevice, s), "P");
-  const bool nystrom = n > (int64_t)c->cfg.nystrom_rows_factor * k;
   if (nystrom) {
     double* Qs = c->tbuf<double>(tag + ".Qs", (size_t)m * p);
-    double* Ap = c->tbuf<double>(tag + ".Ap", (size_t)p * m);
-    double* QAp = c->tbuf<double>(tag + ".QAp", (size_t)p * m);
     double* QQ = c->tbuf<double>(tag + ".QQ", (size_t)p * p);
     if (B)
       ck(mgs_cols(m, p, P, m, Qs, m, tol, s), "mgs");
     else  // MGS of the upper-triangular R_A is the identity (zero where R_jj == 0)
       ck(eye_mask(m, p, P, m, Qs, m, s), "mgs(R)");
-    // QQ = Q[0:p, :] = Q_A[0:p, :] Q_small = Q1[0:p, :] R2^{-1} Q_small  (Spectral.cpp:185-188)
-    ck(panel_to_colmajor64(Q1, ldq, p, m, Ap, p, s), "Q1[0:p]");
-    ck(dgemm_small(false, false, p, m, m, 1.0, Ap, p, T2, m, 0.0, QAp, p, s), "Q_A[0:p]");
+    if (aux) ck(cudaStreamWaitEvent(s, c->join_ev, 0), "join wait");
     ck(dgemm_small(false, false, p, p, m, 1.0, QAp, p, Qs, m, 0.0, QQ, p, s), "QQ");
     ck(dgemm_small(false, false, m, p, p, 1.0, P, m, QQ, p, 0.0, Hm, m, s), "H");
   } else {
     ck(cudaMemcpyAsync(Hm, P, sizeof(double) * m * p, cudaMemcpyDeviceToDevice, s), "H");
+    if (aux) ck(cudaStreamWaitEvent(s, c->join_ev, 0), "join wait");
   }
   ck(dgemm_small(false, true, m, m, p, 1.0, Hm, m, Hm, m, 0.0, Zs, m, s), "H H^T");
   // Zs = H H^T.  The one-sided Jacobi runs on the Cholesky factor L of Zs
@@ -529,7 +540,7 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches, bool finish) {
   ck(panel_copy(c->Zc1, ldk, c->nA, k, Am, ldm2, s), "A_M");
   ck(panel_set_col(Am, ldm2, c->nA, k, c->mu, s), "A_M mu");
   // W = U_w diag(pinv(sqrt(sigma_w)))  (Util.cpp:116-123)
-  Nys nw = svd_sym_nystrom(c, "w", Am, ldm2, m2, Bm, c->nA, s);
+  Nys nw = svd_sym_nystrom(c, "w", Am, ldm2, m2, Bm, c->nA, s, c->s2);
   ck(sqrt_pinv(k, nw.sig, tol, nullptr, Linv_sqrt, s), "Lw");
   ck(cudaMemcpyAsync(c->W, nw.U, sizeof(float) * c->nA * ldk, cudaMemcpyDeviceToDevice, s), "W");
   ck(panel_scale_cols(c->W, ldk, c->nA, k, Linv_sqrt, s), "W scale");
