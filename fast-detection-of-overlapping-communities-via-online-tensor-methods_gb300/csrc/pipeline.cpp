@@ -137,7 +137,7 @@ void check_device_flags(mmsb_ctx* c, const char* stage) { check_flags(c, stage);
 // convergence from a converged FP32 start: 1e-7 -> 1e-14 -> FP64 round-off,
 // the third a margin).
 void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A, double* evals,
-                     double* V, const double* factor, cudaStream_t stream) {
+                     double* V, const double* factor, cudaStream_t stream, cudaStream_t aux) {
   cudaStream_t s = stream ? stream : c->s;
   double* R = c->tbuf<double>(tag + ".eR", (size_t)n * n);
   double* Y = c->tbuf<double>(tag + ".eY", (size_t)n * n);
@@ -159,9 +159,15 @@ void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A
   double* dstate = c->tbuf<double>(tag + ".edelta", 4);  // delta + three maxima
   ck(cudaMemsetAsync(dstate, 0, 4 * sizeof(double), s), "delta");
   for (int step = 0; step < 3; ++step) {
-    ck(dgemm_small(true, false, n, n, n, 1.0, X, n, X, n, 0.0, G, n, s), "X^T X");
+    if (aux) {
+      ck(cudaEventRecord(c->fork_ev, s), "fork");
+      ck(cudaStreamWaitEvent(aux, c->fork_ev, 0), "fork wait");
+    }
+    ck(dgemm_small(true, false, n, n, n, 1.0, X, n, X, n, 0.0, G, n, aux ? aux : s), "X^T X");
+    if (aux) ck(cudaEventRecord(c->join_ev, aux), "join");
     ck(dgemm_small(false, false, n, n, n, 1.0, A, n, X, n, 0.0, AX, n, s), "A X");
     ck(dgemm_small(true, false, n, n, n, 1.0, X, n, AX, n, 0.0, S, n, s), "X^T A X");
+    if (aux) ck(cudaStreamWaitEvent(s, c->join_ev, 0), "join wait");
     ck(oa_correction(n, A, G, S, E, lam, dstate, s), "oa");
     ck(cudaMemcpyAsync(X2, X, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, s), "copy");
     ck(dgemm_small(false, false, n, n, n, 1.0, X, n, E, n, 1.0, X2, n, s), "X + X E");
@@ -254,7 +260,7 @@ Nys svd_sym_nystrom(mmsb_ctx* c, const std::string& tag, const float* A, int lda
   // (L L^T = H H^T), not on H: L's columns are graded like the R factor of a
   // QR preconditioner, and the FP32 sweeps drop from ~13 to ~8 at p = 200,
   // more than paying for the FP64 Cholesky
-  sym_eig_refined(c, tag, m, Zs, ev, Wv, nullptr, s);
+  sym_eig_refined(c, tag, m, Zs, ev, Wv, nullptr, s, aux);
   // sigma = sqrt(ev_k); U = Q_A W_k diag(sigma > tol) = Q1 (R2^{-1} W_k) (masked)
   ck(sig_from_evals(k, ev, sig, s), "sig");
   ck(dgemm_small(false, false, m, k, m, 1.0, T2, m, Wv, m, 0.0, F, m, s), "F");
@@ -421,20 +427,30 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches, bool finish) {
   const int64_t nmax = std::max(std::max(c->nX, c->nA), std::max(c->nB, c->nC));
   float* R[3];
   const int64_t rn[3] = {c->nB, c->nC, c->nA};
-  for (int q = 0; q < 3; ++q) {
-    R[q] = c->tbuf<float>("R" + std::to_string(q), (size_t)rn[q] * ldp);
+  const bool upload = sketches && (sketches[0] || sketches[1] || sketches[2]);
+  // generated sketches: R[0] here and R[1] on the second stream as each side
+  // starts, R[2] and the means after side zc (the W step is their first
+  // reader); uploaded ones share one staging buffer, so all come first
+  for (int q = 0; q < 3; ++q) R[q] = c->tbuf<float>("R" + std::to_string(q), (size_t)rn[q] * ldp);
+  auto make_sketch = [&](int q, cudaStream_t st) {
     if (sketches && sketches[q]) {
       double* tmp = c->tbuf<double>("sketch_upload", (size_t)rn[q] * p);
-      ck(cudaMemcpyAsync(tmp, sketches[q], sizeof(double) * rn[q] * p, cudaMemcpyHostToDevice, s), "H2D sketch");
-      ck(colmajor64_to_panel(tmp, rn[q], p, rn[q], R[q], ldp, s), "sketch panel");
+      ck(cudaMemcpyAsync(tmp, sketches[q], sizeof(double) * rn[q] * p, cudaMemcpyHostToDevice, st), "H2D sketch");
+      ck(colmajor64_to_panel(tmp, rn[q], p, rn[q], R[q], ldp, st), "sketch panel");
     } else {
-      ck(gaussian_panel(R[q], rn[q], p, ldp, c->cfg.seed, 11 + q, s), "gaussian");
+      ck(gaussian_panel(R[q], rn[q], p, ldp, c->cfg.seed, 11 + q, st), "gaussian");
     }
-  }
+  };
   // partition means (Util.cpp:48-51): column sums of G_XP = row sums of G_XP^T
-  ck(row_sums_f64(XAt.rp, XAt.val, c->nA, inv, c->mu, s), "mu_a");
-  ck(row_sums_f64(XBt.rp, XBt.val, c->nB, inv, c->mu + c->nA, s), "mu_b");
-  ck(row_sums_f64(XCt.rp, XCt.val, c->nC, inv, c->mu + c->nA + c->nB, s), "mu_c");
+  auto means = [&]() {
+    ck(row_sums_f64(XAt.rp, XAt.val, c->nA, inv, c->mu, s), "mu_a");
+    ck(row_sums_f64(XBt.rp, XBt.val, c->nB, inv, c->mu + c->nA, s), "mu_b");
+    ck(row_sums_f64(XCt.rp, XCt.val, c->nC, inv, c->mu + c->nA + c->nB, s), "mu_c");
+  };
+  if (upload) {
+    for (int q = 0; q < 3; ++q) make_sketch(q, s);
+    means();
+  }
 
   double* Linv_c = c->tbuf<double>("Linv_c", (size_t)k);
   double* Linv_b = c->tbuf<double>("Linv_b", (size_t)k);
@@ -463,6 +479,10 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches, bool finish) {
   };
   ck(cudaEventRecord(c->fork_ev, s), "fork");
   ck(cudaStreamWaitEvent(c->s2, c->fork_ev, 0), "fork wait");
+  if (!upload) {
+    make_sketch(0, s);
+    make_sketch(1, c->s2);
+  }
   for (auto& sd : sides) {
     const std::string t = sd.tag;
     cudaStream_t st = sd.st;
@@ -485,6 +505,10 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches, bool finish) {
     ck(panel_scale_cols(VL, ldk, sd.n_in, k, Linv_sqrt, st), "VL scale");
     spmm(c, *sd.Gin, VL, ldk, 1.f, T3, st);
     spmm(c, *sd.Gout_t, T3, ldk, (float)inv, sd.U, st);
+  }
+  if (!upload) {  // after side zc on this stream
+    make_sketch(2, s);
+    means();
   }
   ck(cudaEventRecord(c->join_ev, c->s2), "join");
   ck(cudaStreamWaitEvent(s, c->join_ev, 0), "join wait");

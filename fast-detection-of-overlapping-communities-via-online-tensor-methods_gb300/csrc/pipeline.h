@@ -17,8 +17,11 @@ void ck(cudaError_t e, const char* what);
 // factor: optional Y with A = Y Y^T (skips the Cholesky)
 // Reads and clears the device flag word; throws on a set flag (stage names it).
 void check_device_flags(mmsb_ctx* c, const char* stage);
+// aux (optional, idle on entry): a second stream for X^T X beside A X and
+// X^T A X in each refinement step
 void sym_eig_refined(mmsb_ctx* c, const std::string& tag, int n, const double* A, double* evals,
-                     double* V, const double* factor = nullptr, cudaStream_t stream = nullptr);
+                     double* V, const double* factor = nullptr, cudaStream_t stream = nullptr,
+                     cudaStream_t aux = nullptr);
 
 void pipeline_upload(mmsb_ctx* c, const mmsb_csr* blocks);
 // finish == false leaves the device work queued on the context's streams;
