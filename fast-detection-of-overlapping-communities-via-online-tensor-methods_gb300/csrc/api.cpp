@@ -140,6 +140,8 @@ mmsb_status mmsb_create(const mmsb_config* cfg, mmsb_ctx** out) {
     ck(cudaSetDevice(cfg->device), "cudaSetDevice");
     ck(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "stream");
     ck(cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking), "stream");
+    ck(cudaStreamCreateWithFlags(&c->s3, cudaStreamNonBlocking), "stream");
+    ck(cudaStreamCreateWithFlags(&c->s4, cudaStreamNonBlocking), "stream");
     ck(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming), "event");
     ck(cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming), "event");
     for (auto& e : c->ev) ck(cudaEventCreate(&e), "event");

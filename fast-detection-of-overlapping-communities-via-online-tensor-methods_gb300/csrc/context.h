@@ -24,6 +24,7 @@ struct mmsb_ctx {
   cudaStream_t s = nullptr;
   // second stream: the two independent pseudo-inverse sides of the whitening
   cudaStream_t s2 = nullptr;
+  cudaStream_t s3 = nullptr, s4 = nullptr;  // helpers of the two whitening sides
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   std::string err;
   std::atomic<bool> stop{false};

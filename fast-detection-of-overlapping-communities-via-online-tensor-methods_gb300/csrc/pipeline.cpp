@@ -29,6 +29,8 @@ mmsb_ctx::~mmsb_ctx() {
     }
   if (fork_ev) cudaEventDestroy(fork_ev);
   if (join_ev) cudaEventDestroy(join_ev);
+  if (s4) cudaStreamDestroy(s4);
+  if (s3) cudaStreamDestroy(s3);
   if (s2) cudaStreamDestroy(s2);
   if (s) cudaStreamDestroy(s);
 }
@@ -472,10 +474,10 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches, bool finish) {
     float* U;
     double* Linv;
     const char* tag;
-    cudaStream_t st;
+    cudaStream_t st, aux;  // aux: the side's helper stream in its Nystrom step
   } sides[2] = {
-      {&XB, &XCt, &XC, &XBt, c->nB, c->nC, R[0], Vc, c->Uc, Linv_c, "zc", s},
-      {&XC, &XBt, &XB, &XCt, c->nC, c->nB, R[1], Vb, c->Ub, Linv_b, "zb", c->s2},
+      {&XB, &XCt, &XC, &XBt, c->nB, c->nC, R[0], Vc, c->Uc, Linv_c, "zc", s, c->s3},
+      {&XC, &XBt, &XB, &XCt, c->nC, c->nB, R[1], Vb, c->Ub, Linv_b, "zb", c->s2, c->s4},
   };
   ck(cudaEventRecord(c->fork_ev, s), "fork");
   ck(cudaStreamWaitEvent(c->s2, c->fork_ev, 0), "fork wait");
@@ -497,7 +499,7 @@ void pipeline_whiten(mmsb_ctx* c, const double* const* sketches, bool finish) {
     spmm(c, *sd.Gout_t, T1, ldp, (float)inv, XR, st);           // X R         (n_out x p)
     spmm(c, *sd.Gout, XR, ldp, 1.f, T1, st);                    // Gout XR     (n_X x p)
     spmm(c, *sd.Gin_t, T1, ldp, (float)inv, Gram, st);          // X^T X R     (n_in x p)
-    Nys ny = svd_sym_nystrom(c, sd.tag, Gram, ldp, p, nullptr, sd.n_in, st);  // V, sigma
+    Nys ny = svd_sym_nystrom(c, sd.tag, Gram, ldp, p, nullptr, sd.n_in, st, sd.aux);  // V, sigma
     ck(cudaMemcpyAsync(sd.V, ny.U, sizeof(float) * sd.n_in * ldk, cudaMemcpyDeviceToDevice, st), "V");
     // U = X V diag(sqrt(pinv(sigma)));  Linv = pinv(sqrt(sigma))  (Spectral.cpp:235-244, 307)
     ck(sqrt_pinv(k, ny.sig, tol, Linv_sqrt, sd.Linv, st), "Linv");
