@@ -13,7 +13,9 @@
  *     GPU/pre_proc.c:54-58) and 2 on library errors (GPU/pre_proc.c:96-109);
  *   - dense matrices are column-major, like Eigen's default and CULA;
  *   - all pointers passed to the API are HOST pointers; the library owns the
- *     device copies and one CUDA stream per context;
+ *     device copies and the CUDA streams of a context (a main stream, on
+ *     which every call's work is ordered, and helper streams that the
+ *     whitening forks from it and joins back before it returns);
  *   - a context is not thread-safe, except mmsb_request_stop();
  *   - graph blocks are CSR with int64 row offsets and int32 column indices,
  *     0-based (the text readers convert the reference's 1-based COO).
